@@ -1,0 +1,78 @@
+"""The workloads the path is measured and checked on.
+
+Each entry names the mesh, the activation field, the material (stated
+convention mu = E/(2(1+nu)), K = E/(3(1-2nu)) with E = 1, nu = 0.3), the
+quadrature (``-num_gaussian_quad_points``), the C33 sub-iteration count
+(``-C33_subitr_nums``), the follower pressure and the initial state.
+Seeds are SEED_BASE + config index.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import mesh as meshmod
+
+E_MOD = 1.0
+NU = 0.3
+MU = E_MOD / (2.0 * (1.0 + NU))
+BULK = E_MOD / (3.0 * (1.0 - 2.0 * NU))
+H0 = 0.01
+
+
+@dataclass(frozen=True)
+class Workload:
+    name: str
+    nx: int
+    ny: int
+    n_qp: int = 3
+    c33_iters: int = 3
+    pressure: float = 1e-4
+    z_sigma: float = 0.0
+    activation: str = "uniform"      # uniform | smooth | random
+    lambda_a: float = 0.9
+    disp_rel: float = 0.0            # displacement amplitude / edge length h
+    index: int = 0
+
+    @property
+    def seed(self) -> int:
+        return meshmod.SEED_BASE + self.index
+
+    @property
+    def n_elmt(self) -> int:
+        return 2 * self.nx * self.ny
+
+    def build_mesh(self) -> meshmod.Mesh:
+        m = meshmod.flat_membrane(self.nx, self.ny, z_sigma=self.z_sigma, seed=self.seed)
+        if self.activation == "uniform":
+            meshmod.set_uniform_activation(m, self.lambda_a)
+        elif self.activation == "smooth":
+            meshmod.set_smooth_activation(m)
+        elif self.activation == "random":
+            meshmod.set_random_activation(m, self.seed + 1)
+        else:
+            raise ValueError(self.activation)
+        m.meta["workload"] = self.name
+        return m
+
+    def initial_x(self, m: meshmod.Mesh, xyz0_full: np.ndarray) -> np.ndarray:
+        h = m.meta["lx"] / self.nx
+        return meshmod.initial_state(m, xyz0_full, disp_amp=self.disp_rel * h, seed=self.seed + 2)
+
+
+# C1: 32x24 cells (825 nodes, 1536 triangles), z perturbed N(0,1e-3), lambda_a 0.9 along e_x.
+C1 = Workload("C1_flat_32x24", 32, 24, z_sigma=1e-3, activation="uniform", lambda_a=0.9, index=0)
+# C2: 256x192 cells (49,665 nodes, 98,304 triangles), smooth lambda_a field, displacement 1e-2 h.
+C2 = Workload("C2_flat_256x192", 256, 192, activation="smooth", disp_rel=1e-2, index=1)
+# C3: 1024x768 cells (787,425 nodes, 1,572,864 triangles), random fibre angle and lambda_a.
+C3 = Workload("C3_flat_1024x768", 1024, 768, activation="random", index=2)
+
+ALL = {w.name: w for w in (C1, C2, C3)}
+
+
+def small(nx: int, ny: int, **kw) -> Workload:
+    """A small flat case for parity tests (z perturbed, smooth activation, displaced)."""
+    args = dict(z_sigma=1e-3, activation="smooth", disp_rel=1e-2, index=10)
+    args.update(kw)
+    return Workload(f"flat_{nx}x{ny}", nx, ny, **args)

@@ -1,0 +1,247 @@
+/*
+ * petsc-lite implementation (TEST INFRASTRUCTURE ONLY; see petscsys.h).
+ * One rank, host arrays, no threads.
+ */
+#include "petscsys.h"
+
+static int lite_verbose_(void) { return getenv("PETSC_LITE_VERBOSE") != NULL; }
+
+PetscErrorCode PetscLiteError_(PetscErrorCode code, const char *file, int line, const char *fmt, ...)
+{
+  va_list ap;
+  fprintf(stderr, "[petsc-lite] error %d at %s:%d: ", code, file, line);
+  va_start(ap, fmt);
+  vfprintf(stderr, fmt, ap);
+  va_end(ap);
+  fprintf(stderr, "\n");
+  return code;
+}
+
+PetscErrorCode PetscPrintf(MPI_Comm comm, const char *fmt, ...)
+{
+  (void)comm;
+  if (!lite_verbose_()) return 0;
+  va_list ap;
+  va_start(ap, fmt);
+  vfprintf(stderr, fmt, ap);
+  va_end(ap);
+  return 0;
+}
+
+PetscErrorCode PetscFPrintf(MPI_Comm comm, FILE *fd, const char *fmt, ...)
+{
+  (void)comm;
+  va_list ap;
+  va_start(ap, fmt);
+  vfprintf(fd ? fd : stderr, fmt, ap);
+  va_end(ap);
+  return 0;
+}
+
+PetscErrorCode PetscBarrier(void *obj) { (void)obj; return 0; }
+
+/* ---------------- options ---------------- */
+#define LITE_MAX_OPTS 128
+static char lite_opt_name_[LITE_MAX_OPTS][64];
+static char lite_opt_val_[LITE_MAX_OPTS][64];
+static int  lite_nopt_ = 0;
+
+void PetscLiteClearOptions(void) { lite_nopt_ = 0; }
+
+void PetscLiteSetOption(const char *name, const char *value)
+{
+  for (int i = 0; i < lite_nopt_; i++) {
+    if (strcmp(lite_opt_name_[i], name) == 0) {
+      snprintf(lite_opt_val_[i], sizeof(lite_opt_val_[i]), "%s", value);
+      return;
+    }
+  }
+  if (lite_nopt_ >= LITE_MAX_OPTS) return;
+  snprintf(lite_opt_name_[lite_nopt_], sizeof(lite_opt_name_[0]), "%s", name);
+  snprintf(lite_opt_val_[lite_nopt_], sizeof(lite_opt_val_[0]), "%s", value);
+  lite_nopt_++;
+}
+
+static const char *lite_find_(const char *name)
+{
+  for (int i = 0; i < lite_nopt_; i++)
+    if (strcmp(lite_opt_name_[i], name) == 0) return lite_opt_val_[i];
+  return NULL;
+}
+
+PetscErrorCode PetscOptionsGetInt(PetscOptions o, const char pre[], const char name[], PetscInt *v, PetscBool *set)
+{
+  (void)o; (void)pre;
+  const char *s = lite_find_(name);
+  if (s) *v = (PetscInt)strtol(s, NULL, 10);
+  if (set) *set = s ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+PetscErrorCode PetscOptionsGetReal(PetscOptions o, const char pre[], const char name[], PetscReal *v, PetscBool *set)
+{
+  (void)o; (void)pre;
+  const char *s = lite_find_(name);
+  if (s) *v = strtod(s, NULL);
+  if (set) *set = s ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+PetscErrorCode PetscOptionsGetBool(PetscOptions o, const char pre[], const char name[], PetscBool *v, PetscBool *set)
+{
+  (void)o; (void)pre;
+  const char *s = lite_find_(name);
+  if (s) *v = (s[0] == '1' || s[0] == 't' || s[0] == 'T' || s[0] == 'y') ? PETSC_TRUE : PETSC_FALSE;
+  if (set) *set = s ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+PetscErrorCode PetscOptionsGetString(PetscOptions o, const char pre[], const char name[], char *v, size_t len, PetscBool *set)
+{
+  (void)o; (void)pre;
+  const char *s = lite_find_(name);
+  if (s && len) snprintf(v, len, "%s", s);
+  if (set) *set = s ? PETSC_TRUE : PETSC_FALSE;
+  return 0;
+}
+
+/* ---------------- MPI at one rank ---------------- */
+int MPI_Comm_rank(MPI_Comm comm, PetscMPIInt *rank) { (void)comm; *rank = 0; return 0; }
+int MPI_Comm_size(MPI_Comm comm, PetscMPIInt *size) { (void)comm; *size = 1; return 0; }
+
+int MPI_Allreduce(const void *send, void *recv, int n, MPI_Datatype t, MPI_Op op, MPI_Comm comm)
+{
+  (void)op; (void)comm;
+  if (send != MPI_IN_PLACE && n > 0) memcpy(recv, send, (size_t)n * (size_t)t);
+  return 0;
+}
+
+int MPI_Reduce(const void *send, void *recv, int n, MPI_Datatype t, MPI_Op op, int root, MPI_Comm comm)
+{
+  (void)root;
+  return MPI_Allreduce(send, recv, n, t, op, comm);
+}
+
+int MPI_Bcast(void *buf, int n, MPI_Datatype t, int root, MPI_Comm comm)
+{
+  (void)buf; (void)n; (void)t; (void)root; (void)comm;
+  return 0;
+}
+
+PetscErrorCode PetscSortIntWithArray(PetscInt n, PetscInt keys[], PetscInt vals[])
+{
+  for (PetscInt i = 1; i < n; i++) {
+    PetscInt k = keys[i], v = vals[i], j = i - 1;
+    while (j >= 0 && keys[j] > k) { keys[j + 1] = keys[j]; vals[j + 1] = vals[j]; j--; }
+    keys[j + 1] = k; vals[j + 1] = v;
+  }
+  return 0;
+}
+
+/* ---------------- Vec ---------------- */
+PetscErrorCode VecCreateSeq(MPI_Comm c, PetscInt n, Vec *v)
+{
+  (void)c;
+  *v = (Vec)calloc(1, sizeof(**v));
+  (*v)->n = n;
+  (*v)->a = (PetscScalar *)calloc((size_t)(n > 0 ? n : 1), sizeof(PetscScalar));
+  return 0;
+}
+
+PetscErrorCode VecCreateMPI(MPI_Comm c, PetscInt nlocal, PetscInt N, Vec *v)
+{
+  return VecCreateSeq(c, N >= 0 ? N : nlocal, v);
+}
+
+PetscErrorCode VecDuplicate(Vec x, Vec *y) { return VecCreateSeq(0, x->n, y); }
+
+PetscErrorCode VecDestroy(Vec *v)
+{
+  if (v && *v) { free((*v)->a); free(*v); *v = NULL; }
+  return 0;
+}
+
+PetscErrorCode VecSet(Vec v, PetscScalar a)
+{
+  for (PetscInt i = 0; i < v->n; i++) v->a[i] = a;
+  return 0;
+}
+
+PetscErrorCode VecCopy(Vec x, Vec y) { memcpy(y->a, x->a, sizeof(PetscScalar) * (size_t)x->n); return 0; }
+PetscErrorCode VecGetArray(Vec v, PetscScalar **a) { *a = v->a; return 0; }
+PetscErrorCode VecRestoreArray(Vec v, PetscScalar **a) { (void)v; *a = NULL; return 0; }
+PetscErrorCode VecGetArrayRead(Vec v, const PetscScalar **a) { *a = v->a; return 0; }
+PetscErrorCode VecRestoreArrayRead(Vec v, const PetscScalar **a) { (void)v; *a = NULL; return 0; }
+
+PetscErrorCode VecSetValues(Vec v, PetscInt n, const PetscInt idx[], const PetscScalar y[], InsertMode m)
+{
+  for (PetscInt i = 0; i < n; i++) {
+    if (idx[i] < 0) continue;
+    if (idx[i] >= v->n) return PetscLiteError_(PETSC_ERR_ARG_OUTOFRANGE, __FILE__, __LINE__, "VecSetValues index %d >= %d", idx[i], v->n);
+    if (m == ADD_VALUES) v->a[idx[i]] += y[i]; else v->a[idx[i]] = y[i];
+  }
+  return 0;
+}
+
+PetscErrorCode VecAssemblyBegin(Vec v) { (void)v; return 0; }
+PetscErrorCode VecAssemblyEnd(Vec v) { (void)v; return 0; }
+
+PetscErrorCode VecNorm(Vec v, NormType t, PetscReal *r)
+{
+  PetscReal s = 0.0;
+  for (PetscInt i = 0; i < v->n; i++) {
+    PetscReal a = fabs(v->a[i]);
+    if (t == NORM_INFINITY) { if (a > s) s = a; }
+    else if (t == NORM_1) s += a;
+    else s += a * a;
+  }
+  *r = (t == NORM_2 || t == NORM_FROBENIUS) ? sqrt(s) : s;
+  return 0;
+}
+
+PetscErrorCode VecWAXPY(Vec w, PetscScalar a, Vec x, Vec y)
+{
+  for (PetscInt i = 0; i < w->n; i++) w->a[i] = a * x->a[i] + y->a[i];
+  return 0;
+}
+
+PetscErrorCode VecAXPY(Vec y, PetscScalar a, Vec x)
+{
+  for (PetscInt i = 0; i < y->n; i++) y->a[i] += a * x->a[i];
+  return 0;
+}
+
+PetscErrorCode VecScale(Vec x, PetscScalar a)
+{
+  for (PetscInt i = 0; i < x->n; i++) x->a[i] *= a;
+  return 0;
+}
+
+PetscErrorCode VecGetSize(Vec v, PetscInt *n) { *n = v->n; return 0; }
+PetscErrorCode VecGetOwnershipRange(Vec v, PetscInt *lo, PetscInt *hi) { *lo = 0; *hi = v->n; return 0; }
+
+#define LITE_UNSUPPORTED(name) \
+  return PetscLiteError_(PETSC_ERR_SUP, __FILE__, __LINE__, "%s is not part of petsc-lite", name)
+
+PetscErrorCode VecView(Vec v, PetscViewer w) { (void)v; (void)w; LITE_UNSUPPORTED("VecView"); }
+PetscErrorCode VecLoad(Vec v, PetscViewer w) { (void)v; (void)w; LITE_UNSUPPORTED("VecLoad"); }
+PetscErrorCode PetscViewerBinaryOpen(MPI_Comm c, const char name[], PetscFileMode m, PetscViewer *w)
+{ (void)c; (void)name; (void)m; (void)w; LITE_UNSUPPORTED("PetscViewerBinaryOpen"); }
+PetscErrorCode PetscViewerDestroy(PetscViewer *w) { (void)w; return 0; }
+PetscErrorCode PetscViewerBinaryGetDescriptor(PetscViewer w, int *fd) { (void)w; (void)fd; LITE_UNSUPPORTED("PetscViewerBinaryGetDescriptor"); }
+PetscErrorCode PetscBinaryWrite(int fd, const void *p, PetscInt n, PetscDataType t)
+{ (void)fd; (void)p; (void)n; (void)t; LITE_UNSUPPORTED("PetscBinaryWrite"); }
+PetscErrorCode PetscBinaryRead(int fd, void *p, PetscInt n, PetscInt *count, PetscDataType t)
+{ (void)fd; (void)p; (void)n; (void)count; (void)t; LITE_UNSUPPORTED("PetscBinaryRead"); }
+PetscErrorCode PetscRealView(PetscInt n, const PetscReal v[], PetscViewer w) { (void)n; (void)v; (void)w; LITE_UNSUPPORTED("PetscRealView"); }
+
+PetscErrorCode MatCreate(MPI_Comm c, Mat *m) { (void)c; (void)m; LITE_UNSUPPORTED("MatCreate"); }
+PetscErrorCode MatSetSizes(Mat m, PetscInt a, PetscInt b, PetscInt c, PetscInt d)
+{ (void)m; (void)a; (void)b; (void)c; (void)d; LITE_UNSUPPORTED("MatSetSizes"); }
+PetscErrorCode MatSetFromOptions(Mat m) { (void)m; LITE_UNSUPPORTED("MatSetFromOptions"); }
+PetscErrorCode MatSetType(Mat m, MatType t) { (void)m; (void)t; LITE_UNSUPPORTED("MatSetType"); }
+PetscErrorCode MatSetUp(Mat m) { (void)m; LITE_UNSUPPORTED("MatSetUp"); }
+PetscErrorCode MatZeroEntries(Mat m) { (void)m; LITE_UNSUPPORTED("MatZeroEntries"); }
+PetscErrorCode MatGetSize(Mat m, PetscInt *a, PetscInt *b) { (void)m; (void)a; (void)b; LITE_UNSUPPORTED("MatGetSize"); }
+PetscErrorCode MatCreateSeqDense(MPI_Comm c, PetscInt a, PetscInt b, PetscScalar *d, Mat *m)
+{ (void)c; (void)a; (void)b; (void)d; (void)m; LITE_UNSUPPORTED("MatCreateSeqDense"); }

@@ -1,0 +1,2 @@
+/* petsc-lite: forwards to petscsys.h (TEST INFRASTRUCTURE ONLY). */
+#include "petscsys.h"

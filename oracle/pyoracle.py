@@ -1,0 +1,166 @@
+"""ctypes bindings to the oracle libraries (TEST INFRASTRUCTURE ONLY).
+
+``Oracle``   -> oracle/_build/liboracle.so  (restated oracle, builds anywhere)
+``RefOracle`` -> oracle/_ref/libbiofem_ref.so (the reference's own C files;
+                 only where the reference sources exist)
+
+Both expose the same calls: setup(mesh, workload), topology(), residual(x).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_c_int, _c_dbl, _vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_vp)
+
+
+@dataclass
+class Topology:
+    patch: np.ndarray      # (n_elmt, 16) int32
+    ire: np.ndarray
+    val: np.ndarray
+    irv: np.ndarray
+    gtri: np.ndarray       # (n_elmt + 2 n_ghosts, 3)
+    xyz0_full: np.ndarray  # (n_v + n_ghosts, 3)
+    dA0: np.ndarray
+    ghost_nv3: np.ndarray | None = None
+
+
+class _Base:
+    lib: ctypes.CDLL
+    prefix: str
+
+    def _fn(self, name):
+        return getattr(self.lib, f"{self.prefix}_{name}")
+
+    def setup(self, mesh, w, mu: float, bulk: float, h0: float, gamma: float = 1.0, clamp: bool = True):
+        from_mesh = dict(
+            tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),
+            xyz=np.ascontiguousarray(mesh.xyz0, dtype=np.float64),
+            nb=np.ascontiguousarray(mesh.n_bnodes, dtype=np.int32),
+            bn=np.ascontiguousarray(mesh.bnodes, dtype=np.int32),
+            fib=np.ascontiguousarray(mesh.fib, dtype=np.float64),
+            gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64),
+        )
+        self._keep = from_mesh
+        f = self._fn("setup")
+        f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp,
+                      _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
+        rc = f(mesh.n_v, mesh.n_elmt, _p(from_mesh["tri"]), _p(from_mesh["xyz"]), mesh.n_edge,
+               _p(from_mesh["nb"]), _p(from_mesh["bn"]), _p(from_mesh["fib"]), _p(from_mesh["gs"]),
+               w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure, int(clamp))
+        if rc:
+            raise RuntimeError(f"{self.prefix}_setup failed with code {rc}")
+        ng, nd = _c_int(), _c_int()
+        self._fn("sizes")(ctypes.byref(ng), ctypes.byref(nd))
+        self.n_v, self.n_elmt = mesh.n_v, mesh.n_elmt
+        self.n_ghosts, self.n_dof = ng.value, nd.value
+        return self
+
+    def residual(self, x: np.ndarray, want_parts: bool = False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        R = np.zeros(self.n_dof)
+        Fi = np.zeros(self.n_dof)
+        Fe = np.zeros(self.n_dof)
+        rc = self._fn("residual")(_p(x), _p(R), _p(Fi), _p(Fe))
+        if rc:
+            raise RuntimeError(f"{self.prefix}_residual failed with code {rc}")
+        return (R, Fi, Fe) if want_parts else R
+
+
+class Oracle(_Base):
+    prefix = "oracle"
+
+    def __init__(self, build: bool = True):
+        from . import build_oracle  # type: ignore
+        path = build_oracle.build() if build else build_oracle.LIB
+        self.lib = ctypes.CDLL(str(path))
+
+    def set_threads(self, n: int):
+        self.lib.oracle_set_threads(int(n))
+
+    def topology(self) -> Topology:
+        ne, ng, nv = self.n_elmt, self.n_ghosts, self.n_v
+        t = Topology(np.zeros((ne, 16), np.int32), np.zeros(ne, np.int32), np.zeros(ne, np.int32),
+                     np.zeros(ne, np.int32), np.zeros((ne + 2 * ng, 3), np.int32),
+                     np.zeros((nv + ng, 3)), np.zeros(ne), np.zeros(ng, np.int32))
+        rc = self.lib.oracle_topology(_p(t.patch), _p(t.ire), _p(t.val), _p(t.irv), _p(t.gtri),
+                                      _p(t.xyz0_full), _p(t.dA0), _p(t.ghost_nv3))
+        if rc:
+            raise RuntimeError(rc)
+        return t
+
+    def jvp(self, x: np.ndarray, v: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        R = np.zeros(self.n_dof)
+        Jv = np.zeros(self.n_dof)
+        rc = self.lib.oracle_jvp(_p(x), _p(v), _p(R), _p(Jv))
+        if rc:
+            raise RuntimeError(rc)
+        return R, Jv
+
+    def jacobian_dense(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        J = np.zeros((self.n_dof, self.n_dof))  # filled column major -> transpose
+        rc = self.lib.oracle_jacobian_dense(_p(x), _p(J))
+        if rc:
+            raise RuntimeError(rc)
+        return J.T.copy()
+
+    def elem_state(self, x: np.ndarray, ec: int, n_qp: int):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        S = np.zeros((n_qp, 3, 3))
+        C33 = np.zeros(n_qp)
+        g = np.zeros((8, 3))
+        Fb = np.zeros(48)
+        rc = self.lib.oracle_elem_state(_p(x), int(ec), _p(S), _p(C33), _p(g), _p(Fb))
+        if rc:
+            raise RuntimeError(rc)
+        return S, C33, g, Fb
+
+    def irregular_weights(self, v: int) -> np.ndarray:
+        out = np.zeros(5 * (v + 6))
+        rc = self.lib.oracle_irregular_weights(int(v), _p(out))
+        if rc:
+            raise RuntimeError(rc)
+        return out.reshape(5, v + 6)
+
+
+class RefOracle(_Base):
+    prefix = "ref"
+
+    def __init__(self):
+        from . import build_ref  # type: ignore
+        path = build_ref.build()
+        if path is None:
+            raise FileNotFoundError("reference sources are not present on this host")
+        self.lib = ctypes.CDLL(str(path))
+
+    def topology(self) -> Topology:
+        ne, ng, nv = self.n_elmt, self.n_ghosts, self.n_v
+        t = Topology(np.zeros((ne, 16), np.int32), np.zeros(ne, np.int32), np.zeros(ne, np.int32),
+                     np.zeros(ne, np.int32), np.zeros((ne + 2 * ng, 3), np.int32),
+                     np.zeros((nv + ng, 3)), np.zeros(ne))
+        rc = self.lib.ref_topology(_p(t.patch), _p(t.ire), _p(t.val), _p(t.irv), _p(t.gtri),
+                                   _p(t.xyz0_full), _p(t.dA0))
+        if rc:
+            raise RuntimeError(rc)
+        return t
+
+    def elem_state(self, ec: int, n_qp: int):
+        S = np.zeros((n_qp, 3, 3))
+        C33 = np.zeros(n_qp)
+        g = np.zeros((8, 3))
+        rc = self.lib.ref_elem_state(int(ec), _p(S), _p(C33), _p(g))
+        if rc:
+            raise RuntimeError(rc)
+        return S, C33, g

@@ -1,0 +1,97 @@
+"""Pin the restated oracle (oracle/oracle.cpp) to the reference.
+
+The golden fixtures in tests/golden/ were produced by the reference's own C
+files (src/active_strain.c, bending.c, io.c, external.c, math.c compiled by
+oracle/build_ref.py; generator: tests/golden/make_golden.py).  The oracle must
+reproduce them BITWISE: topology tables (GlobalGhostInit/IrrVer/Patch) and the
+FormFunctionFEM residual.  Where the reference sources are present the tests
+also re-run the reference build live on fresh inputs.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from biofem import configs
+from biofem.configs import Workload
+
+FULL = sorted(p for p in GOLDEN.glob("*.npz") if "meta" in np.load(p) and "R" in np.load(p))
+
+
+def load_case(path):
+    d = np.load(path)
+    meta = json.loads(str(d["meta"]))
+    keys = ("name", "nx", "ny", "n_qp", "c33_iters", "pressure", "z_sigma", "activation",
+            "lambda_a", "disp_rel", "index")
+    w = Workload(**{k: meta[k] for k in keys})
+    return w, meta, d
+
+
+@pytest.mark.parametrize("path", FULL, ids=lambda p: p.stem)
+def test_oracle_matches_reference_golden(path, oracle_lib):
+    w, meta, d = load_case(path)
+    m = w.build_mesh()
+    o = oracle_lib.setup(m, w, meta["mu"], meta["bulk"], meta["h0"])
+    t = o.topology()
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        assert np.array_equal(getattr(t, k), d[k]), k
+    x = w.initial_x(m, t.xyz0_full)
+    assert np.array_equal(x, d["x"])
+    R, Fi, Fe = o.residual(x, want_parts=True)
+    assert np.array_equal(R, d["R"])
+    assert np.array_equal(Fi, d["Fint"])
+    assert np.array_equal(Fe, d["Fext"])
+    for k, ec in enumerate(d["sample_elems"]):
+        S, C33, g, _ = o.elem_state(x, int(ec), w.n_qp)
+        np.testing.assert_array_equal(S, d["sample_S"][k])
+        np.testing.assert_array_equal(C33, d["sample_C33"][k])
+        np.testing.assert_array_equal(g, d["sample_geom"][k])
+
+
+def test_golden_fixtures_present():
+    names = {p.stem for p in FULL}
+    assert "C1_flat_32x24" in names and len(names) >= 4
+
+
+def test_oracle_matches_live_reference(oracle_lib):
+    """Fresh shape/parameters not in the fixtures, against the live reference build."""
+    pytest.importorskip("oracle.build_ref")
+    from oracle import build_ref
+    if not build_ref.available():
+        pytest.skip("reference sources not on this host")
+    from oracle.pyoracle import RefOracle
+    w = configs.small(7, 9, n_qp=4, c33_iters=2, activation="random", index=21, pressure=5e-4)
+    m = w.build_mesh()
+    ref = RefOracle().setup(m, w, configs.MU, configs.BULK, configs.H0)
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0)
+    tr, to = ref.topology(), o.topology()
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        assert np.array_equal(getattr(tr, k), getattr(to, k)), k
+    x = w.initial_x(m, tr.xyz0_full)
+    assert np.array_equal(ref.residual(x), o.residual(x))
+
+
+def test_oracle_jvp_matches_central_differences(oracle_lib):
+    """The dual-number directional derivative is the tangent checker; it must
+    agree with central differences of the (bitwise-pinned) residual."""
+    w = configs.small(8, 6, index=22)
+    m = w.build_mesh()
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0)
+    x = w.initial_x(m, o.topology().xyz0_full)
+    v = np.random.default_rng(3).standard_normal(x.size)
+    _, Jv = o.jvp(x, v)
+    h = 1e-6
+    fd = (o.residual(x + h * v) - o.residual(x - h * v)) / (2 * h)
+    assert np.linalg.norm(fd - Jv) <= 1e-8 * np.linalg.norm(Jv)
+
+
+def test_oracle_dense_jacobian_consistent_with_jvp(oracle_lib):
+    w = configs.small(5, 4, index=23)
+    m = w.build_mesh()
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0)
+    x = w.initial_x(m, o.topology().xyz0_full)
+    J = o.jacobian_dense(x)
+    v = np.random.default_rng(4).standard_normal(x.size)
+    _, Jv = o.jvp(x, v)
+    np.testing.assert_allclose(J @ v, Jv, rtol=1e-12, atol=1e-14 * np.abs(Jv).max())
