@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the element residual + tangent + assembly path ("K+R assembly").
+
+One step = one evaluation of R(x) and K(x) = dR/dx of the whole mesh,
+assembled into the global vector and the 3x3-block CSR tangent, through the
+C-ABI (libbiofem_gpu.so).  Default workload: the 256x192-cell flat membrane
+(98,304 triangles, 3 thickness points, 3 C33 sub-iterations, follower
+pressure, clamped boundary ring), FP64.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  --impl reference times the reference's CPU
+algorithm (the restated oracle, oracle/oracle.cpp: the reference's element
+code with its tangent taken exactly by forward-mode dual numbers) on the
+host's cores for a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "biofem-ia_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
+UNIT = "elems/s"
+L2_FLUSH_BYTES = 256 << 20
+CPU_SAMPLE_ELEMS = 2048
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="C2_flat_256x192")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from biofem import configs
+    return configs.ALL[name]
+
+
+def algorithmic_bytes(info, topo, nnzb):
+    """Canonical algorithmic bytes of one R+K evaluation (FP64 K values):
+    4*sum(nen) patch ids + 2*24*(N_v+N_g) for x and X + 32*N_e fibre and
+    activation + 24*N_v residual + 72*nnzb tangent values."""
+    nen = np.where(topo["ire"] == 0, 12, topo["val"] + 6)
+    nt = info.n_v + info.n_ghosts
+    return int(4 * nen.sum() + 48 * nt + 32 * info.n_elmt + 24 * info.n_v + 72 * nnzb)
+
+
+def canonical_flops(n_elmt, n_qp):
+    """F_alg = q [2(3*3*m + m*m*3) + 2*m*3] per element, m = 36."""
+    m = 36
+    return n_elmt * n_qp * (2 * (9 * m + m * m * 3) + 2 * m * 3)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[4 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0):
+    """The reference's element algorithm on the host: R and element tangents
+    for a bounded element sample; returns elems/s.  The subdivision tables come
+    from the library's host builder (bitwise equal to the reference's)."""
+    from oracle.pyoracle import Oracle
+    from biofem import configs
+    o = Oracle().setup_given_topology(mesh, w, topo, configs.MU, configs.BULK, configs.H0)
+    x = np.ascontiguousarray(x_full)
+    chk = ctypes.c_double()
+    n_elems = min(n_elems, mesh.n_elmt)
+    # spread the sample over the mesh: a strided window of consecutive elements
+    e0 = max(0, mesh.n_elmt // 2 - n_elems // 2)
+    times = []
+    for s in range(warmup + steps):
+        t0 = time.perf_counter()
+        rc = o.lib.oracle_rk_sample(x.ctypes.data_as(ctypes.c_void_p), e0, e0 + n_elems, threads, ctypes.byref(chk))
+        dt = time.perf_counter() - t0
+        if rc:
+            raise RuntimeError(f"oracle_rk_sample failed: {rc}")
+        if s >= warmup:
+            times.append(dt)
+    return n_elems * len(times) / sum(times), sum(times), n_elems
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from biofem import configs
+    w = workload(args.workload)
+    mesh = w.build_mesh()
+    from biofem.gpu import GpuShell
+    host = GpuShell(mesh, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    topo = host.topology()
+    host.close()
+    x = w.initial_x(mesh, topo["xyz0_full"])
+    threads = os.cpu_count() or 1
+    sample = 1024
+    val, tot, n = cpu_rk(w, mesh, topo, x, sample, threads, steps=args.steps, warmup=args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded flat membrane)",
+        "config": {"workload": f"{w.name} R+K FP64 ({mesh.n_elmt} triangles, {w.n_qp} thickness points, "
+                               f"{w.c33_iters} C33 sub-iterations)", "sample_elements_per_step": n},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} consecutive elements of {w.name} per step: reference element algorithm "
+                                   f"(oracle/oracle.cpp, bitwise equal to the reference build) + exact element "
+                                   f"tangent by Dual<48> forward mode, OpenMP over elements"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from biofem import configs
+    from biofem.gpu import GpuShell, load_library
+    load_library()
+    w = workload(args.workload)
+    mesh = w.build_mesh()
+    sh = GpuShell(mesh, w, configs.MU, configs.BULK, configs.H0)
+    topo = sh.topology()
+    x_host = w.initial_x(mesh, topo["xyz0_full"])
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    dx = torch.tensor(x_host, device=dev)
+    dR = torch.empty_like(dx)
+    dK = torch.empty(9 * sh.nnzb, dtype=torch.float64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    n_launch_res, n_launch_jac = sh.launch_counts()
+
+    def step():
+        sh.jacobian_device(dx.data_ptr(), dR.data_ptr(), dK.data_ptr(), sp)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            step()
+        sh.sync(sp)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        clocks = ClockSampler(local)
+        clocks.start()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()                     # L2 flush between timed steps (outside the events)
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        sh.sync(sp)
+        clk = clocks.stop()
+        ms_steps = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        ms = sum(ms_steps) / args.steps
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+
+        # per-kernel durations (separate pass; the library records events between launches)
+        sh.kernel_timing(True)
+        for _ in range(args.steps):
+            flush.zero_()
+            step()
+        kms, calls = sh.kernel_times(n_launch_jac)
+        sh.kernel_timing(False)
+        kms = (kms / max(calls, 1)).tolist()
+
+        # residual-only step for reference
+        for _ in range(3):
+            sh.residual_device(dx.data_ptr(), dR.data_ptr(), sp)
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r_ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            r0.record(stream)
+            sh.residual_device(dx.data_ptr(), dR.data_ptr(), sp)
+            r1.record(stream)
+            r1.synchronize()
+            r_ms.append(r0.elapsed_time(r1))
+        sh.sync(sp)
+
+    # end to end through the public host API: pinned x in, R and K out
+    hx = torch.tensor(x_host).pin_memory()
+    hR = torch.empty(sh.n_dof, dtype=torch.float64).pin_memory()
+    hK = torch.empty(9 * sh.nnzb, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        sh.residual_jacobian_host_ptrs(hx.data_ptr(), hR.data_ptr(), hK.data_ptr())
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sh.residual_jacobian_host_ptrs(hx.data_ptr(), hR.data_ptr(), hK.data_ptr())
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    # consistency: the host call returns the same R as the device call
+    Rdev = dR.cpu().numpy()
+    sh.residual_host_ptrs(hx.data_ptr(), hR.data_ptr())
+    same = bool(np.array_equal(Rdev, hR.numpy()))
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    info = sh.info
+    ne = info.n_elmt
+    value = world * ne / (ms * 1e-3)
+    b_alg = algorithmic_bytes(info, topo, sh.nnzb)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    step_gbs = b_alg / (ms * 1e-3) / 1e9
+    names = ["positions", "elem_tangent", "node_gather", "block_gather", "scale"]
+    k_tan = kms[1]
+    f_alg = canonical_flops(ne, w.n_qp)
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        threads = os.cpu_count() or 1
+        cval, ctot, cn = cpu_rk(w, mesh, topo, x_host, CPU_SAMPLE_ELEMS, threads, steps=1, warmup=0)
+        cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{cn} consecutive elements of {w.name}: reference element algorithm (oracle/oracle.cpp, "
+                         f"bitwise equal to the reference build) + exact element tangent by Dual<48> forward mode, "
+                         f"{ctot:.1f} s"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flat membrane, row-alternating diagonals)",
+        "config": {"workload": f"{w.name} R+K FP64: {ne} triangles, {info.n_v} nodes, {info.n_ghosts} ghosts, "
+                               f"{w.n_qp} thickness points, {w.c33_iters} C33 sub-iterations, P={w.pressure}, "
+                               f"clamped ring; tangent 3x3-block CSR nnzb={sh.nnzb}",
+                   "l2": "flushed between timed steps (256 MiB device write outside the events)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": step_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": step_gbs / hbm_peak, "traffic": None,
+                     "peak_source": peak_src,
+                     "note": "achieved = canonical algorithmic bytes of one R+K step / step time; the step is "
+                             "FP64-pipe bound, see compute_roofline"},
+        "compute_roofline": {"kernel": "k_elem_tangent", "bound": "fp64", "kernel_ms": k_tan,
+                             "canonical_flops_per_step": f_alg,
+                             "achieved_tflops_canonical": f_alg / (k_tan * 1e-3) / 1e12,
+                             "peak_tflops": 1.25, "peak_source": "nominal GB300 FP64 (not measured)"},
+        "kernels_ms": dict(zip(names, kms)),
+        "residual_only": {"ms_per_step": sum(r_ms) / len(r_ms), "elems_per_s": ne / (sum(r_ms) / len(r_ms) * 1e-3)},
+        "e2e": {"value": world * ne / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * sh.n_dof,
+                "d2h_bytes_per_step": 8 * sh.n_dof + 72 * sh.nnzb, "host_equals_device_R": same},
+        "gpu_launches": n_launch_jac * args.steps,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

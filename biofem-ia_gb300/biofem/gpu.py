@@ -1,0 +1,256 @@
+"""Host-side mirror of BioFEM-IA's residual / Jacobian interface over the
+C-ABI in include/biofem_gpu.h (libbiofem_gpu.so, sm_103a).
+
+The reference evaluates R(x) inside its PETSc SNES callback
+``FormFunctionFEM(SNES, Vec x, Vec R, void *ctx)`` (main.c:757-1032) and
+never forms a Jacobian (matrix-free, main.c:464-466).  ``GpuShell`` holds one
+mesh resident on the GPU and offers the same call shapes on numpy arrays:
+
+    shell = GpuShell(mesh, workload)
+    R = shell.form_function(x)                 # FormFunctionFEM
+    R, K = shell.form_jacobian(x)              # new: K = dR/dx, 3x3-block CSR
+
+Errors come back as PETSc error numbers (``BiofemError.code``), as the
+reference's PetscCheck/SETERRQ would return them.  There is no CPU fallback:
+without the compiled library (or a GPU for the compute calls) every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parents[1]
+LIB_PATH = PKG / "lib" / "libbiofem_gpu.so"
+
+BIOFEM_FP64 = 0
+BIOFEM_FP32_BULK = 1
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+class BiofemError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"biofem error {code}: {msg}")
+        self.code = code
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("n_v", ctypes.c_int32), ("n_elmt", ctypes.c_int32), ("n_edge", ctypes.c_int32),
+                ("tri", _i32p), ("xyz0", _f64p), ("n_bnodes", _i32p), ("bnodes", _i32p),
+                ("n_fib", _f64p), ("gamma_scale", _f64p)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("n_qp", ctypes.c_int32), ("c33_subitr_nums", ctypes.c_int32), ("mu", ctypes.c_double),
+                ("bulk_modulus", ctypes.c_double), ("h0", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("pressure", ctypes.c_double), ("clamp_edge", ctypes.c_int32), ("precision", ctypes.c_int32)]
+
+
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("n_v", ctypes.c_int32), ("n_ghosts", ctypes.c_int32), ("n_elmt", ctypes.c_int32),
+                ("n_dof", ctypes.c_int32), ("n_irregular", ctypes.c_int32), ("nnzb", ctypes.c_int64),
+                ("n_contrib", ctypes.c_int64), ("device_bytes", ctypes.c_int64)]
+
+
+_LIB = None
+
+# every entry point the header declares (checked by tests/test_cabi.py)
+EXPORTS = ["InitGpuWorkspace", "DestroyGpuWorkspace", "PrepareGpuMesh", "DestroyGpuMesh", "GetGpuMeshInfo",
+           "GetGpuTopology", "GetGpuCsrPattern", "RunGpuResidual", "RunGpuResidualJacobian",
+           "RunGpuResidualDevice", "RunGpuResidualJacobianDevice", "BiofemGpuSync", "FormFunctionFEMGpu",
+           "FormJacobianFEMGpu", "GetGpuLaunchCounts", "BuildHostMesh", "DestroyHostMesh",
+           "GetGpuBasisTables", "BiofemGpuLastError", "EnableGpuKernelTiming", "GetGpuKernelTimes",
+           "GetGpuGhostMap"]
+
+
+def load_library(path: Path | str | None = None) -> ctypes.CDLL:
+    """Load libbiofem_gpu.so (built by __graft_entry__.build() /
+    biofem-ia_gb300/csrc/build.py).  Raises if it is missing."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is not built; run biofem-ia_gb300/csrc/build.py")
+    lib = ctypes.CDLL(str(p))
+    vp = ctypes.c_void_p
+    lib.BiofemGpuLastError.restype = ctypes.c_char_p
+    lib.PrepareGpuMesh.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(vp)]
+    lib.BuildHostMesh.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(vp)]
+    for name in ("DestroyGpuMesh", "DestroyHostMesh"):
+        getattr(lib, name).argtypes = [vp]
+    lib.GetGpuMeshInfo.argtypes = [vp, ctypes.POINTER(MeshInfo)]
+    lib.GetGpuTopology.argtypes = [vp] + [vp] * 7
+    lib.GetGpuCsrPattern.argtypes = [vp, vp, vp]
+    lib.GetGpuGhostMap.argtypes = [vp, vp]
+    lib.RunGpuResidual.argtypes = [vp, vp, vp]
+    lib.RunGpuResidualJacobian.argtypes = [vp, vp, vp, vp]
+    lib.RunGpuResidualDevice.argtypes = [vp, vp, vp, vp]
+    lib.RunGpuResidualJacobianDevice.argtypes = [vp, vp, vp, vp, vp]
+    lib.BiofemGpuSync.argtypes = [vp, vp]
+    lib.GetGpuLaunchCounts.argtypes = [vp, vp, vp]
+    lib.GetGpuBasisTables.argtypes = [vp]
+    lib.EnableGpuKernelTiming.argtypes = [vp, ctypes.c_int]
+    lib.GetGpuKernelTimes.argtypes = [vp, vp, ctypes.c_int32, vp]
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _check(lib, rc: int):
+    if rc:
+        raise BiofemError(rc, lib.BiofemGpuLastError().decode())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def basis_tables() -> np.ndarray:
+    """(11, 5, 16) centroid basis-derivative tables the kernels use."""
+    lib = load_library()
+    out = np.zeros(11 * 80)
+    _check(lib, lib.GetGpuBasisTables(_ptr(out)))
+    return out.reshape(11, 5, 16)
+
+
+class GpuShell:
+    """One mesh resident on the GPU (or, with host_only=True, only its host tables)."""
+
+    def __init__(self, mesh, workload, mu: float, bulk: float, h0: float, gamma: float = 1.0,
+                 clamp_edge: int = 0, precision: int = BIOFEM_FP64, host_only: bool = False):
+        self.lib = load_library()
+        self._arrays = dict(
+            tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),
+            xyz0=np.ascontiguousarray(mesh.xyz0, dtype=np.float64),
+            nb=np.ascontiguousarray(mesh.n_bnodes, dtype=np.int32),
+            bn=np.ascontiguousarray(mesh.bnodes, dtype=np.int32),
+            fib=np.ascontiguousarray(mesh.fib, dtype=np.float64),
+            gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64))
+        a = self._arrays
+        self.desc = MeshDesc(mesh.n_v, mesh.n_elmt, mesh.n_edge,
+                             a["tri"].ctypes.data_as(_i32p), a["xyz0"].ctypes.data_as(_f64p),
+                             a["nb"].ctypes.data_as(_i32p), a["bn"].ctypes.data_as(_i32p),
+                             a["fib"].ctypes.data_as(_f64p), a["gs"].ctypes.data_as(_f64p))
+        self.params = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure,
+                             clamp_edge, precision)
+        self.host_only = host_only
+        h = ctypes.c_void_p()
+        fn = self.lib.BuildHostMesh if host_only else self.lib.PrepareGpuMesh
+        _check(self.lib, fn(ctypes.byref(self.desc), ctypes.byref(self.params), ctypes.byref(h)))
+        self.handle = h
+        info = MeshInfo()
+        _check(self.lib, self.lib.GetGpuMeshInfo(self.handle, ctypes.byref(info)))
+        self.info = info
+        self.n_dof = info.n_dof
+        self.nnzb = info.nnzb
+
+    def close(self):
+        if self.handle:
+            (self.lib.DestroyHostMesh if self.host_only else self.lib.DestroyGpuMesh)(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- tables ----
+    def topology(self) -> dict:
+        i = self.info
+        ne, ng, nv = i.n_elmt, i.n_ghosts, i.n_v
+        t = dict(patch=np.zeros((ne, 16), np.int32), ire=np.zeros(ne, np.int32), val=np.zeros(ne, np.int32),
+                 irv=np.zeros(ne, np.int32), gtri=np.zeros((ne + 2 * ng, 3), np.int32),
+                 xyz0_full=np.zeros((nv + ng, 3)), dA0=np.zeros(ne))
+        _check(self.lib, self.lib.GetGpuTopology(self.handle, *(_ptr(t[k]) for k in
+                                                                ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"))))
+        g3 = np.zeros((ng, 3), np.int32)
+        _check(self.lib, self.lib.GetGpuGhostMap(self.handle, _ptr(g3)))
+        t["ghost3"] = g3
+        t["ghost_nv3"] = g3[:, 2].copy()
+        return t
+
+    def pattern(self):
+        rowptr = np.zeros(self.info.n_v + self.info.n_ghosts + 1, np.int32)
+        colind = np.zeros(self.nnzb, np.int32)
+        _check(self.lib, self.lib.GetGpuCsrPattern(self.handle, _ptr(rowptr), _ptr(colind)))
+        return rowptr, colind
+
+    def launch_counts(self):
+        r, j = ctypes.c_int32(), ctypes.c_int32()
+        _check(self.lib, self.lib.GetGpuLaunchCounts(self.handle, ctypes.byref(r), ctypes.byref(j)))
+        return r.value, j.value
+
+    # ---- FormFunctionFEM / Jacobian on host arrays ----
+    def form_function(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.size != self.n_dof:
+            raise BiofemError(63, f"x has {x.size} entries, expected {self.n_dof}")
+        R = np.empty(self.n_dof)
+        _check(self.lib, self.lib.RunGpuResidual(self.handle, _ptr(x), _ptr(R)))
+        return R
+
+    def form_jacobian(self, x: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.size != self.n_dof:
+            raise BiofemError(63, f"x has {x.size} entries, expected {self.n_dof}")
+        R = np.empty(self.n_dof)
+        K = np.empty((self.nnzb, 3, 3))
+        _check(self.lib, self.lib.RunGpuResidualJacobian(self.handle, _ptr(x), _ptr(R), _ptr(K)))
+        return R, K
+
+    # ---- device-resident calls (raw CUDA pointers as ints) ----
+    def residual_device(self, d_x: int, d_R: int, stream: int = 0):
+        """stream: a cudaStream_t handle as int (0 = the CUDA default stream)."""
+        _check(self.lib, self.lib.RunGpuResidualDevice(self.handle, ctypes.c_void_p(d_x), ctypes.c_void_p(d_R),
+                                                       ctypes.c_void_p(stream or None)))
+
+    def jacobian_device(self, d_x: int, d_R: int, d_K: int, stream: int = 0):
+        _check(self.lib, self.lib.RunGpuResidualJacobianDevice(self.handle, ctypes.c_void_p(d_x), ctypes.c_void_p(d_R),
+                                                               ctypes.c_void_p(d_K), ctypes.c_void_p(stream or None)))
+
+    def sync(self, stream: int = 0):
+        _check(self.lib, self.lib.BiofemGpuSync(self.handle, ctypes.c_void_p(stream or None)))
+
+    def kernel_timing(self, on: bool):
+        _check(self.lib, self.lib.EnableGpuKernelTiming(self.handle, int(on)))
+
+    def kernel_times(self, nslots: int = 5):
+        ms = np.zeros(nslots)
+        calls = ctypes.c_int32()
+        _check(self.lib, self.lib.GetGpuKernelTimes(self.handle, _ptr(ms), nslots, ctypes.byref(calls)))
+        return ms, calls.value
+
+    def residual_jacobian_host_ptrs(self, x_ptr: int, R_ptr: int, K_ptr: int):
+        """RunGpuResidualJacobian on caller-owned (e.g. pinned) host buffers."""
+        _check(self.lib, self.lib.RunGpuResidualJacobian(self.handle, ctypes.c_void_p(x_ptr), ctypes.c_void_p(R_ptr),
+                                                         ctypes.c_void_p(K_ptr)))
+
+    def residual_host_ptrs(self, x_ptr: int, R_ptr: int):
+        _check(self.lib, self.lib.RunGpuResidual(self.handle, ctypes.c_void_p(x_ptr), ctypes.c_void_p(R_ptr)))
+
+    # ---- helpers ----
+    def to_scipy(self, K: np.ndarray):
+        import scipy.sparse as sp
+        rowptr, colind = self.pattern()
+        nb = self.info.n_v + self.info.n_ghosts
+        return sp.bsr_matrix((K.reshape(-1, 3, 3), colind, rowptr), shape=(3 * nb, 3 * nb))
+
+
+def FormFunctionFEM(snes, x: np.ndarray, R: np.ndarray, ctx: GpuShell) -> int:
+    """SNES residual callback shape (main.c:120,757): fills R in place, returns 0."""
+    R[:] = ctx.form_function(x)
+    return 0
+
+
+def FormJacobianFEM(snes, x: np.ndarray, J: np.ndarray, P, ctx: GpuShell) -> int:
+    """SNES Jacobian callback shape (SNESSetJacobian slot, main.c:462-466):
+    fills the (nnzb, 3, 3) block values J in place, returns 0."""
+    _, K = ctx.form_jacobian(x)
+    J[...] = K
+    return 0

@@ -1,0 +1,84 @@
+/*
+ * Internal declarations shared by the host bridge, the topology builder and
+ * the CUDA kernels.  Not part of the C-ABI (include/biofem_gpu.h is).
+ */
+#ifndef BIOFEM_HOST_H
+#define BIOFEM_HOST_H
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/biofem_gpu.h"
+
+namespace biofem {
+
+constexpr int kMaxQp = 6;
+constexpr int kRefPerQp = 20;     /* FP64 reference constants per (element, qp) */
+constexpr int kRefPerElem = 4;    /* gamma, gamma', c1, pref0 */
+constexpr int kNumTables = 11;    /* 0 = regular 12-node patch, v = 3..10 irregular */
+
+/* Topology in IBMNodes layout (see topology.cpp). */
+struct HostTopo {
+  int n_v = 0, n_elmt = 0, n_ghosts = 0, n_edge = 0;
+  std::vector<int> tri_all;                        /* 3*(n_elmt + 2 n_ghosts) */
+  std::vector<int> ghost_nv1, ghost_nv2, ghost_nv3;/* per ghost: x_g = x_nv2 + x_nv1 - x_nv3 */
+  std::vector<int> ire, irv, val, patch;           /* patch: 16*n_elmt */
+  std::vector<double> xyz0_full;                   /* 3*(n_v + n_ghosts) */
+};
+
+int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err);
+
+/* Parameters every element kernel needs (passed by value). */
+struct KParams {
+  int ne, nt, nv, ng, nq, iters;
+  double mu, K, hhalf;
+  double theta[kMaxQp], w[kMaxQp];
+  double pressure;
+  double gamma;
+};
+
+/* Device views of one mesh handle. */
+struct DevMesh {
+  /* topology / per-element constants */
+  const int *patch;          /* 16*ne */
+  const int *einfo;          /* ne: nen | (table << 8) */
+  const int *ecorner;        /* ne: patch slots of nv1, nv2, nv3 (5 bits each) */
+  const double *eref;        /* (kRefPerQp*nq + kRefPerElem) * ne, SoA */
+  const double *ntab;        /* kNumTables * 5 * 16 basis-derivative tables */
+  const int *etri;           /* 3*ne triangle corners (pressure) */
+  const int *ghost3;         /* 3*ng (nv1, nv2, nv3) */
+  const long long *kofs;     /* ne: first Ke block of the element */
+  const double *X;           /* 3*nt reference positions (Vec layout) */
+  const unsigned char *rowkind; /* nt: 0 free real row, 1 clamped row, 2 ghost row */
+  /* residual gather lists */
+  const int *rptr, *ridx;    /* nt+1, into fb scratch (slot*3*ne + e) */
+  const int *pptr, *pidx;    /* nt+1, elements whose corner is the node */
+  /* tangent pattern + gather lists */
+  const int *rowptr, *colind, *blkrow;   /* BSR pattern; block -> row */
+  const long long *cptr;     /* nnzb+1 */
+  const int *cidx;           /* contribution: Ke block id, negative = subtract (-(id+1)) */
+  long long nnzb;
+  /* work arrays */
+  double *pos;               /* 4*nt padded positions */
+  double *fb;                /* 48*ne element forces */
+  double *fp;                /* 3*ne element pressure forces */
+  double *ke;                /* 9*total blocks element matrices */
+  int *status;               /* device error flag */
+  unsigned long long *fmax;  /* max |Fext| as ordered bits */
+};
+
+/* kernel launchers (kernels.cu); return cudaError_t as int */
+int launch_ref_prep(const DevMesh &m, const KParams &p, const double *fib, const double *gscale, double *eref_out, void *stream);
+int launch_positions(const DevMesh &m, const KParams &p, const double *x, void *stream);
+int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream);
+int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream);
+int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream);
+int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream);
+int launch_scale(const DevMesh &m, const KParams &p, double *R, double *K, void *stream);
+int upload_tables(double *d_ntab);
+void host_tables(double *out);   /* kNumTables*5*16 host copy of the basis tables */
+
+} /* namespace biofem */
+
+#endif

@@ -1,0 +1,683 @@
+/*
+ * C-ABI bridge (include/biofem_gpu.h): mesh handles, one-time setup and the
+ * residual / tangent entry points.  Replaces the reference's
+ * src/cuda_wrapper.cpp + the host half of src/cuda_kernel.cu: instead of a
+ * global workspace re-uploaded on every call, each mesh handle keeps its
+ * topology, reference geometry, assembly maps and work arrays resident in
+ * HBM; a call moves only x in and R (and K) out.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <set>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "biofem_host.h"
+
+namespace biofem {
+
+static std::string g_last_error;
+static std::mutex g_mu;
+static cudaStream_t g_stream = nullptr;
+static bool g_init = false;
+
+static int fail(int code, const std::string &msg)
+{
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                             \
+  do {                                                                                             \
+    cudaError_t e_ = (expr);                                                                       \
+    if (e_ != cudaSuccess) return fail(76, std::string(#expr) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+
+/* ---------------- basis-derivative tables ---------------- */
+/* Centroid derivatives of the 12 regular box-spline basis functions in the
+   reference's node ordering, four-decimal values (active_strain.c:69-88);
+   parity with the reference needs these exact constants. */
+static const double kNaC[2][12] = {
+  {-0.0247, -0.0309, 0.0000, -0.4815, -0.1852, 0.0247, 0.4815, 0.0000, -0.0062, 0.0309, 0.1852, 0.0062},
+  {-0.0309, -0.0247, -0.1852, -0.4815, 0.0000, -0.0062, 0.0000, 0.4815, 0.0247, 0.0062, 0.1852, 0.0309}};
+static const double kNabC[3][12] = {
+  {0.1111, 0.2222, -0.2222, -0.2222, 0.4444, 0.1111, -0.2222, -0.8889, 0.0000, 0.2222, 0.4444, 0.0000},
+  {0.2222, 0.1111, 0.4444, -0.2222, -0.2222, 0.0000, -0.8889, -0.2222, 0.1111, 0.0000, 0.4444, 0.2222},
+  {0.1667, 0.1667, -0.1111, 0.2222, -0.1111, -0.0556, -0.4444, -0.4444, -0.0556, 0.0556, 0.5556, 0.0556}};
+
+/* One Loop-subdivision step around an extraordinary vertex of valence v,
+   restricted to the rows the centroid evaluation reads.  Each rule is
+   (row = rb*v + ro, col = cb*v + co, weight), applied in order so that for
+   small v later rules overwrite earlier ones exactly as the reference's
+   assignment sequence does (active_strain.c:594-630). */
+struct SubdivRule { signed char rb, ro, cb, co; double wgt; signed char min_v; };
+static const SubdivRule kRules[] = {
+  /* edge points next to the extraordinary vertex */
+  {0, 1, 0, 0, 0.375, 0}, {0, 1, 0, 1, 0.375, 0}, {0, 1, 0, 2, 0.125, 0}, {0, 1, 1, 0, 0.125, 0},
+  {0, 2, 0, 0, 0.375, 0}, {0, 2, 0, 1, 0.125, 0}, {0, 2, 0, 2, 0.375, 0}, {0, 2, 0, 3, 0.125, 0},
+  {1, -4, 0, 0, 0.375, 6}, {1, -4, 1, -5, 0.125, 6}, {1, -4, 1, -4, 0.375, 6}, {1, -4, 1, -3, 0.125, 6},
+  {1, -3, 0, 0, 0.375, 5}, {1, -3, 1, -4, 0.125, 5}, {1, -3, 1, -3, 0.375, 5}, {1, -3, 1, -2, 0.125, 5},
+  {1, -2, 0, 0, 0.375, 0}, {1, -2, 1, -3, 0.125, 0}, {1, -2, 1, -2, 0.375, 0}, {1, -2, 1, -1, 0.125, 0},
+  {1, -1, 0, 0, 0.375, 0}, {1, -1, 1, -2, 0.125, 0}, {1, -1, 1, -1, 0.375, 0}, {1, -1, 1, 0, 0.125, 0},
+  {1, 0, 0, 0, 0.375, 0}, {1, 0, 0, 1, 0.125, 0}, {1, 0, 1, -1, 0.125, 0}, {1, 0, 1, 0, 0.375, 0},
+  /* the second ring */
+  {1, 1, 0, 0, 0.125, 0}, {1, 1, 0, 1, 0.375, 0}, {1, 1, 1, 0, 0.375, 0}, {1, 1, 1, 1, 0.125, 0},
+  {1, 2, 0, 0, 0.0625, 0}, {1, 2, 0, 1, 0.625, 0}, {1, 2, 0, 2, 0.0625, 0}, {1, 2, 1, 0, 0.0625, 0},
+  {1, 2, 1, 1, 0.0625, 0}, {1, 2, 1, 2, 0.0625, 0}, {1, 2, 1, 3, 0.0625, 0},
+  {1, 3, 0, 0, 0.125, 0}, {1, 3, 0, 1, 0.375, 0}, {1, 3, 0, 2, 0.375, 0}, {1, 3, 1, 3, 0.125, 0},
+  {1, 4, 0, 0, 0.0625, 0}, {1, 4, 0, 1, 0.0625, 0}, {1, 4, 1, -1, 0.0625, 0}, {1, 4, 1, 0, 0.625, 0},
+  {1, 4, 1, 1, 0.0625, 0}, {1, 4, 1, 4, 0.0625, 0}, {1, 4, 1, 5, 0.0625, 0},
+  {1, 5, 0, 0, 0.125, 0}, {1, 5, 1, -1, 0.375, 0}, {1, 5, 1, 0, 0.375, 0}, {1, 5, 1, 5, 0.125, 0},
+  {1, 6, 0, 1, 0.375, 0}, {1, 6, 1, 0, 0.125, 0}, {1, 6, 1, 1, 0.375, 0}, {1, 6, 1, 2, 0.125, 0},
+  {1, 9, 0, 1, 0.125, 0}, {1, 9, 1, 0, 0.375, 0}, {1, 9, 1, 1, 0.375, 0}, {1, 9, 1, 4, 0.125, 0},
+};
+
+/* rows of the refined net that form the regular 12-node sub-patch holding
+   the centroid, in regular-patch order (active_strain.c:608-610) */
+static void subpatch_rows(int v, int rows[12])
+{
+  const int r[12] = {v + 9, v + 6, v + 4, v + 1, v + 2, v + 5, v, 1, v + 3, v - 1, 0, 2};
+  for (int i = 0; i < 12; i++) rows[i] = r[i];
+}
+
+void host_tables(double *out)
+{
+  std::fill(out, out + kNumTables * 80, 0.0);
+  for (int i = 0; i < 12; i++) {
+    out[0 * 16 + i] = kNaC[0][i]; out[1 * 16 + i] = kNaC[1][i];
+    out[2 * 16 + i] = kNabC[0][i]; out[3 * 16 + i] = kNabC[1][i]; out[4 * 16 + i] = kNabC[2][i];
+  }
+  const double pi = 3.14159265358979323846264338327950288419716939937510582;
+  for (int v = 3; v < kNumTables; v++) {
+    const int nen = v + 6, nr = v + 12;
+    std::vector<double> B((size_t)nr * nen, 0.0);
+    /* Loop's vertex rule, weight w(v) = (5/8 - (3/8 + cos(2 pi / v)/4)^2) / v */
+    const double w = (1.0 / (double)v) * (0.625 - std::pow(0.375 + 0.25 * std::cos(2 * pi / (double)v), 2.0));
+    B[0] = 1 - v * w;
+    for (int j = 0; j < v; j++) B[1 + j] = w;
+    for (const SubdivRule &r : kRules) {
+      if (r.min_v && v < r.min_v) continue;
+      const int row = r.rb * v + r.ro, col = r.cb * v + r.co;
+      if (row < 0 || row >= nr || col < 0 || col >= nen) continue;
+      B[(size_t)row * nen + col] = r.wgt;
+    }
+    int rows[12];
+    subpatch_rows(v, rows);
+    const double *Nrow[5] = {kNaC[0], kNaC[1], kNabC[0], kNabC[1], kNabC[2]};
+    const double scale[5] = {-2.0, -2.0, 4.0, 4.0, 4.0};
+    for (int rr = 0; rr < 5; rr++)
+      for (int j = 0; j < nen; j++) {
+        double s = 0.0;
+        for (int i = 0; i < 12; i++) s = s + B[(size_t)rows[i] * nen + j] * Nrow[rr][i];
+        out[v * 80 + rr * 16 + j] = scale[rr] * s;
+      }
+  }
+}
+
+} /* namespace biofem */
+
+using namespace biofem;
+
+/* optional per-kernel timing of the device calls (events on the call's stream) */
+static const int kMaxTimed = 8;
+struct KernelTimer {
+  bool on = false;
+  int n = 0;
+  cudaEvent_t ev[kMaxTimed + 1] = {};
+  float acc_ms[kMaxTimed] = {};
+  int calls = 0;
+};
+
+/* ---------------- the mesh handle ---------------- */
+struct BiofemGpuMesh_ {
+  HostTopo topo;
+  BiofemParams prm{};
+  KParams kp{};
+  std::vector<double> dA0;
+  std::vector<int> rowptr, colind;
+  long long nnzb = 0, ncontrib = 0;
+  int n_irregular = 0;
+  size_t bytes = 0;
+  std::vector<void *> allocs;
+  DevMesh dm{};
+  double *d_x = nullptr, *d_R = nullptr, *d_K = nullptr;   /* staging for host-array calls */
+  KernelTimer timer;
+};
+
+static std::set<BiofemGpuMesh *> g_meshes;
+static KernelTimer &timer_of(BiofemGpuMesh *m) { return m->timer; }
+
+/* device-variant stream argument: a cudaStream_t; NULL is the CUDA default stream */
+static inline cudaStream_t pick_stream(void *s) { return (cudaStream_t)s; }
+
+static inline void tmark(BiofemGpuMesh *m, cudaStream_t st, int i)
+{
+  KernelTimer &t = timer_of(m);
+  if (t.on && i <= kMaxTimed) { cudaEventRecord(t.ev[i], st); t.n = i; }
+}
+
+template <class T>
+static int dalloc(BiofemGpuMesh *m, T **p, size_t n)
+{
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess) return fail(55, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  m->allocs.push_back(q);
+  m->bytes += std::max<size_t>(n, 1) * sizeof(T);
+  *p = reinterpret_cast<T *>(q);
+  return 0;
+}
+
+template <class T>
+static int dupload(BiofemGpuMesh *m, T **p, const std::vector<T> &h)
+{
+  int rc = dalloc(m, p, h.size());
+  if (rc) return rc;
+  if (!h.empty()) CUDA_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+static void free_mesh(BiofemGpuMesh *m)
+{
+  for (int i = 0; i <= kMaxTimed; i++) if (m->timer.ev[i]) cudaEventDestroy(m->timer.ev[i]);
+  for (void *p : m->allocs) cudaFree(p);
+  m->allocs.clear();
+  delete m;
+}
+
+/* Host-side build of every map; no CUDA calls (usable without a GPU). */
+static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const BiofemParams &prm,
+                           std::vector<int> &einfo, std::vector<int> &ecorner, std::vector<long long> &kofs, std::vector<unsigned char> &rowkind,
+                           std::vector<int> &rptr, std::vector<int> &ridx, std::vector<int> &pptr, std::vector<int> &pidx,
+                           std::vector<int> &blkrow, std::vector<long long> &cptr, std::vector<int> &cidx)
+{
+  std::string err;
+  int rc = build_topology(d, m->topo, err);
+  if (rc) return fail(rc, err);
+  const HostTopo &T = m->topo;
+  const int ne = T.n_elmt, nv = T.n_v, ng = T.n_ghosts, nt = nv + ng;
+  if (prm.clamp_edge >= d.n_edge) return fail(63, "clamp_edge beyond the number of boundary rings");
+
+  einfo.assign(ne, 0);
+  ecorner.assign(ne, 0);
+  kofs.assign(ne, 0);
+  long long acc = 0;
+  m->n_irregular = 0;
+  for (int e = 0; e < ne; e++) {
+    const int nen = T.ire[e] ? T.val[e] + 6 : 12;
+    const int tab = T.ire[e] ? T.val[e] : 0;
+    if (T.ire[e]) m->n_irregular++;
+    einfo[e] = nen | (tab << 8);
+    /* patch slots holding the triangle's corners (first occurrence) */
+    int packed = 0;
+    for (int k = 0; k < 3; k++) {
+      const int node = T.tri_all[3 * (size_t)e + k];
+      int slot = -1;
+      for (int a = 0; a < nen && slot < 0; a++) if (T.patch[16 * (size_t)e + a] == node) slot = a;
+      if (slot < 0) return fail(77, "a triangle corner is missing from its own patch");
+      packed |= slot << (5 * k);
+    }
+    ecorner[e] = packed;
+    kofs[e] = acc;
+    acc += (long long)nen * nen;
+  }
+  if (acc >= (1LL << 31)) return fail(63, "element-matrix scratch exceeds the int32 block index");
+
+  rowkind.assign(nt, 0);
+  for (int g = nv; g < nt; g++) rowkind[g] = 2;
+  if (prm.clamp_edge >= 0) {
+    int start = 0;
+    for (int r = 0; r < prm.clamp_edge; r++) start += d.n_bnodes[r];
+    for (int i = 0; i < d.n_bnodes[prm.clamp_edge]; i++) rowkind[d.bnodes[start + i]] = 1;
+  }
+
+  /* residual gather lists: (element, slot) in element order for real rows */
+  rptr.assign(nt + 1, 0);
+  for (int e = 0; e < ne; e++) {
+    const int nen = einfo[e] & 0xff;
+    for (int a = 0; a < nen; a++) {
+      const int node = T.patch[16 * (size_t)e + a];
+      if (node < nv) rptr[node + 1]++;
+    }
+  }
+  for (int i = 0; i < nt; i++) rptr[i + 1] += rptr[i];
+  ridx.assign(rptr[nt], 0);
+  {
+    std::vector<int> fill(rptr.begin(), rptr.end() - 1);
+    for (int e = 0; e < ne; e++) {
+      const int nen = einfo[e] & 0xff;
+      for (int a = 0; a < nen; a++) {
+        const int node = T.patch[16 * (size_t)e + a];
+        if (node < nv) ridx[fill[node]++] = (int)((long long)3 * a * ne + e);
+      }
+    }
+  }
+  /* pressure gather lists: element corners */
+  pptr.assign(nt + 1, 0);
+  if (prm.pressure != 0.0) {
+    for (int e = 0; e < ne; e++) for (int k = 0; k < 3; k++) pptr[T.tri_all[3 * (size_t)e + k] + 1]++;
+  }
+  for (int i = 0; i < nt; i++) pptr[i + 1] += pptr[i];
+  pidx.assign(pptr[nt], 0);
+  if (prm.pressure != 0.0) {
+    std::vector<int> fill(pptr.begin(), pptr.end() - 1);
+    for (int e = 0; e < ne; e++) for (int k = 0; k < 3; k++) pidx[fill[T.tri_all[3 * (size_t)e + k]]++] = e;
+  }
+
+  /* column expansion of a patch slot: real node, or the ghost's parents */
+  auto expand = [&](int node, int cols[3], int sg[3]) -> int {
+    if (node < nv) { cols[0] = node; sg[0] = 1; return 1; }
+    const int g = node - nv;
+    cols[0] = T.ghost_nv2[g]; sg[0] = 1;
+    cols[1] = T.ghost_nv1[g]; sg[1] = 1;
+    cols[2] = T.ghost_nv3[g]; sg[2] = -1;
+    return 3;
+  };
+
+  /* BSR pattern */
+  m->rowptr.assign(nt + 1, 0);
+  std::vector<std::vector<int>> rows_tmp;  /* built row by row below */
+  std::vector<int> mark(nt, -1);
+  std::vector<int> cols_acc;
+  m->colind.clear();
+  for (int i = 0; i < nt; i++) {
+    cols_acc.clear();
+    if (rowkind[i] != 0) {
+      cols_acc.push_back(i);
+    } else {
+      cols_acc.push_back(i);
+      mark[i] = i;
+      for (int c = rptr[i]; c < rptr[i + 1]; c++) {
+        const int e = ridx[c] % ne;
+        const int nen = einfo[e] & 0xff;
+        for (int b = 0; b < nen; b++) {
+          int cols[3], sg[3];
+          const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
+          for (int q = 0; q < k; q++)
+            if (mark[cols[q]] != i) { mark[cols[q]] = i; cols_acc.push_back(cols[q]); }
+        }
+      }
+      std::sort(cols_acc.begin(), cols_acc.end());
+    }
+    m->colind.insert(m->colind.end(), cols_acc.begin(), cols_acc.end());
+    m->rowptr[i + 1] = (int)m->colind.size();
+  }
+  m->nnzb = (long long)m->colind.size();
+  blkrow.assign(m->nnzb, 0);
+  for (int i = 0; i < nt; i++) for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) blkrow[k] = i;
+
+  /* element-block -> tangent-block contributions, element order */
+  auto find_blk = [&](int i, int j) -> long long {
+    const int *b = m->colind.data() + m->rowptr[i], *en = m->colind.data() + m->rowptr[i + 1];
+    const int *p = std::lower_bound(b, en, j);
+    return (p != en && *p == j) ? (long long)(p - m->colind.data()) : -1;
+  };
+  cptr.assign(m->nnzb + 1, 0);
+  for (int pass = 0; pass < 2; pass++) {
+    std::vector<long long> fill;
+    if (pass == 1) {
+      for (long long k = 0; k < m->nnzb; k++) cptr[k + 1] += cptr[k];
+      m->ncontrib = cptr[m->nnzb];
+      if (m->ncontrib >= (1LL << 31)) return fail(63, "assembly map exceeds int32");
+      cidx.assign(m->ncontrib, 0);
+      fill.assign(cptr.begin(), cptr.end() - 1);
+    }
+    for (int e = 0; e < ne; e++) {
+      const int nen = einfo[e] & 0xff;
+      for (int a = 0; a < nen; a++) {
+        const int i = T.patch[16 * (size_t)e + a];
+        if (i >= nv || rowkind[i] != 0) continue;
+        for (int b = 0; b < nen; b++) {
+          int cols[3], sg[3];
+          const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
+          const long long blk_id = kofs[e] + (long long)a * nen + b;
+          for (int q = 0; q < k; q++) {
+            const long long kb = find_blk(i, cols[q]);
+            if (kb < 0) return fail(77, "tangent pattern is missing an element block");
+            if (pass == 0) cptr[kb + 1]++;
+            else cidx[fill[kb]++] = sg[q] > 0 ? (int)blk_id : (int)(-(blk_id + 1));
+          }
+        }
+      }
+    }
+  }
+  /* dA0 on the host too (GetGpuTopology); same expression as AreaNormal */
+  m->dA0.assign(ne, 0.0);
+  for (int e = 0; e < ne; e++) {
+    const double *X = T.xyz0_full.data();
+    const int a = T.tri_all[3 * (size_t)e], b = T.tri_all[3 * (size_t)e + 1], c = T.tri_all[3 * (size_t)e + 2];
+    const double d21[3] = {X[3 * b] - X[3 * a], X[3 * b + 1] - X[3 * a + 1], X[3 * b + 2] - X[3 * a + 2]};
+    const double d31[3] = {X[3 * c] - X[3 * a], X[3 * c + 1] - X[3 * a + 1], X[3 * c + 2] - X[3 * a + 2]};
+    const double cx = d21[1] * d31[2] - d31[1] * d21[2], cy = -d21[0] * d31[2] + d31[0] * d21[2], cz = d21[0] * d31[1] - d31[0] * d21[1];
+    m->dA0[e] = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+  }
+  return 0;
+}
+
+static int check_params(const BiofemParams &p)
+{
+  if (p.n_qp < 1 || p.n_qp > kMaxQp) return fail(63, "n_qp must be between 1 and 6");
+  if (p.c33_subitr_nums < 1) return fail(62, "C33_subitr_nums must be >= 1");
+  if (!(p.h0 > 0.0)) return fail(62, "h0 must be positive");
+  if (p.precision != BIOFEM_FP64 && p.precision != BIOFEM_FP32_BULK) return fail(62, "unknown precision");
+  return 0;
+}
+
+static void gauss(int n, double *th, double *w)
+{
+  switch (n) {
+  case 1: th[0] = 0.0; w[0] = 2.0; break;
+  case 2: th[0] = -0.5773502691896257; th[1] = 0.5773502691896257; w[0] = w[1] = 1.0; break;
+  case 3: th[0] = -0.7745966692414834; th[1] = 0.0; th[2] = 0.7745966692414834;
+          w[0] = w[2] = 0.5555555555555556; w[1] = 0.8888888888888888; break;
+  case 4: th[0] = -0.8611363115940526; th[1] = -0.3399810435848563; th[2] = 0.3399810435848563; th[3] = 0.8611363115940526;
+          w[0] = w[3] = 0.3478548451374538; w[1] = w[2] = 0.6521451548625461; break;
+  case 5: th[0] = -0.9061798459386640; th[1] = -0.5384693101056831; th[2] = 0.0; th[3] = 0.5384693101056831; th[4] = 0.9061798459386640;
+          w[0] = w[4] = 0.2369268850561891; w[1] = w[3] = 0.4786286704993665; w[2] = 0.5688888888888889; break;
+  default: th[0] = -0.9324695142031521; th[1] = -0.6612093864662645; th[2] = -0.2386191860831969;
+           th[3] = 0.2386191860831969; th[4] = 0.6612093864662645; th[5] = 0.9324695142031521;
+           w[0] = w[5] = 0.1713244923791704; w[1] = w[4] = 0.3607615730481386; w[2] = w[3] = 0.4679139345726910; break;
+  }
+}
+
+extern "C" {
+
+int InitGpuWorkspace(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_init) return 0;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(76, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  CUDA_TRY(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+  g_init = true;
+  return 0;
+}
+
+int DestroyGpuWorkspace(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (BiofemGpuMesh *m : g_meshes) free_mesh(m);
+  g_meshes.clear();
+  if (g_stream) cudaStreamDestroy(g_stream);
+  g_stream = nullptr;
+  g_init = false;
+  return 0;
+}
+
+const char *BiofemGpuLastError(void) { return g_last_error.c_str(); }
+
+/* Host-only: topology + maps without touching the GPU (used by tests and by
+   callers that want the tables).  Returns a handle whose device views are empty. */
+int BuildHostMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, BiofemGpuMesh **out)
+{
+  if (!mesh || !params || !out) return fail(85, "null argument");
+  int rc = check_params(*params);
+  if (rc) return rc;
+  BiofemGpuMesh *m = new BiofemGpuMesh();
+  m->prm = *params;
+  std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx, blkrow, cidx;
+  std::vector<long long> kofs, cptr;
+  std::vector<unsigned char> rowkind;
+  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, kofs, rowkind, rptr, ridx, pptr, pidx, blkrow, cptr, cidx);
+  if (rc) { delete m; return rc; }
+  *out = m;
+  return 0;
+}
+
+int DestroyHostMesh(BiofemGpuMesh *m) { delete m; return 0; }
+
+int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, BiofemGpuMesh **out)
+{
+  if (!mesh || !params || !out) return fail(85, "null argument");
+  int rc = check_params(*params);
+  if (rc) return rc;
+  if (!g_init) { rc = InitGpuWorkspace(); if (rc) return rc; }
+  if (params->precision != BIOFEM_FP64) return fail(56, "FP32-bulk form is not built into this library yet");
+  BiofemGpuMesh *m = new BiofemGpuMesh();
+  m->prm = *params;
+  std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx, blkrow, cidx;
+  std::vector<long long> kofs, cptr;
+  std::vector<unsigned char> rowkind;
+  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, kofs, rowkind, rptr, ridx, pptr, pidx, blkrow, cptr, cidx);
+  if (rc) { delete m; return rc; }
+  const HostTopo &T = m->topo;
+  const int ne = T.n_elmt, nv = T.n_v, ng = T.n_ghosts, nt = nv + ng;
+
+  KParams &kp = m->kp;
+  kp.ne = ne; kp.nt = nt; kp.nv = nv; kp.ng = ng; kp.nq = params->n_qp; kp.iters = params->c33_subitr_nums;
+  kp.mu = params->mu; kp.K = params->bulk_modulus; kp.hhalf = 0.5 * params->h0;
+  kp.pressure = params->pressure; kp.gamma = params->gamma;
+  gauss(params->n_qp, kp.theta, kp.w);
+
+  DevMesh &dm = m->dm;
+  std::vector<int> ghost3(3 * (size_t)ng);
+  for (int g = 0; g < ng; g++) { ghost3[3 * g] = T.ghost_nv1[g]; ghost3[3 * g + 1] = T.ghost_nv2[g]; ghost3[3 * g + 2] = T.ghost_nv3[g]; }
+  std::vector<int> etri(T.tri_all.begin(), T.tri_all.begin() + 3 * (size_t)ne);
+  std::vector<double> tabs(kNumTables * 80);
+  host_tables(tabs.data());
+  std::vector<double> fib(mesh->n_fib, mesh->n_fib + 3 * (size_t)ne), gsc(mesh->gamma_scale, mesh->gamma_scale + ne);
+
+#define UP(field, vec) do { rc = dupload(m, const_cast<std::remove_const<std::remove_pointer<decltype(dm.field)>::type>::type **>(&dm.field), vec); if (rc) { free_mesh(m); return rc; } } while (0)
+  UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(etri, etri); UP(ghost3, ghost3); UP(kofs, kofs);
+  UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(pptr, pptr); UP(pidx, pidx);
+  UP(rowptr, m->rowptr); UP(colind, m->colind); UP(blkrow, blkrow); UP(cptr, cptr); UP(cidx, cidx);
+#undef UP
+  dm.nnzb = m->nnzb;
+  double *d_fib = nullptr, *d_gsc = nullptr, *d_eref = nullptr;
+  const size_t nref = (size_t)(kRefPerQp * kp.nq + kRefPerElem) * ne;
+  if ((rc = dupload(m, &d_fib, fib)) || (rc = dupload(m, &d_gsc, gsc)) || (rc = dalloc(m, &d_eref, nref)) ||
+      (rc = dalloc(m, &dm.pos, 4 * (size_t)nt)) || (rc = dalloc(m, &dm.fb, 48 * (size_t)ne)) ||
+      (rc = dalloc(m, &dm.fp, 3 * (size_t)ne)) || (rc = dalloc(m, &dm.ke, 9 * (size_t)(kofs.empty() ? 0 : kofs.back() + 256))) ||
+      (rc = dalloc(m, &dm.status, 1)) || (rc = dalloc(m, &dm.fmax, 1)) ||
+      (rc = dalloc(m, &m->d_x, 3 * (size_t)nt)) || (rc = dalloc(m, &m->d_R, 3 * (size_t)nt)) ||
+      (rc = dalloc(m, &m->d_K, 9 * (size_t)m->nnzb))) {
+    free_mesh(m);
+    return rc;
+  }
+  dm.eref = d_eref;
+  CUDA_TRY(cudaMemset(dm.status, 0, sizeof(int)));
+  CUDA_TRY(cudaMemset(dm.fp, 0, 3 * sizeof(double) * (size_t)ne));
+  /* reference positions (ghosts included) -> one-time reference geometry */
+  if ((rc = launch_positions(dm, kp, dm.X, g_stream)) || (rc = launch_ref_prep(dm, kp, d_fib, d_gsc, d_eref, g_stream))) {
+    free_mesh(m);
+    return fail(76, std::string("reference preparation launch: ") + cudaGetErrorString((cudaError_t)rc));
+  }
+  cudaError_t e = cudaStreamSynchronize(g_stream);
+  if (e != cudaSuccess) { free_mesh(m); return fail(76, std::string("reference preparation: ") + cudaGetErrorString(e)); }
+  g_meshes.insert(m);
+  *out = m;
+  return 0;
+}
+
+int DestroyGpuMesh(BiofemGpuMesh *m)
+{
+  if (!m) return 0;
+  if (g_meshes.erase(m)) free_mesh(m);
+  return 0;
+}
+
+int GetGpuMeshInfo(const BiofemGpuMesh *m, BiofemMeshInfo *info)
+{
+  if (!m || !info) return fail(85, "null argument");
+  info->n_v = m->topo.n_v; info->n_ghosts = m->topo.n_ghosts; info->n_elmt = m->topo.n_elmt;
+  info->n_dof = 3 * (m->topo.n_v + m->topo.n_ghosts);
+  info->n_irregular = m->n_irregular;
+  info->nnzb = m->nnzb; info->n_contrib = m->ncontrib; info->device_bytes = (int64_t)m->bytes;
+  return 0;
+}
+
+int GetGpuTopology(const BiofemGpuMesh *m, int32_t *patch, int32_t *ire, int32_t *val, int32_t *irv,
+                   int32_t *gtri, double *xyz0_full, double *dA0)
+{
+  if (!m) return fail(85, "null argument");
+  const HostTopo &T = m->topo;
+  if (patch) std::copy(T.patch.begin(), T.patch.end(), patch);
+  if (ire) std::copy(T.ire.begin(), T.ire.end(), ire);
+  if (val) std::copy(T.val.begin(), T.val.end(), val);
+  if (irv) std::copy(T.irv.begin(), T.irv.end(), irv);
+  if (gtri) std::copy(T.tri_all.begin(), T.tri_all.end(), gtri);
+  if (xyz0_full) std::copy(T.xyz0_full.begin(), T.xyz0_full.end(), xyz0_full);
+  if (dA0) std::copy(m->dA0.begin(), m->dA0.end(), dA0);
+  return 0;
+}
+
+int GetGpuGhostMap(const BiofemGpuMesh *m, int32_t *ghost3)
+{
+  if (!m || !ghost3) return fail(85, "null argument");
+  const HostTopo &T = m->topo;
+  for (int g = 0; g < T.n_ghosts; g++) {
+    ghost3[3 * g] = T.ghost_nv1[g]; ghost3[3 * g + 1] = T.ghost_nv2[g]; ghost3[3 * g + 2] = T.ghost_nv3[g];
+  }
+  return 0;
+}
+
+int GetGpuCsrPattern(const BiofemGpuMesh *m, int32_t *rowptr, int32_t *colind)
+{
+  if (!m) return fail(85, "null argument");
+  if (rowptr) std::copy(m->rowptr.begin(), m->rowptr.end(), rowptr);
+  if (colind) std::copy(m->colind.begin(), m->colind.end(), colind);
+  return 0;
+}
+
+int GetGpuLaunchCounts(const BiofemGpuMesh *m, int32_t *res, int32_t *jac)
+{
+  (void)m;
+  if (res) *res = 4;   /* positions, element residual, node gather, scale */
+  if (jac) *jac = 5;   /* positions, element tangent, node gather, block gather, scale */
+  return 0;
+}
+
+static void timer_collect(BiofemGpuMesh *m)
+{
+  KernelTimer &t = m->timer;
+  if (!t.on || t.n == 0) return;
+  cudaEventSynchronize(t.ev[t.n]);
+  for (int i = 0; i < t.n; i++) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t.ev[i], t.ev[i + 1]);
+    t.acc_ms[i] += ms;
+  }
+  t.calls++;
+  t.n = 0;
+}
+
+int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *stream)
+{
+  if (!m || !d_x || !d_R) return fail(85, "null argument");
+  cudaStream_t st = pick_stream(stream);
+  int rc = 0;
+  tmark(m, st, 0);
+  if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
+  if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
+  if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 3); }
+  if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, nullptr, st); tmark(m, st, 4); }
+  if (rc) return fail(76, std::string("residual launch: ") + cudaGetErrorString((cudaError_t)rc));
+  timer_collect(m);
+  return 0;
+}
+
+int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, double *d_K, void *stream)
+{
+  if (!m || !d_x || !d_R || !d_K) return fail(85, "null argument");
+  cudaStream_t st = pick_stream(stream);
+  int rc = 0;
+  tmark(m, st, 0);
+  if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
+  if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 2); }
+  if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 3); }
+  if (!rc) { rc = launch_block_gather(m->dm, m->kp, d_K, st); tmark(m, st, 4); }
+  if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, d_K, st); tmark(m, st, 5); }
+  if (rc) return fail(76, std::string("jacobian launch: ") + cudaGetErrorString((cudaError_t)rc));
+  timer_collect(m);
+  return 0;
+}
+
+/* Per-kernel event timing of the device calls: on = 1 starts (and clears)
+   accumulation, 0 stops.  Timing synchronises on the last event of every call. */
+int EnableGpuKernelTiming(BiofemGpuMesh *m, int on)
+{
+  if (!m) return fail(85, "null argument");
+  KernelTimer &t = m->timer;
+  if (on && !t.ev[0])
+    for (int i = 0; i <= kMaxTimed; i++) CUDA_TRY(cudaEventCreate(&t.ev[i]));
+  t.on = on != 0;
+  t.n = 0; t.calls = 0;
+  for (int i = 0; i < kMaxTimed; i++) t.acc_ms[i] = 0.f;
+  return 0;
+}
+
+/* Accumulated milliseconds per kernel slot (launch order of the last kind of
+   call) and the number of calls timed. */
+int GetGpuKernelTimes(const BiofemGpuMesh *m, double *ms, int32_t nslots, int32_t *calls)
+{
+  if (!m || !ms) return fail(85, "null argument");
+  for (int i = 0; i < nslots && i < kMaxTimed; i++) ms[i] = m->timer.acc_ms[i];
+  if (calls) *calls = m->timer.calls;
+  return 0;
+}
+
+int BiofemGpuSync(BiofemGpuMesh *m, void *stream)
+{
+  if (!m) return fail(85, "null argument");
+  cudaStream_t st = pick_stream(stream);
+  CUDA_TRY(cudaStreamSynchronize(st));
+  int status = 0;
+  CUDA_TRY(cudaMemcpy(&status, m->dm.status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (status) {
+    CUDA_TRY(cudaMemset(m->dm.status, 0, sizeof(int)));
+    return fail(72, "CC3333 too small in the C33 solve (ModElemC33, active_strain.c:1676)");
+  }
+  return 0;
+}
+
+int RunGpuResidual(BiofemGpuMesh *m, const double *x, double *R)
+{
+  if (!m || !x || !R) return fail(85, "null argument");
+  const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
+  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, g_stream));
+  int rc = RunGpuResidualDevice(m, m->d_x, m->d_R, g_stream);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+  return BiofemGpuSync(m, g_stream);
+}
+
+int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, double *K)
+{
+  if (!m || !x || !K) return fail(85, "null argument");
+  const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
+  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, g_stream));
+  int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, m->d_K, g_stream);
+  if (rc) return rc;
+  if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+  CUDA_TRY(cudaMemcpyAsync(K, m->d_K, 9 * (size_t)m->nnzb * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+  return BiofemGpuSync(m, g_stream);
+}
+
+int FormFunctionFEMGpu(void *snes, const double *x, double *R, void *ctx)
+{
+  (void)snes;
+  return RunGpuResidual(reinterpret_cast<BiofemGpuMesh *>(ctx), x, R);
+}
+
+int FormJacobianFEMGpu(void *snes, const double *x, double *K, void *ctx)
+{
+  (void)snes;
+  return RunGpuResidualJacobian(reinterpret_cast<BiofemGpuMesh *>(ctx), x, nullptr, K);
+}
+
+/* Basis-derivative tables (regular + irregular valences 3..10), 11*5*16. */
+int GetGpuBasisTables(double *out)
+{
+  if (!out) return fail(85, "null argument");
+  host_tables(out);
+  return 0;
+}
+
+} /* extern "C" */

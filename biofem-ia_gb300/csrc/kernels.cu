@@ -1,0 +1,458 @@
+/*
+ * sm_103a kernels of the element residual / tangent / assembly path.
+ *
+ *   k_positions      x (Vec layout) -> padded node positions; ghost nodes
+ *                    x_g = x_nv2 + x_nv1 - x_nv3 (GlobalGhost, bending.c:1763-1814)
+ *   k_ref_prep       one-time reference geometry per element (geom0 + the
+ *                    reference half of ElemUpdateG and ElemActDefGrad)
+ *   k_elem_residual  one thread per element: geometry, closed-form stress,
+ *                    element forces Fb (ElemUpdFint) and the follower-pressure
+ *                    corner force (SurfaceNormalPressure, external.c:589-624)
+ *   k_elem_tangent   16 lanes per element: lane j carries d/dy_j through the
+ *                    same code (forward mode), giving column j of df/dy; the
+ *                    half-warp then forms K_e = N^T (df/dy) N in shared memory
+ *   k_node_gather    one thread per node: Fint / Fext summed over the node's
+ *                    element contributions in element order (the order
+ *                    FInternalAct's VecSetValues loop adds them), R = Fint - Fext,
+ *                    clamp rows R = x - X, ghost rows 0 (main.c:844-1016)
+ *   k_block_gather   one thread per tangent value: sum of the element-matrix
+ *                    entries mapped to that 3x3 block, in element order
+ *   k_scale          R, K *= 1 / max(|Fext|_inf, 1) (main.c:1020-1026)
+ *
+ * Assembly is deterministic: every sum runs in a fixed order given by the
+ * precomputed element-to-node / element-to-block maps, independent of the
+ * launch configuration.
+ */
+#include <cuda_runtime.h>
+
+#include "element.cuh"
+
+namespace biofem {
+
+/* ---------------- helpers ---------------- */
+__device__ __forceinline__ void load_node(const double *pos, int node, double &x, double &y, double &z)
+{
+  const double2 a = __ldg(reinterpret_cast<const double2 *>(pos) + 2 * (size_t)node);
+  const double b = __ldg(pos + 4 * (size_t)node + 2);
+  x = a.x; y = a.y; z = b;
+}
+
+__device__ __forceinline__ void set_status(int *status, int bits)
+{
+  if (bits) atomicOr(status, bits);
+}
+
+/* y = N x over the element patch (regular table or IN arrays of valence v). */
+__device__ __forceinline__ void gather_y(const double *pos, const int *patch, int e, int nen, const double *tab,
+                                         double y[15])
+{
+  for (int k = 0; k < 15; k++) y[k] = 0.0;
+  const int4 *p4 = reinterpret_cast<const int4 *>(patch + 16 * (size_t)e);
+  int nodes[16];
+  const int4 q0 = __ldg(p4), q1 = __ldg(p4 + 1), q2 = __ldg(p4 + 2), q3 = __ldg(p4 + 3);
+  nodes[0] = q0.x; nodes[1] = q0.y; nodes[2] = q0.z; nodes[3] = q0.w;
+  nodes[4] = q1.x; nodes[5] = q1.y; nodes[6] = q1.z; nodes[7] = q1.w;
+  nodes[8] = q2.x; nodes[9] = q2.y; nodes[10] = q2.z; nodes[11] = q2.w;
+  nodes[12] = q3.x; nodes[13] = q3.y; nodes[14] = q3.z; nodes[15] = q3.w;
+#pragma unroll 4
+  for (int i = 0; i < nen; i++) {
+    double x, yy, z;
+    load_node(pos, nodes[i], x, yy, z);
+#pragma unroll
+    for (int r = 0; r < 5; r++) {
+      const double c = tab[r * 16 + i];
+      y[3 * r] += c * x; y[3 * r + 1] += c * yy; y[3 * r + 2] += c * z;
+    }
+  }
+}
+
+/* ---------------- positions / ghosts ---------------- */
+__global__ void k_positions(int nv, int ng, const double *__restrict__ x, const int *__restrict__ ghost3,
+                            double *__restrict__ pos)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double o[4] = {0.0, 0.0, 0.0, 0.0};
+  if (i < nv) {
+    o[0] = x[3 * (size_t)i]; o[1] = x[3 * (size_t)i + 1]; o[2] = x[3 * (size_t)i + 2];
+  } else if (i < nv + ng) {
+    const int g = i - nv;
+    const int n1 = ghost3[3 * g], n2 = ghost3[3 * g + 1], n3 = ghost3[3 * g + 2];
+    for (int d = 0; d < 3; d++) o[d] = x[3 * (size_t)n2 + d] + x[3 * (size_t)n1 + d] - x[3 * (size_t)n3 + d];
+  } else {
+    return;
+  }
+  double2 *dst = reinterpret_cast<double2 *>(pos) + 2 * (size_t)i;
+  dst[0] = make_double2(o[0], o[1]);
+  dst[1] = make_double2(o[2], o[3]);
+}
+
+/* ---------------- reference preparation ---------------- */
+/* 3x3 inverse by cofactors (math.c:75-89 form). */
+__device__ __forceinline__ void inv3(const double A[3][3], double B[3][3])
+{
+  const double det = A[0][0] * (A[2][2] * A[1][1] - A[2][1] * A[1][2]) - A[1][0] * (A[2][2] * A[0][1] - A[2][1] * A[0][2])
+                   + A[2][0] * (A[1][2] * A[0][1] - A[1][1] * A[0][2]);
+  const double c = 1.0 / det;
+  B[0][0] = c * (A[2][2] * A[1][1] - A[2][1] * A[1][2]);
+  B[0][1] = -c * (A[2][2] * A[0][1] - A[2][1] * A[0][2]);
+  B[0][2] = c * (A[1][2] * A[0][1] - A[1][1] * A[0][2]);
+  B[1][0] = -c * (A[2][2] * A[1][0] - A[2][0] * A[1][2]);
+  B[1][1] = c * (A[2][2] * A[0][0] - A[2][0] * A[0][2]);
+  B[1][2] = -c * (A[1][2] * A[0][0] - A[1][0] * A[0][2]);
+  B[2][0] = c * (A[2][1] * A[1][0] - A[2][0] * A[1][1]);
+  B[2][1] = -c * (A[2][1] * A[0][0] - A[2][0] * A[0][1]);
+  B[2][2] = c * (A[1][1] * A[0][0] - A[1][0] * A[0][1]);
+}
+
+__device__ __forceinline__ double det3(const double A[3][3])
+{
+  return A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0])
+       + A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]);
+}
+
+__global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib, const double *__restrict__ gscale,
+                           double *__restrict__ eref)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ne) return;
+  const int info = m.einfo[e];
+  const int nen = info & 0xff, tabi = info >> 8;
+  double y[15];
+  gather_y(m.pos, m.patch, e, nen, m.ntab + tabi * 80, y);
+  const V3<double> a1 = {y[0], y[1], y[2]}, a2 = {y[3], y[4], y[5]};
+  const V3<double> Aaa = {y[6], y[7], y[8]}, Abb = {y[9], y[10], y[11]}, Aab = {y[12], y[13], y[14]};
+  const V3<double> cr = cross(a1, a2);
+  const double cn = sqrt(dot(cr, cr));
+  const V3<double> n = {cr.x / cn, cr.y / cn, cr.z / cn};
+  V3<double> a31 = cross(Aaa, a2) + cross(a1, Aab), a32 = cross(Aab, a2) + cross(a1, Abb);
+  a31 = {a31.x / cn, a31.y / cn, a31.z / cn};
+  a32 = {a32.x / cn, a32.y / cn, a32.z / cn};
+  const V3<double> f = {fib[3 * (size_t)e], fib[3 * (size_t)e + 1], fib[3 * (size_t)e + 2]};
+  const double gam = p.gamma * gscale[e];
+  const double phi = dot(f, f);
+  const double gamp = gam / (1.0 - gam * phi);
+  const double c1 = 2.0 * gamp + gamp * gamp * phi;
+  /* flat reference triangle area (AreaNormal, io.c:1646-1669) */
+  double X[3][3];
+  for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
+  const V3<double> d21 = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
+  const V3<double> d31 = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
+  const V3<double> ca = cross(d21, d31);
+  const double dA0 = 0.5 * sqrt(ca.x * ca.x + ca.y * ca.y + ca.z * ca.z);
+  const size_t ne = p.ne;
+  for (int q = 0; q < p.nq; q++) {
+    const double th3 = p.hhalf * p.theta[q];
+    const V3<double> g[3] = {a1 + scl(th3, a31), a2 + scl(th3, a32), n};
+    double G[3][3], Gi[3][3];
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) G[i][j] = dot(g[i], g[j]);
+    inv3(G, Gi);
+    double t[3], s[3];
+    for (int i = 0; i < 3; i++) t[i] = dot(g[i], f);
+    for (int i = 0; i < 3; i++) s[i] = Gi[i][0] * t[0] + Gi[i][1] * t[1] + Gi[i][2] * t[2];
+    const double omg = 1.0 - gam * phi;
+    const double rho = 1.0 / (det3(G) * omg * omg);
+    /* v = Fa_inv.Cov G^-1 e3, w = Fa_inv.Cov G^-1 v, A^T x = G (Fa.Cont x) */
+    double u[3] = {Gi[0][2], Gi[1][2], Gi[2][2]};
+    double v[3], gv[3], w[3];
+    const double tu = t[0] * u[0] + t[1] * u[1] + t[2] * u[2];
+    for (int i = 0; i < 3; i++) v[i] = G[i][0] * u[0] + G[i][1] * u[1] + G[i][2] * u[2] + gamp * t[i] * tu;
+    for (int i = 0; i < 3; i++) gv[i] = Gi[i][0] * v[0] + Gi[i][1] * v[1] + Gi[i][2] * v[2];
+    const double tgv = t[0] * gv[0] + t[1] * gv[1] + t[2] * gv[2];
+    for (int i = 0; i < 3; i++) w[i] = G[i][0] * gv[0] + G[i][1] * gv[1] + G[i][2] * gv[2] + gamp * t[i] * tgv;
+    auto aT = [&](const double xin[3], double out[3]) {
+      double fa[3];
+      const double sx = s[0] * xin[0] + s[1] * xin[1] + s[2] * xin[2];
+      for (int i = 0; i < 3; i++) fa[i] = Gi[i][0] * xin[0] + Gi[i][1] * xin[1] + Gi[i][2] * xin[2] - gam * s[i] * sx;
+      for (int i = 0; i < 3; i++) out[i] = G[i][0] * fa[0] + G[i][1] * fa[1] + G[i][2] * fa[2];
+    };
+    double av[3], aw[3], ae[3];
+    const double e3[3] = {0.0, 0.0, 1.0};
+    aT(v, av); aT(w, aw); aT(e3, ae);
+    double *o = eref + (size_t)kRefPerQp * q * ne + e;
+    o[0] = Gi[0][0]; o[1 * ne] = Gi[1][1]; o[2 * ne] = 0.5 * (Gi[0][1] + Gi[1][0]); o[3 * ne] = Gi[2][2];
+    for (int k = 0; k < 3; k++) {
+      o[(4 + k) * ne] = s[k]; o[(7 + k) * ne] = t[k];
+      o[(11 + k) * ne] = av[k]; o[(14 + k) * ne] = aw[k]; o[(17 + k) * ne] = ae[k];
+    }
+    o[10 * ne] = rho;
+  }
+  double *o = eref + (size_t)kRefPerQp * p.nq * ne + e;
+  o[0] = gam; o[ne] = gamp; o[2 * ne] = c1; o[3 * ne] = 0.5 * (2.0 * p.hhalf) * dA0;
+}
+
+/* ---------------- residual element kernel ---------------- */
+__global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p)
+{
+  __shared__ double tabs[kNumTables * 80];
+  for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ne) return;
+  const int info = m.einfo[e];
+  const int nen = info & 0xff, tabi = info >> 8;
+  const double *tab = tabs + tabi * 80;
+  double y[15];
+  gather_y(m.pos, m.patch, e, nen, tab, y);
+  double f[15];
+  int st = 0;
+  elem_forces<double>(y, p, m.eref + e, p.ne, f, st);
+  set_status(m.status, st);
+  /* Fb_a = sum_r N[r][a] f_r, stored slot-major: fb[(3a+d)*ne + e] */
+  const size_t ne = p.ne;
+  for (int a = 0; a < nen; a++) {
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+#pragma unroll
+    for (int r = 0; r < 5; r++) {
+      const double c = tab[r * 16 + a];
+      fx += c * f[3 * r]; fy += c * f[3 * r + 1]; fz += c * f[3 * r + 2];
+    }
+    m.fb[(3 * a) * ne + e] = fx;
+    m.fb[(3 * a + 1) * ne + e] = fy;
+    m.fb[(3 * a + 2) * ne + e] = fz;
+  }
+  /* follower pressure: each corner receives n P dA / 3 = P (x2-x1)x(x3-x1) / 6 */
+  if (p.pressure != 0.0) {
+    double X[3][3];
+    for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
+    const V3<double> d21 = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
+    const V3<double> d31 = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
+    const V3<double> ca = cross(d21, d31);
+    const double nrm = sqrt(ca.x * ca.x + ca.y * ca.y + ca.z * ca.z);
+    const double dA = 0.5 * nrm;
+    m.fp[e] = (ca.x / nrm) * p.pressure * dA / 3.;
+    m.fp[ne + e] = (ca.y / nrm) * p.pressure * dA / 3.;
+    m.fp[2 * ne + e] = (ca.z / nrm) * p.pressure * dA / 3.;
+  }
+}
+
+/* ---------------- tangent element kernel ---------------- */
+constexpr int kTanElemsPerCta = 8;   /* 16 lanes per element, 128 threads */
+
+__global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
+{
+  __shared__ double tabs[kNumTables * 80];
+  __shared__ double Dsh[kTanElemsPerCta][15 * 16];   /* D[r][s] at r*16+s */
+  __shared__ double Tsh[kTanElemsPerCta][15 * 48];   /* T[r3][c] : (D N) */
+  for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 15;
+  const int slot = threadIdx.x >> 4;
+  const int e = blockIdx.x * kTanElemsPerCta + slot;
+  const bool live = e < p.ne;
+  const int ee = live ? e : p.ne - 1;
+  const int info = m.einfo[ee];
+  const int nen = info & 0xff, tabi = info >> 8;
+  const double *tab = tabs + tabi * 80;
+  double y[15];
+  gather_y(m.pos, m.patch, ee, nen, tab, y);
+  D1 yd[15], fd[15];
+#pragma unroll
+  for (int k = 0; k < 15; k++) yd[k] = D1{y[k], k == lane ? 1.0 : 0.0};
+  int st = 0;
+  elem_forces<D1>(yd, p, m.eref + ee, p.ne, fd, st);
+  if (live) set_status(m.status, st);
+  const size_t ne = p.ne;
+  /* column `lane` of D = df/dy */
+  if (lane < 15) {
+#pragma unroll
+    for (int r = 0; r < 15; r++) Dsh[slot][r * 16 + lane] = fd[r].d;
+  }
+  /* element force (primal part, identical in every lane) */
+  if (live) {
+    for (int idx = lane; idx < 3 * nen; idx += 16) {
+      const int a = idx / 3, d = idx - 3 * a;
+      double s = 0.0;
+#pragma unroll
+      for (int r = 0; r < 5; r++) s += tab[r * 16 + a] * fd[3 * r + d].v;
+      m.fb[(size_t)idx * ne + e] = s;
+    }
+    if (lane == 0 && p.pressure != 0.0) {
+      double X[3][3];
+      for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
+      const V3<double> d21 = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
+      const V3<double> d31 = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
+      const V3<double> ca = cross(d21, d31);
+      const double nrm = sqrt(ca.x * ca.x + ca.y * ca.y + ca.z * ca.z);
+      const double dA = 0.5 * nrm;
+      m.fp[e] = (ca.x / nrm) * p.pressure * dA / 3.;
+      m.fp[ne + e] = (ca.y / nrm) * p.pressure * dA / 3.;
+      m.fp[2 * ne + e] = (ca.z / nrm) * p.pressure * dA / 3.;
+    }
+  }
+  __syncwarp();
+  /* T[(r,i)][(b,j)] = sum_s D[(r,i)][(s,j)] N[s][b] */
+  const int ncol = 3 * nen;
+  for (int idx = lane; idx < 15 * ncol; idx += 16) {
+    const int ri = idx / ncol, c = idx - ri * ncol;
+    const int b = c / 3, j = c - 3 * b;
+    double s = 0.0;
+#pragma unroll
+    for (int sr = 0; sr < 5; sr++) s += Dsh[slot][ri * 16 + 3 * sr + j] * tab[sr * 16 + b];
+    Tsh[slot][ri * 48 + c] = s;
+  }
+  __syncwarp();
+  if (!live) return;
+  /* Follower-pressure load stiffness: every corner carries P/6 (x2-x1)x(x3-x1),
+     so d/dx1 = [b-a]x, d/dx2 = -[b]x, d/dx3 = [a]x with a = x2-x1, b = x3-x1,
+     entering K = dR/dx with a minus sign at the corner rows. */
+  const int cs = m.ecorner[e];
+  const int cslot[3] = {cs & 31, (cs >> 5) & 31, (cs >> 10) & 31};
+  double dc[3][3][3];   /* dc[k] = d c / d x_k as a 3x3 matrix */
+  {
+    double X[3][3];
+    for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
+    const double av[3] = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
+    const double bv[3] = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
+    const double vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
+    const double sc = -p.pressure / 6.0;
+    for (int k = 0; k < 3; k++) {
+      const double *v = vv[k];
+      dc[k][0][0] = 0.0;        dc[k][0][1] = -sc * v[2]; dc[k][0][2] = sc * v[1];
+      dc[k][1][0] = sc * v[2];  dc[k][1][1] = 0.0;        dc[k][1][2] = -sc * v[0];
+      dc[k][2][0] = -sc * v[1]; dc[k][2][1] = sc * v[0];  dc[k][2][2] = 0.0;
+    }
+  }
+  /* K_e[(a,i)][(b,j)] = sum_r N[r][a] T[(r,i)][(b,j)], block layout (a*nen+b)*9 + 3i + j */
+  double *ke = m.ke + (size_t)m.kofs[e] * 9;
+  const int nval = 9 * nen * nen;
+  for (int idx = lane; idx < nval; idx += 16) {
+    const int blk = idx / 9, w = idx - 9 * blk;
+    const int a = blk / nen, b = blk - a * nen;
+    const int i = w / 3, j = w - 3 * i;
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < 5; r++) s += tab[r * 16 + a] * Tsh[slot][(3 * r + i) * 48 + 3 * b + j];
+    if (p.pressure != 0.0 && (a == cslot[0] || a == cslot[1] || a == cslot[2])) {
+      for (int k = 0; k < 3; k++)
+        if (b == cslot[k]) s += dc[k][i][j];
+    }
+    ke[idx] = s;
+  }
+}
+
+/* ---------------- node gather (residual assembly) ---------------- */
+__device__ __forceinline__ unsigned long long abs_bits(double v)
+{
+  return (unsigned long long)__double_as_longlong(fabs(v));
+}
+
+__global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x, double *__restrict__ R)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long lmax = 0ull;
+  if (i < p.nt) {
+    const size_t ne = p.ne;
+    double fi[3] = {0.0, 0.0, 0.0}, fe[3] = {0.0, 0.0, 0.0};
+    for (int c = m.rptr[i]; c < m.rptr[i + 1]; c++) {
+      const size_t base = (size_t)m.ridx[c];   /* 3*slot*ne + e */
+      fi[0] += m.fb[base]; fi[1] += m.fb[base + ne]; fi[2] += m.fb[base + 2 * ne];
+    }
+    for (int c = m.pptr[i]; c < m.pptr[i + 1]; c++) {
+      const size_t e = (size_t)m.pidx[c];
+      fe[0] += m.fp[e]; fe[1] += m.fp[ne + e]; fe[2] += m.fp[2 * ne + e];
+    }
+    const int kind = m.rowkind[i];
+    for (int d = 0; d < 3; d++) {
+      double r;
+      if (kind == 2) r = 0.0;
+      else if (kind == 1) r = x[3 * (size_t)i + d] - m.X[3 * (size_t)i + d];
+      else r = -1.0 * fe[d] + fi[d];
+      R[3 * (size_t)i + d] = r;
+      const unsigned long long b = abs_bits(fe[d]);
+      lmax = b > lmax ? b : lmax;
+    }
+  }
+  /* warp max then one atomic per warp */
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_down_sync(0xffffffffu, lmax, o);
+    lmax = v > lmax ? v : lmax;
+  }
+  if ((threadIdx.x & 31) == 0 && lmax) atomicMax(m.fmax, lmax);
+}
+
+/* ---------------- block gather (tangent assembly) ---------------- */
+__global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
+{
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 9 * m.nnzb) return;
+  const long long k = t / 9;
+  const int w = (int)(t - 9 * k);
+  const int row = m.blkrow[k];
+  const int kind = m.rowkind[row];
+  double s = 0.0;
+  if (kind != 0) {
+    s = (m.colind[k] == row && (w == 0 || w == 4 || w == 8)) ? 1.0 : 0.0;
+  } else {
+    for (long long c = m.cptr[k]; c < m.cptr[k + 1]; c++) {
+      const int id = m.cidx[c];
+      if (id >= 0) s += m.ke[(size_t)id * 9 + w];
+      else s -= m.ke[(size_t)(-(id + 1)) * 9 + w];
+    }
+  }
+  K[t] = s;
+}
+
+/* ---------------- scaling ---------------- */
+__global__ void k_scale(DevMesh m, KParams p, double *__restrict__ R, double *__restrict__ K)
+{
+  const double fmax = __longlong_as_double((long long)*m.fmax);
+  if (!(fmax > 1.0)) return;
+  const double sc = 1.0 / fmax;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nR = 3LL * p.nt;
+  if (t < nR) R[t] = R[t] * sc;
+  if (K && t < 9 * m.nnzb) {
+    if (m.rowkind[m.blkrow[t / 9]] != 2) K[t] = K[t] * sc;
+  }
+}
+
+/* ---------------- launchers ---------------- */
+static inline int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
+
+int launch_ref_prep(const DevMesh &m, const KParams &p, const double *fib, const double *gscale, double *eref_out, void *stream)
+{
+  k_ref_prep<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p, fib, gscale, eref_out);
+  return (int)cudaGetLastError();
+}
+
+int launch_positions(const DevMesh &m, const KParams &p, const double *x, void *stream)
+{
+  k_positions<<<blocks_for(p.nt, 256), 256, 0, (cudaStream_t)stream>>>(p.nv, p.ng, x, m.ghost3, m.pos);
+  return (int)cudaGetLastError();
+}
+
+int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream)
+{
+  k_elem_residual<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p);
+  return (int)cudaGetLastError();
+}
+
+int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream)
+{
+  k_elem_tangent<<<blocks_for(p.ne, kTanElemsPerCta), 128, 0, (cudaStream_t)stream>>>(m, p);
+  return (int)cudaGetLastError();
+}
+
+int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream)
+{
+  cudaMemsetAsync(m.fmax, 0, sizeof(unsigned long long), (cudaStream_t)stream);
+  k_node_gather<<<blocks_for(p.nt, 256), 256, 0, (cudaStream_t)stream>>>(m, p, x, R);
+  return (int)cudaGetLastError();
+}
+
+int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream)
+{
+  if (m.nnzb == 0) return 0;
+  k_block_gather<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K);
+  return (int)cudaGetLastError();
+}
+
+int launch_scale(const DevMesh &m, const KParams &p, double *R, double *K, void *stream)
+{
+  long long n = 3LL * p.nt;
+  if (K && 9 * m.nnzb > n) n = 9 * m.nnzb;
+  k_scale<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(m, p, R, K);
+  return (int)cudaGetLastError();
+}
+
+} /* namespace biofem */

@@ -1,0 +1,150 @@
+/*
+ * biofem_gpu.h -- C-ABI of the GB300 (sm_103a) element residual / tangent /
+ * assembly path for BioFEM-IA's active-strain Kirchhoff-Love shell.
+ *
+ * Shaped like the reference's GPU bridge, include/cuda_bridge.h:10-15
+ * (InitCudaWorkspace / DestroyCudaWorkspace / PrepareCudaHostWorkspace /
+ * Run*Kernel, all extern "C", PetscErrorCode return), but taking plain
+ * arrays instead of FE* so that callers need neither PETSc nor CUDA headers.
+ * A PETSc build binds these from its SNES callbacks.
+ *
+ * Conventions
+ *   - Every entry point returns an int that is PetscErrorCode-compatible:
+ *     0 = success, otherwise a PETSc error number (56 unsupported, 58 wrong
+ *     order, 62 bad argument, 63 out of range, 72 floating point, 76 CUDA
+ *     library error, 77 internal).  BiofemGpuLastError() gives the message.
+ *   - Index type is int32 (PetscInt default), reals are double (PetscReal).
+ *   - Vectors use the reference's Vec layout: 3*(n_v + n_ghosts) entries,
+ *     node-major (x, y, z), real nodes first, then one ghost node per
+ *     boundary-ring node (io.c:329-345, dmplex_geom.c:836-857).
+ *   - The tangent is a 3x3-block CSR (BSR) matrix over the same node
+ *     numbering.  Block values are row-major within the block.
+ *   - Host-side API is single-threaded per mesh handle.
+ */
+#ifndef BIOFEM_GPU_H
+#define BIOFEM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Mesh arrays, 0-based, as io.c Input() fills IBMNodes (io.c:373-479;
+   include/variables.h:44-89).  Boundary rings are closed loops with one ghost
+   node per ring node (bending.c:1670-1757). */
+typedef struct {
+  int32_t n_v;                 /* real nodes */
+  int32_t n_elmt;              /* real triangles */
+  int32_t n_edge;              /* boundary rings */
+  const int32_t *tri;          /* 3*n_elmt corners (nv1, nv2, nv3) */
+  const double  *xyz0;         /* 3*n_v reference coordinates (x_bp0, y_bp0, z_bp0 interleaved) */
+  const int32_t *n_bnodes;     /* n_edge ring lengths */
+  const int32_t *bnodes;       /* sum(n_bnodes) ring node ids in ring order */
+  const double  *n_fib;        /* 3*n_elmt fibre directions (ibm->n_fib) */
+  const double  *gamma_scale;  /* n_elmt per-element activation multiplier (ibm->gamma_scale) */
+} BiofemMeshDesc;
+
+/* Options of the path (active_strain.c:90-110, main.c:190-252). */
+typedef struct {
+  int32_t n_qp;                /* -num_gaussian_quad_points, 1..6 (6 is an extension) */
+  int32_t c33_subitr_nums;     /* -C33_subitr_nums, >= 1 */
+  double  mu;                  /* -mu */
+  double  bulk_modulus;        /* -bulk_modulus */
+  double  h0;                  /* -h0 */
+  double  gamma;               /* -muscle_act_gamma (gamma_ramp_type 0) */
+  double  pressure;            /* follower normal pressure P (external.c:589), 0 = none */
+  int32_t clamp_edge;          /* ring clamped in x,y,z by EdgeDirectionalFix (external.c:1706); -1 = none */
+  int32_t precision;           /* BIOFEM_FP64 or BIOFEM_FP32_BULK */
+} BiofemParams;
+
+enum { BIOFEM_FP64 = 0, BIOFEM_FP32_BULK = 1 };
+
+typedef struct {
+  int32_t n_v, n_ghosts, n_elmt, n_dof;
+  int32_t n_irregular;         /* elements on the one-step-subdivision branch */
+  int64_t nnzb;                /* 3x3 blocks in the tangent pattern */
+  int64_t n_contrib;           /* element-block contributions (assembly map size) */
+  int64_t device_bytes;        /* device memory held by the handle */
+} BiofemMeshInfo;
+
+typedef struct BiofemGpuMesh_ BiofemGpuMesh;
+
+/* Replaces InitCudaWorkspace (cuda_bridge.h:10): selects the device, creates
+   the stream.  Idempotent. */
+int InitGpuWorkspace(void);
+/* Replaces DestroyCudaWorkspace (cuda_bridge.h:11): frees every mesh handle
+   still alive and the stream. */
+int DestroyGpuWorkspace(void);
+
+/* Replaces PrepareCudaHostWorkspace (cuda_bridge.h:12) and the one-time
+   geometry of FEM_DMPlexGeomSetup (dmplex_geom.c:799-879): builds the
+   subdivision topology (GlobalGhostInit/IrrVer/Patch, bending.c:1188-1757),
+   dA0 (main.c:1447-1452), the reference geometry of every element, the
+   assembly maps and the tangent pattern, and uploads everything. */
+int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, BiofemGpuMesh **out);
+int DestroyGpuMesh(BiofemGpuMesh *m);
+int GetGpuMeshInfo(const BiofemGpuMesh *m, BiofemMeshInfo *info);
+
+/* Host copies of the topology the handle uses (same layout as IBMNodes):
+   patch 16*n_elmt, ire/val/irv n_elmt, gtri 3*(n_elmt+2*n_ghosts),
+   xyz0_full 3*(n_v+n_ghosts), dA0 n_elmt.  Any pointer may be NULL. */
+int GetGpuTopology(const BiofemGpuMesh *m, int32_t *patch, int32_t *ire, int32_t *val, int32_t *irv,
+                   int32_t *gtri, double *xyz0_full, double *dA0);
+/* Ghost rule of every ghost node g (GlobalGhostInit/GlobalGhost,
+   bending.c:1670-1814): x_g = x[nv2] + x[nv1] - x[nv3]; ghost3 holds
+   (nv1, nv2, nv3) per ghost, 3*n_ghosts entries. */
+int GetGpuGhostMap(const BiofemGpuMesh *m, int32_t *ghost3);
+/* Tangent pattern: rowptr (n_v+n_ghosts+1), colind (nnzb). */
+int GetGpuCsrPattern(const BiofemGpuMesh *m, int32_t *rowptr, int32_t *colind);
+
+/* FormFunctionFEM body (main.c:757-1032): R(x) with host arrays of n_dof
+   entries; copies in, computes, copies out.  Replaces the CPU residual the
+   reference's SNES callback evaluates. */
+int RunGpuResidual(BiofemGpuMesh *m, const double *x, double *R);
+/* R(x) and the tangent K = dR/dx (new: the reference is matrix-free,
+   main.c:464-466).  Kvals has 9*nnzb entries.  R may be NULL. */
+int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, double *Kvals);
+
+/* Device-resident variants: pointers are device memory, work is enqueued on
+   `stream` (a cudaStream_t; NULL = the CUDA default stream) and not
+   synchronised.  BiofemGpuSync() waits and reports device-side errors. */
+int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *stream);
+int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, double *d_Kvals, void *stream);
+int BiofemGpuSync(BiofemGpuMesh *m, void *stream);
+
+/* SNES-callback-shaped wrappers (main.c:120 FormFunctionFEM(SNES, Vec, Vec,
+   void*) and the Jacobian slot SNESSetJacobian, main.c:462-466) taking host
+   arrays; ctx is the BiofemGpuMesh*.  `snes` is passed through unused. */
+int FormFunctionFEMGpu(void *snes, const double *x, double *R, void *ctx);
+int FormJacobianFEMGpu(void *snes, const double *x, double *Kvals, void *ctx);
+
+/* Per-kernel CUDA-event timing of the device calls (off by default): slot i
+   is the i-th launch of the call (residual: positions, element residual,
+   node gather, scale; jacobian: positions, element tangent, node gather,
+   block gather, scale).  Times accumulate over calls until re-enabled. */
+int EnableGpuKernelTiming(BiofemGpuMesh *m, int on);
+int GetGpuKernelTimes(const BiofemGpuMesh *m, double *ms, int32_t nslots, int32_t *calls);
+
+/* Number of kernels one RunGpuResidual* / RunGpuResidualJacobian* call
+   launches (for launch accounting). */
+int GetGpuLaunchCounts(const BiofemGpuMesh *m, int32_t *residual_launches, int32_t *jacobian_launches);
+
+/* Host-only build of the same topology, maps and tangent pattern without a
+   GPU (no CUDA call is made): lets a caller or a test inspect the tables.
+   The handle only serves GetGpuMeshInfo / GetGpuTopology / GetGpuCsrPattern
+   and must be released with DestroyHostMesh. */
+int BuildHostMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, BiofemGpuMesh **out);
+int DestroyHostMesh(BiofemGpuMesh *m);
+
+/* Centroid basis-derivative tables the kernels use: 11 tables x 5 rows x 16
+   (table 0 = regular patch, active_strain.c:69-88; table v = the one-step
+   subdivision weights of valence v, active_strain.c:594-666). */
+int GetGpuBasisTables(double *out);
+
+const char *BiofemGpuLastError(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

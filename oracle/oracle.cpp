@@ -799,6 +799,58 @@ int oracle_setup(int n_v, int n_elmt, const int *tri, const double *xyz0,
   return 0;
 }
 
+/* Same as oracle_setup but with the subdivision topology supplied by the
+   caller (patch/ire/val/irv, the ghost triangles and the reflected interior
+   node of every ghost): skips the O(N^2) GlobalGhostInit/IrrVer/Patch
+   searches for large meshes.  Tables must equal the reference's (the
+   product's O(N) builder is checked bitwise against them). */
+int oracle_setup_given_topology(int n_v, int n_elmt, const int *tri_all, const double *xyz0_full,
+                                int n_edge, const int *n_bnodes, const int *bnodes,
+                                const int *patch16, const int *ire, const int *val, const int *irv,
+                                const int *ghost_nv3, const double *fib, const double *gamma_scale,
+                                int n_qp, int c33_iters, double mu, double K, double h0,
+                                double gamma, double pressure, int clamp_edge0)
+{
+  delete g_body;
+  g_body = new Body();
+  Body &B = *g_body;
+  Mesh &m = B.m;
+  Params &P = B.P;
+  if (gauss_rule(n_qp, P.theta, P.w)) return 63;
+  if (c33_iters < 1) return 62;
+  P.n_qp = n_qp; P.c33_iters = c33_iters; P.mu = mu; P.K = K; P.h0 = h0;
+  P.gamma = gamma; P.pressure = pressure; P.clamp = clamp_edge0;
+  m.n_v = n_v; m.n_elmt = n_elmt; m.n_edge = n_edge;
+  m.n_bnodes.assign(n_bnodes, n_bnodes + n_edge);
+  int sum = 0;
+  for (int e = 0; e < n_edge; e++) sum += n_bnodes[e];
+  m.n_ghosts = sum;
+  m.bnodes.assign(bnodes, bnodes + sum);
+  const int ntri = n_elmt + 2 * sum, ntot = n_v + sum;
+  m.nv1.resize(ntri); m.nv2.resize(ntri); m.nv3.resize(ntri);
+  for (int t = 0; t < ntri; t++) { m.nv1[t] = tri_all[3 * t]; m.nv2[t] = tri_all[3 * t + 1]; m.nv3[t] = tri_all[3 * t + 2]; }
+  m.x0.resize(ntot); m.y0.resize(ntot); m.z0.resize(ntot);
+  for (int v = 0; v < ntot; v++) { m.x0[v] = xyz0_full[3 * v]; m.y0[v] = xyz0_full[3 * v + 1]; m.z0[v] = xyz0_full[3 * v + 2]; }
+  m.fib.assign(fib, fib + 3 * n_elmt);
+  m.gscale.assign(gamma_scale, gamma_scale + n_elmt);
+  m.ire.assign(ire, ire + n_elmt); m.val.assign(val, val + n_elmt); m.irv.assign(irv, irv + n_elmt);
+  m.patch.assign(patch16, patch16 + 16 * n_elmt);
+  m.ghost_nv3.assign(ghost_nv3, ghost_nv3 + sum);
+  m.dA0.assign(n_elmt, 0.0);
+  for (int ec = 0; ec < n_elmt; ec++) {
+    double dA; V3<double> n;
+    area_normal(m, m.x0.data(), m.y0.data(), m.z0.data(), ec, dA, n);
+    m.dA0[ec] = dA;
+  }
+  B.ref.resize(n_elmt);
+  for (int ec = 0; ec < n_elmt; ec++) {
+    int rc = ref_elem(m, P, ec, B.ref[ec]);
+    if (rc) return rc;
+  }
+  B.ready = true;
+  return 0;
+}
+
 int oracle_set_threads(int n) { g_threads = n > 0 ? n : 1; return 0; }
 
 int oracle_sizes(int *n_ghosts, int *n_dof)
@@ -892,6 +944,63 @@ int oracle_irregular_weights(int v, double *out)
 {
   const int nen = v + 6;
   return irregular_weights(v, out, out + nen, out + 2 * nen, out + 3 * nen, out + 4 * nen);
+}
+
+/* CPU baseline of R+K: for elements [e0, e1) evaluate the element force and
+   its derivative w.r.t. the element's patch coordinates (forward mode over
+   all 3*nen patch coordinates at once, Dual<48>), using `threads` OpenMP
+   threads, then assemble the element forces in element order.  Returns a
+   checksum in *chk (keeps the work observable).  This is the reference's
+   own per-element algorithm (active_strain.c) with its tangent taken
+   exactly; the reference itself has no tangent. */
+int oracle_rk_sample(const double *x, int e0, int e1, int threads, double *chk)
+{
+  if (!g_body || !g_body->ready) return 58;
+  const Body &B = *g_body;
+  const Mesh &m = B.m;
+  if (e0 < 0 || e1 > m.n_elmt || e0 > e1) return 63;
+  const int ntot = m.n_v + m.n_ghosts;
+  std::vector<double> xb(ntot), yb(ntot), zb(ntot);
+  for (int v = 0; v < m.n_v; v++) { xb[v] = x[3 * v]; yb[v] = x[3 * v + 1]; zb[v] = x[3 * v + 2]; }
+  for (int v = m.n_v; v < ntot; v++) { xb[v] = m.x0[v]; yb[v] = m.y0[v]; zb[v] = m.z0[v]; }
+  global_ghost(m, xb.data(), yb.data(), zb.data());
+  const int ne = e1 - e0;
+  std::vector<double> part((size_t)ne, 0.0);
+  std::vector<int> rcs(ne, 0);
+#ifdef _OPENMP
+#pragma omp parallel num_threads(threads > 0 ? threads : 1)
+#endif
+  {
+    /* per-thread coordinate copies carrying the element's seeds */
+    std::vector<Dual<48>> xd(ntot), yd(ntot), zd(ntot);
+    for (int v = 0; v < ntot; v++) { xd[v] = Dual<48>(xb[v]); yd[v] = Dual<48>(yb[v]); zd[v] = Dual<48>(zb[v]); }
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 8)
+#endif
+    for (int k = 0; k < ne; k++) {
+      const int ec = e0 + k;
+      const int nen = (m.ire[ec] == 0) ? 12 : m.val[ec] + 6;
+      const int *pt = &m.patch[16 * ec];
+      for (int a = 0; a < nen; a++) {
+        const int n = pt[a];
+        xd[n].d[3 * a] = 1.0; yd[n].d[3 * a + 1] = 1.0; zd[n].d[3 * a + 2] = 1.0;
+      }
+      Dual<48> Fb[48];
+      rcs[k] = elem_forces<Dual<48>>(m, B.P, ec, B.ref[ec], xd.data(), yd.data(), zd.data(), Fb);
+      double s = 0.0;
+      for (int i = 0; i < 3 * nen; i++) { s += Fb[i].v; for (int j = 0; j < 3 * nen; j++) s += 1e-3 * Fb[i].d[j]; }
+      part[k] = s;
+      for (int a = 0; a < nen; a++) {
+        const int n = pt[a];
+        for (int j = 0; j < 48; j++) { xd[n].d[j] = 0.0; yd[n].d[j] = 0.0; zd[n].d[j] = 0.0; }
+      }
+    }
+  }
+  for (int k = 0; k < ne; k++) if (rcs[k]) return rcs[k];
+  double c = 0.0;
+  for (int k = 0; k < ne; k++) c += part[k];
+  *chk = c;
+  return 0;
 }
 
 void oracle_teardown(void) { delete g_body; g_body = nullptr; }

@@ -84,6 +84,40 @@ class Oracle(_Base):
         path = build_oracle.build() if build else build_oracle.LIB
         self.lib = ctypes.CDLL(str(path))
 
+    def setup_given_topology(self, mesh, w, topo: dict, mu: float, bulk: float, h0: float,
+                             gamma: float = 1.0, clamp: bool = True):
+        """oracle_setup with the subdivision tables supplied (dict with patch,
+        ire, val, irv, gtri, xyz0_full as returned by GetGpuTopology)."""
+        ng = int(mesh.n_bnodes.sum())
+        gtri = np.ascontiguousarray(topo["gtri"], dtype=np.int32)
+        # the reflected interior node of ghost g: the ghost's main triangle is
+        # (nv1, nv2, ghost); recover nv3 from x_g = x_nv2 + x_nv1 - x_nv3 is not
+        # possible from positions alone, so take it from the caller if present
+        gnv3 = np.ascontiguousarray(topo["ghost_nv3"], dtype=np.int32)
+        keep = dict(gtri=gtri, x=np.ascontiguousarray(topo["xyz0_full"], dtype=np.float64),
+                    nb=np.ascontiguousarray(mesh.n_bnodes, dtype=np.int32),
+                    bn=np.ascontiguousarray(mesh.bnodes, dtype=np.int32),
+                    patch=np.ascontiguousarray(topo["patch"], dtype=np.int32),
+                    ire=np.ascontiguousarray(topo["ire"], dtype=np.int32),
+                    val=np.ascontiguousarray(topo["val"], dtype=np.int32),
+                    irv=np.ascontiguousarray(topo["irv"], dtype=np.int32), gnv3=gnv3,
+                    fib=np.ascontiguousarray(mesh.fib, dtype=np.float64),
+                    gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64))
+        self._keep = keep
+        f = self.lib.oracle_setup_given_topology
+        f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                      _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
+        rc = f(mesh.n_v, mesh.n_elmt, _p(keep["gtri"]), _p(keep["x"]), mesh.n_edge, _p(keep["nb"]), _p(keep["bn"]),
+               _p(keep["patch"]), _p(keep["ire"]), _p(keep["val"]), _p(keep["irv"]), _p(keep["gnv3"]),
+               _p(keep["fib"]), _p(keep["gs"]), w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure, int(clamp))
+        if rc:
+            raise RuntimeError(f"oracle_setup_given_topology failed with code {rc}")
+        ng_, nd = _c_int(), _c_int()
+        self.lib.oracle_sizes(ctypes.byref(ng_), ctypes.byref(nd))
+        self.n_v, self.n_elmt = mesh.n_v, mesh.n_elmt
+        self.n_ghosts, self.n_dof = ng_.value, nd.value
+        return self
+
     def set_threads(self, n: int):
         self.lib.oracle_set_threads(int(n))
 

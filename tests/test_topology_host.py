@@ -1,0 +1,82 @@
+"""The O(N) topology builder and the basis tables of the product library,
+checked against the oracle (which is bitwise-pinned to the reference) on the
+CPU: no GPU is touched (BuildHostMesh makes no CUDA call)."""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from biofem import configs
+from biofem.gpu import GpuShell, basis_tables
+from biofem.mesh import flat_membrane, set_random_activation
+
+SHAPES = [(6, 5), (9, 7), (12, 8), (10, 6), (32, 24), (17, 3), (3, 11), (40, 2)]
+
+
+@pytest.mark.parametrize("nx,ny", SHAPES)
+def test_host_topology_equals_oracle(nx, ny, oracle_lib):
+    w = configs.small(nx, ny, index=30)
+    m = w.build_mesh()
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0)
+    to = o.topology()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    th = sh.topology()
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        assert np.array_equal(th[k], getattr(to, k)), k
+    sh.close()
+
+
+def test_host_topology_matches_reference_checksum_C2():
+    """C2 (98,304 triangles): the reference's O(N^2) Patch() output is stored
+    as SHA-256 checksums in tests/golden/C2_flat_256x192.npz."""
+    import hashlib
+    path = GOLDEN / "C2_flat_256x192.npz"
+    d = np.load(path)
+    meta = json.loads(str(d["meta"]))
+    w = configs.C2
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    t = sh.topology()
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    assert sha(t["patch"]) == meta["sha_patch"]
+    assert sha(t["ire"]) == meta["sha_ire"]
+    assert sha(t["val"]) == meta["sha_val"]
+    assert sha(t["irv"]) == meta["sha_irv"]
+    assert sha(t["gtri"]) == meta["sha_gtri"]
+    sh.close()
+
+
+def test_basis_tables_equal_oracle_subdivision_weights(oracle_lib):
+    tab = basis_tables()
+    for v in range(3, 11):
+        ref = oracle_lib.irregular_weights(v)
+        assert np.array_equal(tab[v, :, : v + 6], ref), v
+        assert not tab[v, :, v + 6:].any()
+
+
+def test_pattern_is_symmetric_structure_on_free_rows():
+    w = configs.small(10, 8, index=31)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    rowptr, colind = sh.pattern()
+    nb = sh.info.n_v + sh.info.n_ghosts
+    assert rowptr[-1] == sh.nnzb and np.all(np.diff(rowptr) >= 1)
+    for i in range(nb):
+        cols = colind[rowptr[i]:rowptr[i + 1]]
+        assert np.all(np.diff(cols) > 0) and i in cols
+        assert cols.max() < sh.info.n_v or i >= sh.info.n_v  # ghost columns are folded away
+    sh.close()
+
+
+def test_invalid_inputs_raise():
+    from biofem.gpu import BiofemError
+    w = configs.small(6, 5, index=32)
+    m = w.build_mesh()
+    bad = configs.Workload("bad", 6, 5, n_qp=7)
+    with pytest.raises(BiofemError) as ei:
+        GpuShell(m, bad, configs.MU, configs.BULK, configs.H0, host_only=True)
+    assert ei.value.code == 63
+    m.tri[0, 0] = 10**6
+    with pytest.raises(BiofemError):
+        GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
