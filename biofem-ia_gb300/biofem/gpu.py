@@ -64,7 +64,7 @@ EXPORTS = ["InitGpuWorkspace", "DestroyGpuWorkspace", "PrepareGpuMesh", "Destroy
            "RunGpuResidualDevice", "RunGpuResidualJacobianDevice", "BiofemGpuSync", "FormFunctionFEMGpu",
            "FormJacobianFEMGpu", "GetGpuLaunchCounts", "BuildHostMesh", "DestroyHostMesh",
            "GetGpuBasisTables", "BiofemGpuLastError", "EnableGpuKernelTiming", "GetGpuKernelTimes",
-           "GetGpuGhostMap"]
+           "GetGpuGhostMap", "RunGpuResidualNoAlloc"]
 
 
 def load_library(path: Path | str | None = None) -> ctypes.CDLL:
@@ -91,6 +91,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
     lib.RunGpuResidualJacobian.argtypes = [vp, vp, vp, vp]
     lib.RunGpuResidualDevice.argtypes = [vp, vp, vp, vp]
     lib.RunGpuResidualJacobianDevice.argtypes = [vp, vp, vp, vp, vp]
+    lib.RunGpuResidualNoAlloc.argtypes = [vp, vp, vp, vp]
     lib.BiofemGpuSync.argtypes = [vp, vp]
     lib.GetGpuLaunchCounts.argtypes = [vp, vp, vp]
     lib.GetGpuBasisTables.argtypes = [vp]
@@ -213,6 +214,12 @@ class GpuShell:
     def jacobian_device(self, d_x: int, d_R: int, d_K: int, stream: int = 0):
         _check(self.lib, self.lib.RunGpuResidualJacobianDevice(self.handle, ctypes.c_void_p(d_x), ctypes.c_void_p(d_R),
                                                                ctypes.c_void_p(d_K), ctypes.c_void_p(stream or None)))
+
+    def residual_device_noalloc(self, d_x: int, d_R: int, stream: int = 0):
+        """RunGpuResidualNoAlloc: same residual, work arrays in the library's
+        fixed device array (no allocation; meshes up to ~19k triangles)."""
+        _check(self.lib, self.lib.RunGpuResidualNoAlloc(self.handle, ctypes.c_void_p(d_x), ctypes.c_void_p(d_R),
+                                                        ctypes.c_void_p(stream or None)))
 
     def sync(self, stream: int = 0):
         _check(self.lib, self.lib.BiofemGpuSync(self.handle, ctypes.c_void_p(stream or None)))

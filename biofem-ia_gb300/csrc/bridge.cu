@@ -151,6 +151,17 @@ struct BiofemGpuMesh_ {
 };
 
 static std::set<BiofemGpuMesh *> g_meshes;
+
+namespace biofem {
+/* accessors for the no-allocation residual (noalloc.cu) */
+int noalloc_fail(int code, const std::string &msg) { return fail(code, msg); }
+const DevMesh *mesh_devview(const BiofemGpuMesh *m, const KParams **kp)
+{
+  if (!m || !m->dm.patch) return nullptr;
+  *kp = &m->kp;
+  return &m->dm;
+}
+} /* namespace biofem */
 static KernelTimer &timer_of(BiofemGpuMesh *m) { return m->timer; }
 
 /* device-variant stream argument: a cudaStream_t; NULL is the CUDA default stream */

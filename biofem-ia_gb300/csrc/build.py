@@ -19,7 +19,7 @@ ROOT = PKG.parent
 LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libbiofem_gpu.so"
 OBJ_DIR = LIB_DIR / "obj"
-CUDA_SOURCES = ["kernels.cu", "bridge.cu"]
+CUDA_SOURCES = ["kernels.cu", "bridge.cu", "noalloc.cu"]
 CXX_SOURCES = ["topology.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

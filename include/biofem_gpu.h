@@ -113,6 +113,21 @@ int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void 
 int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, double *d_Kvals, void *stream);
 int BiofemGpuSync(BiofemGpuMesh *m, void *stream);
 
+/* Residual for callers that cannot allocate device memory when they call:
+   a serving loop or host code that has reserved a fixed HBM budget (its own
+   pool) and must not have the library reach cudaMalloc, which can fail under
+   the budget, fragments the pool and synchronises the device.  No
+   counterpart in the reference.  Same result as RunGpuResidualDevice for a
+   prepared handle; d_x / d_R are device pointers the caller owns; allocates
+   nothing.  The per-call work arrays live in one fixed 8 MiB device array
+   (1,048,576 doubles) that each GPU loading the library holds until exit:
+   meshes needing more than 4*(n_v+n_ghosts) + 51*n_elmt + 1 doubles (about
+   19,000 triangles) are rejected with error 63.  All calls share that array:
+   calls that overlap on the GPU race and must be serialised.  The first call
+   on a device looks up the array's address (once per device); make it before
+   any stream capture. */
+int RunGpuResidualNoAlloc(BiofemGpuMesh *m, const double *d_x, double *d_R, void *stream);
+
 /* SNES-callback-shaped wrappers (main.c:120 FormFunctionFEM(SNES, Vec, Vec,
    void*) and the Jacobian slot SNESSetJacobian, main.c:462-466) taking host
    arrays; ctx is the BiofemGpuMesh*.  `snes` is passed through unused. */
