@@ -254,6 +254,40 @@ def run_ours(args):
             r_ms.append(r0.elapsed_time(r1))
         sh.sync(sp)
 
+    # FP32-bulk form on the same workload: residual FP64, tangent FP32
+    from biofem.gpu import BIOFEM_FP32_BULK
+    s32 = GpuShell(mesh, w, configs.MU, configs.BULK, configs.H0, precision=BIOFEM_FP32_BULK)
+    dK32 = torch.empty(9 * s32.nnzb, dtype=torch.float32, device=dev)
+    dR32 = torch.empty_like(dx)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            s32.jacobian_device(dx.data_ptr(), dR32.data_ptr(), dK32.data_ptr(), sp)
+        s32.sync(sp)
+        f_ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            r0.record(stream)
+            s32.jacobian_device(dx.data_ptr(), dR32.data_ptr(), dK32.data_ptr(), sp)
+            r1.record(stream)
+            r1.synchronize()
+            f_ms.append(r0.elapsed_time(r1))
+        s32.sync(sp)
+        s32.kernel_timing(True)
+        n32 = s32.launch_counts()[1]
+        for _ in range(args.steps):
+            flush.zero_()
+            s32.jacobian_device(dx.data_ptr(), dR32.data_ptr(), dK32.data_ptr(), sp)
+        k32, c32 = s32.kernel_times(n32)
+        s32.kernel_timing(False)
+    torch.cuda.synchronize()
+    K64h = dK.cpu().numpy()
+    K32h = dK32.cpu().numpy().astype(np.float64)
+    fp32_frob = float(np.linalg.norm(K32h - K64h) / np.linalg.norm(K64h))
+    fp32_rdiff = float(np.abs(dR32.cpu().numpy() - dR.cpu().numpy()).max())
+    f32_step = sum(f_ms) / len(f_ms)
+    s32.close()
+
     # end to end through the public host API: pinned x in, R and K out
     hx = torch.tensor(x_host).pin_memory()
     hR = torch.empty(sh.n_dof, dtype=torch.float64).pin_memory()
@@ -323,6 +357,13 @@ def run_ours(args):
         "residual_only": {"ms_per_step": sum(r_ms) / len(r_ms), "elems_per_s": ne / (sum(r_ms) / len(r_ms) * 1e-3)},
         "e2e": {"value": world * ne / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * sh.n_dof,
                 "d2h_bytes_per_step": 8 * sh.n_dof + 72 * sh.nnzb, "host_equals_device_R": same},
+        "fp32_bulk": {"ms_per_step": f32_step, "elems_per_s": world * ne / (f32_step * 1e-3),
+                      "speedup_vs_fp64": ms / f32_step,
+                      "K_frobenius_rel_err_vs_fp64": fp32_frob, "R_max_abs_diff_vs_fp64": fp32_rdiff,
+                      "kernels_ms": dict(zip(["positions", "elem_residual_fp64", "elem_tangent_fp32", "node_gather",
+                                              "block_gather_fp32", "scale"], (k32 / max(c32, 1)).tolist())),
+                      "roofline_hbm_frac": (b_alg - 36 * sh.nnzb) / (f32_step * 1e-3) / 1e9 / hbm_peak,
+                      "note": "residual FP64, tangent FP32 on patch-local shifted coordinates, K values FP32"},
         "gpu_launches": n_launch_jac * args.steps,
         "clocks": clk,
     }

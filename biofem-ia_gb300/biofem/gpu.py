@@ -53,7 +53,7 @@ class Params(ctypes.Structure):
 class MeshInfo(ctypes.Structure):
     _fields_ = [("n_v", ctypes.c_int32), ("n_ghosts", ctypes.c_int32), ("n_elmt", ctypes.c_int32),
                 ("n_dof", ctypes.c_int32), ("n_irregular", ctypes.c_int32), ("nnzb", ctypes.c_int64),
-                ("n_contrib", ctypes.c_int64), ("device_bytes", ctypes.c_int64)]
+                ("n_contrib", ctypes.c_int64), ("device_bytes", ctypes.c_int64), ("precision", ctypes.c_int32)]
 
 
 _LIB = None
@@ -149,6 +149,8 @@ class GpuShell:
         self.info = info
         self.n_dof = info.n_dof
         self.nnzb = info.nnzb
+        self.precision = precision
+        self.k_dtype = np.float64 if precision == BIOFEM_FP64 else np.float32
 
     def close(self):
         if self.handle:
@@ -201,7 +203,7 @@ class GpuShell:
         if x.size != self.n_dof:
             raise BiofemError(63, f"x has {x.size} entries, expected {self.n_dof}")
         R = np.empty(self.n_dof)
-        K = np.empty((self.nnzb, 3, 3))
+        K = np.empty((self.nnzb, 3, 3), dtype=self.k_dtype)
         _check(self.lib, self.lib.RunGpuResidualJacobian(self.handle, _ptr(x), _ptr(R), _ptr(K)))
         return R, K
 
@@ -246,7 +248,7 @@ class GpuShell:
         import scipy.sparse as sp
         rowptr, colind = self.pattern()
         nb = self.info.n_v + self.info.n_ghosts
-        return sp.bsr_matrix((K.reshape(-1, 3, 3), colind, rowptr), shape=(3 * nb, 3 * nb))
+        return sp.bsr_matrix((K.reshape(-1, 3, 3).astype(np.float64), colind, rowptr), shape=(3 * nb, 3 * nb))
 
 
 def FormFunctionFEM(snes, x: np.ndarray, R: np.ndarray, ctx: GpuShell) -> int:

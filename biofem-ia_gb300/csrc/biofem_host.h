@@ -45,6 +45,7 @@ struct DevMesh {
   const int *einfo;          /* ne: nen | (table << 8) */
   const int *ecorner;        /* ne: patch slots of nv1, nv2, nv3 (5 bits each) */
   const double *eref;        /* (kRefPerQp*nq + kRefPerElem) * ne, SoA */
+  const float *erefF;        /* the same in FP32 (FP32-bulk handles only) */
   const double *ntab;        /* kNumTables * 5 * 16 basis-derivative tables */
   const int *etri;           /* 3*ne triangle corners (pressure) */
   const int *ghost3;         /* 3*ng (nv1, nv2, nv3) */
@@ -63,7 +64,8 @@ struct DevMesh {
   double *pos;               /* 4*nt padded positions */
   double *fb;                /* 48*ne element forces */
   double *fp;                /* 3*ne element pressure forces */
-  double *ke;                /* 9*total blocks element matrices */
+  double *ke;                /* 9*total blocks element matrices (FP64 handles) */
+  float *keF;                /* 9*total blocks element matrices (FP32-bulk handles) */
   int *status;               /* device error flag */
   unsigned long long *fmax;  /* max |Fext| as ordered bits */
 };
@@ -76,6 +78,10 @@ int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream);
 int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream);
 int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream);
 int launch_scale(const DevMesh &m, const KParams &p, double *R, double *K, void *stream);
+int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);
+int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream);
+int launch_scale_f32(const DevMesh &m, const KParams &p, double *R, float *K, void *stream);
+int launch_to_float(const double *a, float *b, long long n, void *stream);
 int upload_tables(double *d_ntab);
 void host_tables(double *out);   /* kNumTables*5*16 host copy of the basis tables */
 

@@ -146,7 +146,8 @@ struct BiofemGpuMesh_ {
   size_t bytes = 0;
   std::vector<void *> allocs;
   DevMesh dm{};
-  double *d_x = nullptr, *d_R = nullptr, *d_K = nullptr;   /* staging for host-array calls */
+  double *d_x = nullptr, *d_R = nullptr;   /* staging for host-array calls */
+  void *d_K = nullptr;                      /* K values: double (FP64) or float (FP32-bulk) */
   KernelTimer timer;
 };
 
@@ -450,7 +451,6 @@ int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofe
   int rc = check_params(*params);
   if (rc) return rc;
   if (!g_init) { rc = InitGpuWorkspace(); if (rc) return rc; }
-  if (params->precision != BIOFEM_FP64) return fail(56, "FP32-bulk form is not built into this library yet");
   BiofemGpuMesh *m = new BiofemGpuMesh();
   m->prm = *params;
   std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx, blkrow, cidx;
@@ -485,20 +485,36 @@ int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofe
   const size_t nref = (size_t)(kRefPerQp * kp.nq + kRefPerElem) * ne;
   if ((rc = dupload(m, &d_fib, fib)) || (rc = dupload(m, &d_gsc, gsc)) || (rc = dalloc(m, &d_eref, nref)) ||
       (rc = dalloc(m, &dm.pos, 4 * (size_t)nt)) || (rc = dalloc(m, &dm.fb, 48 * (size_t)ne)) ||
-      (rc = dalloc(m, &dm.fp, 3 * (size_t)ne)) || (rc = dalloc(m, &dm.ke, 9 * (size_t)(kofs.empty() ? 0 : kofs.back() + 256))) ||
+      (rc = dalloc(m, &dm.fp, 3 * (size_t)ne)) ||
       (rc = dalloc(m, &dm.status, 1)) || (rc = dalloc(m, &dm.fmax, 1)) ||
-      (rc = dalloc(m, &m->d_x, 3 * (size_t)nt)) || (rc = dalloc(m, &m->d_R, 3 * (size_t)nt)) ||
-      (rc = dalloc(m, &m->d_K, 9 * (size_t)m->nnzb))) {
+      (rc = dalloc(m, &m->d_x, 3 * (size_t)nt)) || (rc = dalloc(m, &m->d_R, 3 * (size_t)nt))) {
     free_mesh(m);
     return rc;
   }
+  const size_t keblocks = (size_t)(kofs.empty() ? 0 : kofs.back() + 256);
+  float *d_erefF = nullptr;
+  if (params->precision == BIOFEM_FP64) {
+    double *dK = nullptr;
+    if ((rc = dalloc(m, &dm.ke, 9 * keblocks)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb))) { free_mesh(m); return rc; }
+    m->d_K = dK;
+  } else {
+    float *dK = nullptr;
+    if ((rc = dalloc(m, &dm.keF, 9 * keblocks)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb)) ||
+        (rc = dalloc(m, &d_erefF, nref))) { free_mesh(m); return rc; }
+    m->d_K = dK;
+  }
   dm.eref = d_eref;
+  dm.erefF = d_erefF;
   CUDA_TRY(cudaMemset(dm.status, 0, sizeof(int)));
   CUDA_TRY(cudaMemset(dm.fp, 0, 3 * sizeof(double) * (size_t)ne));
   /* reference positions (ghosts included) -> one-time reference geometry */
   if ((rc = launch_positions(dm, kp, dm.X, g_stream)) || (rc = launch_ref_prep(dm, kp, d_fib, d_gsc, d_eref, g_stream))) {
     free_mesh(m);
     return fail(76, std::string("reference preparation launch: ") + cudaGetErrorString((cudaError_t)rc));
+  }
+  if (d_erefF && (rc = launch_to_float(d_eref, d_erefF, (long long)nref, g_stream))) {
+    free_mesh(m);
+    return fail(76, std::string("reference conversion launch: ") + cudaGetErrorString((cudaError_t)rc));
   }
   cudaError_t e = cudaStreamSynchronize(g_stream);
   if (e != cudaSuccess) { free_mesh(m); return fail(76, std::string("reference preparation: ") + cudaGetErrorString(e)); }
@@ -521,6 +537,7 @@ int GetGpuMeshInfo(const BiofemGpuMesh *m, BiofemMeshInfo *info)
   info->n_dof = 3 * (m->topo.n_v + m->topo.n_ghosts);
   info->n_irregular = m->n_irregular;
   info->nnzb = m->nnzb; info->n_contrib = m->ncontrib; info->device_bytes = (int64_t)m->bytes;
+  info->precision = m->prm.precision;
   return 0;
 }
 
@@ -559,9 +576,11 @@ int GetGpuCsrPattern(const BiofemGpuMesh *m, int32_t *rowptr, int32_t *colind)
 
 int GetGpuLaunchCounts(const BiofemGpuMesh *m, int32_t *res, int32_t *jac)
 {
-  (void)m;
+  if (!m) return fail(85, "null argument");
   if (res) *res = 4;   /* positions, element residual, node gather, scale */
-  if (jac) *jac = 5;   /* positions, element tangent, node gather, block gather, scale */
+  /* FP64: positions, element tangent, node gather, block gather, scale;
+     FP32-bulk adds the FP64 element residual */
+  if (jac) *jac = m->prm.precision == BIOFEM_FP64 ? 5 : 6;
   return 0;
 }
 
@@ -594,17 +613,30 @@ int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void 
   return 0;
 }
 
-int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, double *d_K, void *stream)
+int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream)
 {
   if (!m || !d_x || !d_R || !d_K) return fail(85, "null argument");
+  if (!m->dm.patch) return fail(58, "host-only handle");
   cudaStream_t st = pick_stream(stream);
   int rc = 0;
   tmark(m, st, 0);
-  if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
-  if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 2); }
-  if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 3); }
-  if (!rc) { rc = launch_block_gather(m->dm, m->kp, d_K, st); tmark(m, st, 4); }
-  if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, d_K, st); tmark(m, st, 5); }
+  if (m->prm.precision == BIOFEM_FP64) {
+    double *K = static_cast<double *>(d_K);
+    if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
+    if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 2); }
+    if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 3); }
+    if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st); tmark(m, st, 4); }
+    if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, K, st); tmark(m, st, 5); }
+  } else {
+    /* FP32-bulk: residual in FP64, tangent (D, K_e, K) in FP32 */
+    float *K = static_cast<float *>(d_K);
+    if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
+    if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
+    if (!rc) { rc = launch_elem_tangent_f32(m->dm, m->kp, st); tmark(m, st, 3); }
+    if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
+    if (!rc) { rc = launch_block_gather_f32(m->dm, m->kp, K, st); tmark(m, st, 5); }
+    if (!rc) { rc = launch_scale_f32(m->dm, m->kp, d_R, K, st); tmark(m, st, 6); }
+  }
   if (rc) return fail(76, std::string("jacobian launch: ") + cudaGetErrorString((cudaError_t)rc));
   timer_collect(m);
   return 0;
@@ -659,15 +691,16 @@ int RunGpuResidual(BiofemGpuMesh *m, const double *x, double *R)
   return BiofemGpuSync(m, g_stream);
 }
 
-int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, double *K)
+int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K)
 {
   if (!m || !x || !K) return fail(85, "null argument");
   const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
+  const size_t kbytes = 9 * (size_t)m->nnzb * (m->prm.precision == BIOFEM_FP64 ? sizeof(double) : sizeof(float));
   CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, g_stream));
   int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, m->d_K, g_stream);
   if (rc) return rc;
   if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
-  CUDA_TRY(cudaMemcpyAsync(K, m->d_K, 9 * (size_t)m->nnzb * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+  CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, g_stream));
   return BiofemGpuSync(m, g_stream);
 }
 
@@ -677,7 +710,7 @@ int FormFunctionFEMGpu(void *snes, const double *x, double *R, void *ctx)
   return RunGpuResidual(reinterpret_cast<BiofemGpuMesh *>(ctx), x, R);
 }
 
-int FormJacobianFEMGpu(void *snes, const double *x, double *K, void *ctx)
+int FormJacobianFEMGpu(void *snes, const double *x, void *K, void *ctx)
 {
   (void)snes;
   return RunGpuResidualJacobian(reinterpret_cast<BiofemGpuMesh *>(ctx), x, nullptr, K);

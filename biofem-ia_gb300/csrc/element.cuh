@@ -44,26 +44,37 @@
 namespace biofem {
 
 /* ---------------- scalar types ---------------- */
-struct D1 { double v, d; };
+/* One-direction dual number over the real type R (double or float). */
+template <class R> struct D1 { R v, d; };
+typedef D1<double> D1d;
+typedef D1<float> D1f;
 
-__host__ __device__ __forceinline__ double val(double a) { return a; }
-__host__ __device__ __forceinline__ double val(const D1 &a) { return a.v; }
+template <class R> __host__ __device__ __forceinline__ R val(R a) { return a; }
+template <class R> __host__ __device__ __forceinline__ R val(const D1<R> &a) { return a.v; }
 
-__host__ __device__ __forceinline__ D1 operator+(D1 a, D1 b) { return {a.v + b.v, a.d + b.d}; }
-__host__ __device__ __forceinline__ D1 operator-(D1 a, D1 b) { return {a.v - b.v, a.d - b.d}; }
-__host__ __device__ __forceinline__ D1 operator-(D1 a) { return {-a.v, -a.d}; }
-__host__ __device__ __forceinline__ D1 operator*(D1 a, D1 b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
-__host__ __device__ __forceinline__ D1 operator+(D1 a, double b) { return {a.v + b, a.d}; }
-__host__ __device__ __forceinline__ D1 operator+(double a, D1 b) { return {a + b.v, b.d}; }
-__host__ __device__ __forceinline__ D1 operator-(D1 a, double b) { return {a.v - b, a.d}; }
-__host__ __device__ __forceinline__ D1 operator-(double a, D1 b) { return {a - b.v, -b.d}; }
-__host__ __device__ __forceinline__ D1 operator*(D1 a, double b) { return {a.v * b, a.d * b}; }
-__host__ __device__ __forceinline__ D1 operator*(double a, D1 b) { return {a * b.v, a * b.d}; }
-__host__ __device__ __forceinline__ D1 operator/(D1 a, D1 b) { double q = a.v / b.v; return {q, (a.d - q * b.d) / b.v}; }
-__host__ __device__ __forceinline__ D1 operator/(double a, D1 b) { double q = a / b.v; return {q, -q * b.d / b.v}; }
-__host__ __device__ __forceinline__ D1 operator/(D1 a, double b) { return {a.v / b, a.d / b}; }
-__host__ __device__ __forceinline__ D1 dsqrt(D1 a) { double r = sqrt(a.v); return {r, a.d / (2.0 * r)}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator+(D1<R> a, D1<R> b) { return {a.v + b.v, a.d + b.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator-(D1<R> a, D1<R> b) { return {a.v - b.v, a.d - b.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator-(D1<R> a) { return {-a.v, -a.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator*(D1<R> a, D1<R> b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator+(D1<R> a, R b) { return {a.v + b, a.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator+(R a, D1<R> b) { return {a + b.v, b.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator-(D1<R> a, R b) { return {a.v - b, a.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator-(R a, D1<R> b) { return {a - b.v, -b.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator*(D1<R> a, R b) { return {a.v * b, a.d * b}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator*(R a, D1<R> b) { return {a * b.v, a * b.d}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator/(D1<R> a, D1<R> b) { R q = a.v / b.v; return {q, (a.d - q * b.d) / b.v}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator/(R a, D1<R> b) { R q = a / b.v; return {q, -q * b.d / b.v}; }
+template <class R> __host__ __device__ __forceinline__ D1<R> operator/(D1<R> a, R b) { return {a.v / b, a.d / b}; }
+__host__ __device__ __forceinline__ D1d dsqrt(D1d a) { double r = sqrt(a.v); return {r, a.d / (2.0 * r)}; }
+__host__ __device__ __forceinline__ D1f dsqrt(D1f a) { float r = sqrtf(a.v); return {r, a.d / (2.0f * r)}; }
 __host__ __device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
+__host__ __device__ __forceinline__ float dsqrt(float a) { return sqrtf(a); }
+__host__ __device__ __forceinline__ double dabs(double a) { return fabs(a); }
+__host__ __device__ __forceinline__ float dabs(float a) { return fabsf(a); }
+
+/* real type underlying a scalar */
+template <class T> struct RealOf { typedef T type; };
+template <class R> struct RealOf<D1<R>> { typedef R type; };
 
 template <class T> struct V3 { T x, y, z; };
 template <class T> __host__ __device__ __forceinline__ V3<T> operator+(const V3<T> &a, const V3<T> &b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
@@ -76,38 +87,54 @@ template <class T> __host__ __device__ __forceinline__ V3<T> cross(const V3<T> &
 }
 
 /* Reference constants of one (element, qp), see the header comment. */
-struct QpRef {
-  double gc00, gc11, gc01, gc22;   /* G^-1 entries used by S */
-  double s[3], t[3];
-  double rho;
-  double av[3], aw[3], ae[3];      /* A^T v, A^T w, A^T e3 */
+template <class R> struct QpRef {
+  R gc00, gc11, gc01, gc22;   /* G^-1 entries used by S */
+  R s[3], t[3];
+  R rho;
+  R av[3], aw[3], ae[3];      /* A^T v, A^T w, A^T e3 */
 };
 
+/* Material / quadrature constants in the working precision R. */
+template <class R> struct EPar {
+  R mu, K, hhalf;
+  R theta[kMaxQp], w[kMaxQp];
+  int nq, iters;
+};
+
+template <class R> __host__ __device__ __forceinline__ EPar<R> epar(const KParams &p)
+{
+  EPar<R> e;
+  e.mu = (R)p.mu; e.K = (R)p.K; e.hhalf = (R)p.hhalf; e.nq = p.nq; e.iters = p.iters;
+  for (int q = 0; q < kMaxQp; q++) { e.theta[q] = (R)p.theta[q]; e.w[q] = (R)p.w[q]; }
+  return e;
+}
+
 /* Quadratic form (A^T x)^T Ci (A^T y) with Ci = [[c00 c01 0][c01 c11 0][0 0 c22]]. */
-template <class T>
+template <class T, class R>
 __host__ __device__ __forceinline__ T qform(const T &c00, const T &c11, const T &c01, const T &c22,
-                                            const double *x, const double *y)
+                                            const R *x, const R *y)
 {
   return x[0] * (c00 * y[0] + c01 * y[1]) + x[1] * (c01 * y[0] + c11 * y[1]) + (x[2] * y[2]) * c22;
 }
 
 /* Stress of one thickness point after the C33 sub-iterations:
    returns S^11, S^22, S^12 in sv[0..2]; status bit 1 on a vanishing CC3333. */
-template <class T>
-__host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 12 22 */, const QpRef &r,
-                                                   double gam, double gamp, double c1, double mu, double K,
+template <class T, class R>
+__host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 12 22 */, const QpRef<R> &r,
+                                                   R gam, R gamp, R c1, R mu, R K,
                                                    int iters, T sv[3], int &status)
 {
+  const R one = R(1), two = R(2), half = R(0.5), quarter = R(0.25);
   const T &g00 = gm[0], &g11 = gm[1], &g01 = gm[2], &g02 = gm[3], &g12 = gm[4], &g22 = gm[5];
   /* ElemCGDefTens: C_inv in-plane = in-plane block of gm^-1, C33 = 1 */
   T cof00 = g11 * g22 - g12 * g12;
   T cof11 = g00 * g22 - g02 * g02;
   T cof01 = g02 * g12 - g01 * g22;
   T det = g00 * cof00 + g01 * cof01 + g02 * (g01 * g12 - g11 * g02);
-  T idet = 1.0 / det;
+  T idet = one / det;
   T c00 = cof00 * idet, c11 = cof11 * idet, c01 = cof01 * idet;
-  T c22 = T{1.0};
-  T C33 = T{1.0};
+  T c22 = T{one};
+  T C33 = T{one};
   for (int it = 0; it < iters; it++) {
     const T u0 = c00 * r.t[0] + c01 * r.t[1];
     const T u1 = c01 * r.t[0] + c11 * r.t[1];
@@ -116,19 +143,19 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
     const T detci = (c00 * c11 - c01 * c01) * c22;
     const T Je = dsqrt(r.rho / detci);
     const T alpha = K * (Je * Je - Je) - mu;
-    const T beta = (0.5 * K) * Je * (2.0 * Je - 1.0);
-    const T half_a = 0.5 * alpha;
-    const double gg = gam * gamp;
+    const T beta = (half * K) * Je * (two * Je - one);
+    const T half_a = half * alpha;
+    const R gg = gam * gamp;
     /* S^33 */
     const T S33 = mu * (r.gc22 + c1 * r.s[2] * r.s[2])
-                + half_a * (2.0 * c22 + (gamp - gam) * r.s[2] * u2 - gg * r.s[2] * r.s[2] * tau);
+                + half_a * (two * c22 + (gamp - gam) * r.s[2] * u2 - gg * r.s[2] * r.s[2] * tau);
     if (it == iters - 1) {
       sv[0] = mu * (r.gc00 + c1 * r.s[0] * r.s[0])
-            + half_a * (2.0 * c00 + (gamp - gam) * r.s[0] * u0 - gg * r.s[0] * r.s[0] * tau);
+            + half_a * (two * c00 + (gamp - gam) * r.s[0] * u0 - gg * r.s[0] * r.s[0] * tau);
       sv[1] = mu * (r.gc11 + c1 * r.s[1] * r.s[1])
-            + half_a * (2.0 * c11 + (gamp - gam) * r.s[1] * u1 - gg * r.s[1] * r.s[1] * tau);
+            + half_a * (two * c11 + (gamp - gam) * r.s[1] * u1 - gg * r.s[1] * r.s[1] * tau);
       sv[2] = mu * (r.gc01 + c1 * r.s[0] * r.s[1])
-            + half_a * (2.0 * c01 + gamp * r.s[1] * u0 - gam * r.s[0] * u1 - gg * r.s[0] * r.s[1] * tau);
+            + half_a * (two * c01 + gamp * r.s[1] * u0 - gam * r.s[0] * u1 - gg * r.s[0] * r.s[1] * tau);
     }
     /* CC3333 */
     const T qvv = qform(c00, c11, c01, c22, r.av, r.av);
@@ -137,19 +164,19 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
     const T qvw = qform(c00, c11, c01, c22, r.av, r.aw);
     const T qve = qform(c00, c11, c01, c22, r.av, r.ae);
     const T qwe = qform(c00, c11, c01, c22, r.aw, r.ae);
-    const T twob = 2.0 * beta;
-    const T CC = 0.25 * (2.0 * (beta - alpha) * qvv * qvv + 2.0 * twob * qvv * qwe - 4.0 * alpha * qvw * qve
-                         + (twob - alpha) * qwe * qwe - alpha * qww * qee);
+    const T twob = two * beta;
+    const T CC = quarter * (two * (beta - alpha) * qvv * qvv + two * twob * qvv * qwe - R(4) * alpha * qvw * qve
+                            + (twob - alpha) * qwe * qwe - alpha * qww * qee);
     /* ModElemC33 (active_strain.c:1654-1707) */
-    if (!(fabs(val(CC)) > 1e-14)) { status |= 1; return; }
+    if (!(dabs(val(CC)) > R(1e-14))) { status |= 1; return; }
     T dC = -S33 / CC;
     T Ct = C33 + dC;
-    if (val(g00) * (val(g11) * val(Ct)) - val(g01) * (val(g01) * val(Ct)) <= 0.0) {
-      double lo = 0.0, hi = 1.0;
+    if (val(g00) * (val(g11) * val(Ct)) - val(g01) * (val(g01) * val(Ct)) <= R(0)) {
+      R lo = R(0), hi = one;
       for (int bk = 0; bk < 16; bk++) {
-        const double mid = 0.5 * (lo + hi);
-        const double ct = val(C33) + mid * val(dC);
-        if (val(g00) * (val(g11) * ct) - val(g01) * (val(g01) * ct) > 0.0) lo = mid; else hi = mid;
+        const R mid = half * (lo + hi);
+        const R ct = val(C33) + mid * val(dC);
+        if (val(g00) * (val(g11) * ct) - val(g01) * (val(g01) * ct) > R(0)) lo = mid; else hi = mid;
       }
       dC = dC * lo;
       Ct = C33 + dC;
@@ -157,41 +184,43 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
     C33 = Ct;
     if (it + 1 < iters) {
       /* C_inv = INV([[gm00 gm01 0][gm01 gm11 0][0 0 C33]]) */
-      const T id2 = 1.0 / (g00 * g11 - g01 * g01);
-      c00 = g11 * id2; c11 = g00 * id2; c01 = -g01 * id2; c22 = 1.0 / C33;
+      const T id2 = one / (g00 * g11 - g01 * g01);
+      c00 = g11 * id2; c11 = g00 * id2; c01 = -g01 * id2; c22 = one / C33;
     }
   }
 }
 
 /* f(y): the 15 force components of the element.
-   ref points at the element's first SoA constant; stride = ne. */
-template <class T>
-__host__ __device__ __forceinline__ void elem_forces(const T y[15], const KParams &p, const double *ref, int stride,
+   ref points at the element's first SoA constant (type R); stride = ne. */
+template <class T, class R>
+__host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R> &p, const R *ref, int stride,
                                                      T f[15], int &status)
 {
+  const R one = R(1), two = R(2);
   const V3<T> a1 = {y[0], y[1], y[2]}, a2 = {y[3], y[4], y[5]};
   const V3<T> Aaa = {y[6], y[7], y[8]}, Abb = {y[9], y[10], y[11]}, Aab = {y[12], y[13], y[14]};
   const V3<T> cr = cross(a1, a2);
   const T cn = dsqrt(dot(cr, cr));
-  const T icn = 1.0 / cn;
+  const T icn = one / cn;
   const V3<T> n = scl(icn, cr);
   const V3<T> t1 = cross(a2, n);
-  const V3<T> gc1 = scl(1.0 / dot(a1, t1), t1);
+  const V3<T> gc1 = scl(one / dot(a1, t1), t1);
   const V3<T> t2 = cross(n, a1);
-  const V3<T> gc2 = scl(1.0 / dot(a2, t2), t2);
+  const V3<T> gc2 = scl(one / dot(a2, t2), t2);
   const V3<T> a31 = scl(icn, cross(Aaa, a2) + cross(a1, Aab));
   const V3<T> a32 = scl(icn, cross(Aab, a2) + cross(a1, Abb));
 
   const int nq = p.nq;
-  const double gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];
-  const double gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
-  const double c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
-  const double pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
+  const R gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];
+  const R gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
+  const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
+  const R pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
 
-  T N0 = T{0.0}, N1 = T{0.0}, N2 = T{0.0}, M0 = T{0.0}, M1 = T{0.0}, M2 = T{0.0};
+  const T zero = T{R(0)};
+  T N0 = zero, N1 = zero, N2 = zero, M0 = zero, M1 = zero, M2 = zero;
   for (int q = 0; q < nq; q++) {
-    QpRef r;
-    const double *rq = ref + (size_t)kRefPerQp * q * stride;
+    QpRef<R> r;
+    const R *rq = ref + (size_t)kRefPerQp * q * stride;
     r.gc00 = rq[0]; r.gc11 = rq[(size_t)1 * stride]; r.gc01 = rq[(size_t)2 * stride]; r.gc22 = rq[(size_t)3 * stride];
     for (int k = 0; k < 3; k++) {
       r.s[k] = rq[(size_t)(4 + k) * stride];
@@ -201,18 +230,18 @@ __host__ __device__ __forceinline__ void elem_forces(const T y[15], const KParam
       r.ae[k] = rq[(size_t)(17 + k) * stride];
     }
     r.rho = rq[(size_t)10 * stride];
-    const double th3 = p.hhalf * p.theta[q];
+    const R th3 = p.hhalf * p.theta[q];
     const V3<T> g1 = a1 + scl(th3, a31), g2 = a2 + scl(th3, a32);
     T gm[6] = {dot(g1, g1), dot(g2, g2), dot(g1, g2), dot(g1, n), dot(g2, n), dot(n, n)};
     T sv[3];
     qp_stress(gm, r, gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
-    const double wq = p.w[q], wt = p.w[q] * th3;
+    const R wq = p.w[q], wt = p.w[q] * th3;
     N0 = N0 + wq * sv[0]; N1 = N1 + wq * sv[1]; N2 = N2 + wq * sv[2];
     M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
   }
   N0 = pref0 * N0; N1 = pref0 * N1; N2 = pref0 * N2;
   M0 = pref0 * M0; M1 = pref0 * M1; M2 = pref0 * M2;
-  const T twoM2 = 2.0 * M2;
+  const T twoM2 = two * M2;
   const V3<T> Q = scl(M0, Aaa) + scl(M1, Abb) + scl(twoM2, Aab);
   const V3<T> f1 = scl(N0, a1) + scl(N2, a2) - scl(dot(gc1, Q), n);
   const V3<T> f2 = scl(N1, a2) + scl(N2, a1) - scl(dot(gc2, Q), n);

@@ -195,7 +195,8 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p)
   gather_y(m.pos, m.patch, e, nen, tab, y);
   double f[15];
   int st = 0;
-  elem_forces<double>(y, p, m.eref + e, p.ne, f, st);
+  const EPar<double> ep = epar<double>(p);
+  elem_forces<double, double>(y, ep, m.eref + e, p.ne, f, st);
   set_status(m.status, st);
   /* Fb_a = sum_r N[r][a] f_r, stored slot-major: fb[(3a+d)*ne + e] */
   const size_t ne = p.ne;
@@ -245,11 +246,12 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   const double *tab = tabs + tabi * 80;
   double y[15];
   gather_y(m.pos, m.patch, ee, nen, tab, y);
-  D1 yd[15], fd[15];
+  D1d yd[15], fd[15];
 #pragma unroll
-  for (int k = 0; k < 15; k++) yd[k] = D1{y[k], k == lane ? 1.0 : 0.0};
+  for (int k = 0; k < 15; k++) yd[k] = D1d{y[k], k == lane ? 1.0 : 0.0};
   int st = 0;
-  elem_forces<D1>(yd, p, m.eref + ee, p.ne, fd, st);
+  const EPar<double> ep = epar<double>(p);
+  elem_forces<D1d, double>(yd, ep, m.eref + ee, p.ne, fd, st);
   if (live) set_status(m.status, st);
   const size_t ne = p.ne;
   /* column `lane` of D = df/dy */
@@ -328,6 +330,160 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
     }
     ke[idx] = s;
   }
+}
+
+/* ---------------- FP32-bulk tangent ---------------- */
+/* Same element math as k_elem_tangent in single precision.  Node positions
+   are shifted to the element's first corner in FP64 (one node per lane, then
+   shared by shuffles) and rounded to FP32, so the FP32 values carry the
+   element-size digits; the shift is put back through (sum_i N_r[i]) * x_c,
+   which is not zero for the truncated second-derivative rows (their rows sum
+   to -1e-4 / -1e-4 / +2e-4).  Element matrices are written in FP32. */
+__global__ void __launch_bounds__(128) k_elem_tangent_f32(DevMesh m, KParams p)
+{
+  __shared__ float tabs[kNumTables * 80];
+  __shared__ float tsum[kNumTables * 5];
+  __shared__ float Dsh[kTanElemsPerCta][15 * 16];
+  __shared__ float Tsh[kTanElemsPerCta][15 * 48];
+  for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = (float)m.ntab[i];
+  for (int i = threadIdx.x; i < kNumTables * 5; i += blockDim.x) {
+    double sacc = 0.0;
+    for (int k = 0; k < 16; k++) sacc += m.ntab[i * 16 + k];
+    tsum[i] = (float)sacc;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 15;
+  const int slot = threadIdx.x >> 4;
+  const int e = blockIdx.x * kTanElemsPerCta + slot;
+  const bool live = e < p.ne;
+  const int ee = live ? e : p.ne - 1;
+  const int info = m.einfo[ee];
+  const int nen = info & 0xff, tabi = info >> 8;
+  const float *tab = tabs + tabi * 80;
+  /* shifted coordinates: lane i < nen owns patch node i */
+  const int c0 = m.etri[3 * (size_t)ee];
+  double xc, yc, zc;
+  load_node(m.pos, c0, xc, yc, zc);
+  float dx = 0.f, dy = 0.f, dz = 0.f;
+  if (lane < nen) {
+    const int node = m.patch[16 * (size_t)ee + lane];
+    double X, Y, Z;
+    load_node(m.pos, node, X, Y, Z);
+    dx = (float)(X - xc); dy = (float)(Y - yc); dz = (float)(Z - zc);
+  }
+  float y[15];
+#pragma unroll
+  for (int r = 0; r < 5; r++) {
+    const float sr = tsum[tabi * 5 + r];
+    y[3 * r] = sr * (float)xc; y[3 * r + 1] = sr * (float)yc; y[3 * r + 2] = sr * (float)zc;
+  }
+  const unsigned hmask = 0xffffffffu;
+  for (int i = 0; i < 16; i++) {
+    const float ax = __shfl_sync(hmask, dx, i, 16), ay = __shfl_sync(hmask, dy, i, 16), az = __shfl_sync(hmask, dz, i, 16);
+    if (i < nen) {
+#pragma unroll
+      for (int r = 0; r < 5; r++) {
+        const float c = tab[r * 16 + i];
+        y[3 * r] = fmaf(c, ax, y[3 * r]); y[3 * r + 1] = fmaf(c, ay, y[3 * r + 1]); y[3 * r + 2] = fmaf(c, az, y[3 * r + 2]);
+      }
+    }
+  }
+  D1f yd[15], fd[15];
+#pragma unroll
+  for (int k = 0; k < 15; k++) yd[k] = D1f{y[k], k == lane ? 1.f : 0.f};
+  int st = 0;
+  const EPar<float> ep = epar<float>(p);
+  elem_forces<D1f, float>(yd, ep, m.erefF + ee, p.ne, fd, st);
+  if (live) set_status(m.status, st);
+  if (lane < 15) {
+#pragma unroll
+    for (int r = 0; r < 15; r++) Dsh[slot][r * 16 + lane] = fd[r].d;
+  }
+  /* pressure stiffness from the shifted corner coordinates */
+  const int cs = m.ecorner[ee];
+  const int cslot[3] = {cs & 31, (cs >> 5) & 31, (cs >> 10) & 31};
+  float xk[3][3];
+  for (int k = 0; k < 3; k++) {
+    xk[k][0] = __shfl_sync(hmask, dx, cslot[k], 16);
+    xk[k][1] = __shfl_sync(hmask, dy, cslot[k], 16);
+    xk[k][2] = __shfl_sync(hmask, dz, cslot[k], 16);
+  }
+  __syncwarp();
+  const int ncol = 3 * nen;
+  for (int idx = lane; idx < 15 * ncol; idx += 16) {
+    const int ri = idx / ncol, c = idx - ri * ncol;
+    const int b = c / 3, j = c - 3 * b;
+    float sacc = 0.f;
+#pragma unroll
+    for (int sr = 0; sr < 5; sr++) sacc = fmaf(Dsh[slot][ri * 16 + 3 * sr + j], tab[sr * 16 + b], sacc);
+    Tsh[slot][ri * 48 + c] = sacc;
+  }
+  __syncwarp();
+  if (!live) return;
+  float dc[3][3][3];
+  {
+    const float av[3] = {xk[1][0] - xk[0][0], xk[1][1] - xk[0][1], xk[1][2] - xk[0][2]};
+    const float bv[3] = {xk[2][0] - xk[0][0], xk[2][1] - xk[0][1], xk[2][2] - xk[0][2]};
+    const float vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
+    const float sc = (float)(-p.pressure / 6.0);
+    for (int k = 0; k < 3; k++) {
+      const float *v = vv[k];
+      dc[k][0][0] = 0.f;        dc[k][0][1] = -sc * v[2]; dc[k][0][2] = sc * v[1];
+      dc[k][1][0] = sc * v[2];  dc[k][1][1] = 0.f;        dc[k][1][2] = -sc * v[0];
+      dc[k][2][0] = -sc * v[1]; dc[k][2][1] = sc * v[0];  dc[k][2][2] = 0.f;
+    }
+  }
+  float *ke = m.keF + (size_t)m.kofs[e] * 9;
+  const int nval = 9 * nen * nen;
+  for (int idx = lane; idx < nval; idx += 16) {
+    const int blk = idx / 9, w = idx - 9 * blk;
+    const int a = blk / nen, b = blk - a * nen;
+    const int i = w / 3, j = w - 3 * i;
+    float sacc = 0.f;
+#pragma unroll
+    for (int r = 0; r < 5; r++) sacc = fmaf(tab[r * 16 + a], Tsh[slot][(3 * r + i) * 48 + 3 * b + j], sacc);
+    if (p.pressure != 0.0 && (a == cslot[0] || a == cslot[1] || a == cslot[2])) {
+      for (int k = 0; k < 3; k++)
+        if (b == cslot[k]) sacc += dc[k][i][j];
+    }
+    ke[idx] = sacc;
+  }
+}
+
+/* FP32 block gather with compensated (Kahan) summation in element order. */
+__global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K)
+{
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 9 * m.nnzb) return;
+  const long long k = t / 9;
+  const int w = (int)(t - 9 * k);
+  const int row = m.blkrow[k];
+  const int kind = m.rowkind[row];
+  float s = 0.f;
+  if (kind != 0) {
+    s = (m.colind[k] == row && (w == 0 || w == 4 || w == 8)) ? 1.f : 0.f;
+  } else {
+    float comp = 0.f;
+    for (long long c = m.cptr[k]; c < m.cptr[k + 1]; c++) {
+      const int id = m.cidx[c];
+      const float v = id >= 0 ? m.keF[(size_t)id * 9 + w] : -m.keF[(size_t)(-(id + 1)) * 9 + w];
+      const float yv = v - comp;
+      const float tt = s + yv;
+      comp = (tt - s) - yv;
+      s = tt;
+    }
+  }
+  K[t] = s;
+}
+
+__global__ void k_scale_f32(DevMesh m, KParams p, double *__restrict__ R, float *__restrict__ K)
+{
+  const double fmax = __longlong_as_double((long long)*m.fmax);
+  if (!(fmax > 1.0)) return;
+  const double sc = 1.0 / fmax;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 3LL * p.nt) R[t] = R[t] * sc;
+  if (t < 9 * m.nnzb && m.rowkind[m.blkrow[t / 9]] != 2) K[t] = (float)(K[t] * sc);
 }
 
 /* ---------------- node gather (residual assembly) ---------------- */
@@ -430,6 +586,39 @@ int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream)
 int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream)
 {
   k_elem_tangent<<<blocks_for(p.ne, kTanElemsPerCta), 128, 0, (cudaStream_t)stream>>>(m, p);
+  return (int)cudaGetLastError();
+}
+
+int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream)
+{
+  k_elem_tangent_f32<<<blocks_for(p.ne, kTanElemsPerCta), 128, 0, (cudaStream_t)stream>>>(m, p);
+  return (int)cudaGetLastError();
+}
+
+int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream)
+{
+  if (m.nnzb == 0) return 0;
+  k_block_gather_f32<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K);
+  return (int)cudaGetLastError();
+}
+
+int launch_scale_f32(const DevMesh &m, const KParams &p, double *R, float *K, void *stream)
+{
+  long long n = 3LL * p.nt;
+  if (9 * m.nnzb > n) n = 9 * m.nnzb;
+  k_scale_f32<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(m, p, R, K);
+  return (int)cudaGetLastError();
+}
+
+__global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long long n)
+{
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = (float)a[t];
+}
+
+int launch_to_float(const double *a, float *b, long long n, void *stream)
+{
+  k_to_float<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(a, b, n);
   return (int)cudaGetLastError();
 }
 

@@ -66,6 +66,7 @@ typedef struct {
   int64_t nnzb;                /* 3x3 blocks in the tangent pattern */
   int64_t n_contrib;           /* element-block contributions (assembly map size) */
   int64_t device_bytes;        /* device memory held by the handle */
+  int32_t precision;           /* BIOFEM_FP64 or BIOFEM_FP32_BULK */
 } BiofemMeshInfo;
 
 typedef struct BiofemGpuMesh_ BiofemGpuMesh;
@@ -103,14 +104,17 @@ int GetGpuCsrPattern(const BiofemGpuMesh *m, int32_t *rowptr, int32_t *colind);
    reference's SNES callback evaluates. */
 int RunGpuResidual(BiofemGpuMesh *m, const double *x, double *R);
 /* R(x) and the tangent K = dR/dx (new: the reference is matrix-free,
-   main.c:464-466).  Kvals has 9*nnzb entries.  R may be NULL. */
-int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, double *Kvals);
+   main.c:464-466).  Kvals has 9*nnzb entries: double for a BIOFEM_FP64
+   handle, float for a BIOFEM_FP32_BULK handle (whose residual is still FP64
+   and whose tangent is formed in FP32 on patch-local shifted coordinates).
+   R may be NULL. */
+int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *Kvals);
 
 /* Device-resident variants: pointers are device memory, work is enqueued on
    `stream` (a cudaStream_t; NULL = the CUDA default stream) and not
    synchronised.  BiofemGpuSync() waits and reports device-side errors. */
 int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *stream);
-int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, double *d_Kvals, void *stream);
+int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_Kvals, void *stream);
 int BiofemGpuSync(BiofemGpuMesh *m, void *stream);
 
 /* Residual for callers that cannot allocate device memory when they call:
@@ -132,7 +136,7 @@ int RunGpuResidualNoAlloc(BiofemGpuMesh *m, const double *d_x, double *d_R, void
    void*) and the Jacobian slot SNESSetJacobian, main.c:462-466) taking host
    arrays; ctx is the BiofemGpuMesh*.  `snes` is passed through unused. */
 int FormFunctionFEMGpu(void *snes, const double *x, double *R, void *ctx);
-int FormJacobianFEMGpu(void *snes, const double *x, double *Kvals, void *ctx);
+int FormJacobianFEMGpu(void *snes, const double *x, void *Kvals, void *ctx);
 
 /* Per-kernel CUDA-event timing of the device calls (off by default): slot i
    is the i-th launch of the call (residual: positions, element residual,

@@ -1,0 +1,56 @@
+"""FP32-bulk form: the residual stays FP64 (identical to the plain path);
+the tangent (subdivision basis, tangent vectors, curvature, df/dy, element
+matrices, K values) runs in FP32 on patch-local shifted coordinates.
+
+Stated tolerances for the FP32-bulk tangent:
+  ||K32 - K64||_F <= 2e-5 ||K64||_F,  ||K32 v - J v||_2 <= 2e-5 ||J v||_2
+(J v = exact dual-number directional derivative of the oracle residual).
+"""
+import numpy as np
+import pytest
+
+from biofem import configs
+
+pytestmark = pytest.mark.gpu
+
+
+def pair(w):
+    from biofem.gpu import GpuShell, BIOFEM_FP32_BULK
+    m = w.build_mesh()
+    s64 = GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    s32 = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=BIOFEM_FP32_BULK)
+    return m, s64, s32
+
+
+@pytest.mark.parametrize("w", [configs.C1, configs.small(12, 9, activation="random", index=70, pressure=1e-3),
+                               configs.C2], ids=lambda w: w.name)
+def test_fp32_bulk_tangent_error(w, oracle_lib):
+    m, s64, s32 = pair(w)
+    t = s64.topology()
+    x = w.initial_x(m, t["xyz0_full"])
+    R64, K64 = s64.form_jacobian(x)
+    R32, K32 = s32.form_jacobian(x)
+    assert K32.dtype == np.float32
+    np.testing.assert_array_equal(R32, R64)           # residual path is FP64 in both forms
+    frob = np.linalg.norm(K32.astype(np.float64) - K64) / np.linalg.norm(K64)
+    assert frob <= 2e-5, frob
+    o = oracle_lib.setup_given_topology(m, w, t, configs.MU, configs.BULK, configs.H0)
+    o.set_threads(8)
+    v = np.random.default_rng(11).standard_normal(x.size)
+    _, Jv = o.jvp(x, v)
+    nreal = 3 * m.n_v
+    Kv = s32.to_scipy(K32) @ v
+    assert np.linalg.norm(Kv[:nreal] - Jv[:nreal]) <= 2e-5 * np.linalg.norm(Jv[:nreal])
+    s64.close()
+    s32.close()
+
+
+def test_fp32_bulk_is_deterministic():
+    w = configs.small(16, 12, index=71)
+    m, s64, s32 = pair(w)
+    x = w.initial_x(m, s64.topology()["xyz0_full"])
+    _, K1 = s32.form_jacobian(x)
+    _, K2 = s32.form_jacobian(x)
+    assert np.array_equal(K1, K2)
+    s64.close()
+    s32.close()
