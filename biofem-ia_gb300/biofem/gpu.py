@@ -56,6 +56,24 @@ class MeshInfo(ctypes.Structure):
                 ("n_contrib", ctypes.c_int64), ("device_bytes", ctypes.c_int64), ("precision", ctypes.c_int32)]
 
 
+class NewtonOptions(ctypes.Structure):
+    _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("max_newton", ctypes.c_int32),
+                ("gmres_restart", ctypes.c_int32), ("gmres_max_it", ctypes.c_int32), ("gmres_rtol", ctypes.c_double),
+                ("line_search", ctypes.c_int32)]
+
+
+class NewtonStats(ctypes.Structure):
+    _fields_ = [("newton_its", ctypes.c_int32), ("gmres_its_total", ctypes.c_int32), ("gmres_its_last", ctypes.c_int32),
+                ("residual_evals", ctypes.c_int32), ("jacobian_evals", ctypes.c_int32), ("converged", ctypes.c_int32),
+                ("r0", ctypes.c_double), ("rfinal", ctypes.c_double), ("gmres_relres_last", ctypes.c_double),
+                ("rhist", ctypes.c_double * 64)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "rhist"}
+        d["rhist"] = list(self.rhist[: self.newton_its + 1])
+        return d
+
+
 _LIB = None
 
 # every entry point the header declares (checked by tests/test_cabi.py)
@@ -64,7 +82,8 @@ EXPORTS = ["InitGpuWorkspace", "DestroyGpuWorkspace", "PrepareGpuMesh", "Destroy
            "RunGpuResidualDevice", "RunGpuResidualJacobianDevice", "BiofemGpuSync", "FormFunctionFEMGpu",
            "FormJacobianFEMGpu", "GetGpuLaunchCounts", "BuildHostMesh", "DestroyHostMesh",
            "GetGpuBasisTables", "BiofemGpuLastError", "EnableGpuKernelTiming", "GetGpuKernelTimes",
-           "GetGpuGhostMap", "RunGpuResidualNoAlloc"]
+           "GetGpuGhostMap", "RunGpuResidualNoAlloc", "BiofemNewtonDefaults", "RunGpuNewtonSolve",
+           "RunGpuNewtonSolveDevice"]
 
 
 def load_library(path: Path | str | None = None) -> ctypes.CDLL:
@@ -92,6 +111,10 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
     lib.RunGpuResidualDevice.argtypes = [vp, vp, vp, vp]
     lib.RunGpuResidualJacobianDevice.argtypes = [vp, vp, vp, vp, vp]
     lib.RunGpuResidualNoAlloc.argtypes = [vp, vp, vp, vp]
+    lib.BiofemNewtonDefaults.argtypes = [ctypes.POINTER(NewtonOptions)]
+    lib.BiofemNewtonDefaults.restype = None
+    lib.RunGpuNewtonSolve.argtypes = [vp, vp, ctypes.POINTER(NewtonOptions), ctypes.POINTER(NewtonStats)]
+    lib.RunGpuNewtonSolveDevice.argtypes = [vp, vp, ctypes.POINTER(NewtonOptions), ctypes.POINTER(NewtonStats), vp]
     lib.BiofemGpuSync.argtypes = [vp, vp]
     lib.GetGpuLaunchCounts.argtypes = [vp, vp, vp]
     lib.GetGpuBasisTables.argtypes = [vp]
@@ -206,6 +229,30 @@ class GpuShell:
         K = np.empty((self.nnzb, 3, 3), dtype=self.k_dtype)
         _check(self.lib, self.lib.RunGpuResidualJacobian(self.handle, _ptr(x), _ptr(R), _ptr(K)))
         return R, K
+
+    # ---- one load step ----
+    def newton_options(self, **kw) -> NewtonOptions:
+        o = NewtonOptions()
+        self.lib.BiofemNewtonDefaults(ctypes.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+    def newton(self, x: np.ndarray, **kw):
+        """RunGpuNewtonSolve: Newton + GMRES/block-Jacobi load step from x.
+        Returns (x_converged, stats dict)."""
+        x = np.array(x, dtype=np.float64, copy=True)
+        o = self.newton_options(**kw)
+        st = NewtonStats()
+        _check(self.lib, self.lib.RunGpuNewtonSolve(self.handle, _ptr(x), ctypes.byref(o), ctypes.byref(st)))
+        return x, st.as_dict()
+
+    def newton_device(self, d_x: int, stream: int = 0, **kw):
+        o = self.newton_options(**kw)
+        st = NewtonStats()
+        _check(self.lib, self.lib.RunGpuNewtonSolveDevice(self.handle, ctypes.c_void_p(d_x), ctypes.byref(o),
+                                                          ctypes.byref(st), ctypes.c_void_p(stream or None)))
+        return st.as_dict()
 
     # ---- device-resident calls (raw CUDA pointers as ints) ----
     def residual_device(self, d_x: int, d_R: int, stream: int = 0):

@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/biofem_gpu.h"
 
 namespace biofem {
@@ -83,6 +85,18 @@ int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *
 int launch_scale_f32(const DevMesh &m, const KParams &p, double *R, float *K, void *stream);
 int launch_to_float(const double *a, float *b, long long n, void *stream);
 int upload_tables(double *d_ntab);
+
+/* device Newton / GMRES (solver.cu) */
+struct SolverWork;
+SolverWork *solver_create(int n, int nb, int m, int *rc);
+void solver_destroy(SolverWork *w);
+double *solver_xbuf(SolverWork *w);
+int solver_m(const SolverWork *w);
+typedef int (*ResidualFn)(void *ctx, const double *x, double *R, void *stream);
+typedef int (*JacobianFn)(void *ctx, const double *x, double *R, void *K, void *stream);
+int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, double *dR, double *x,
+                  const BiofemNewtonOptions &o, BiofemNewtonStats &s, SolverWork *w, cudaStream_t st,
+                  ResidualFn residual, JacobianFn jacobian, void *ctx, std::string &err);
 void host_tables(double *out);   /* kNumTables*5*16 host copy of the basis tables */
 
 } /* namespace biofem */

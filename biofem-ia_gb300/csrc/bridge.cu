@@ -148,6 +148,7 @@ struct BiofemGpuMesh_ {
   DevMesh dm{};
   double *d_x = nullptr, *d_R = nullptr;   /* staging for host-array calls */
   void *d_K = nullptr;                      /* K values: double (FP64) or float (FP32-bulk) */
+  SolverWork *solver = nullptr;             /* Newton/GMRES work, created on first solve */
   KernelTimer timer;
 };
 
@@ -197,6 +198,7 @@ static int dupload(BiofemGpuMesh *m, T **p, const std::vector<T> &h)
 
 static void free_mesh(BiofemGpuMesh *m)
 {
+  if (m->solver) solver_destroy(m->solver);
   for (int i = 0; i <= kMaxTimed; i++) if (m->timer.ev[i]) cudaEventDestroy(m->timer.ev[i]);
   for (void *p : m->allocs) cudaFree(p);
   m->allocs.clear();
@@ -714,6 +716,69 @@ int FormJacobianFEMGpu(void *snes, const double *x, void *K, void *ctx)
 {
   (void)snes;
   return RunGpuResidualJacobian(reinterpret_cast<BiofemGpuMesh *>(ctx), x, nullptr, K);
+}
+
+void BiofemNewtonDefaults(BiofemNewtonOptions *o)
+{
+  if (!o) return;
+  o->rtol = 1e-10; o->atol = 0.0; o->max_newton = 20;
+  o->gmres_restart = 100; o->gmres_max_it = 5000; o->gmres_rtol = 1e-9; o->line_search = 1;
+}
+
+static int newton_residual_cb(void *ctx, const double *x, double *R, void *stream)
+{
+  return RunGpuResidualDevice(static_cast<BiofemGpuMesh *>(ctx), x, R, stream);
+}
+
+static int newton_jacobian_cb(void *ctx, const double *x, double *R, void *K, void *stream)
+{
+  return RunGpuResidualJacobianDevice(static_cast<BiofemGpuMesh *>(ctx), x, R, K, stream);
+}
+
+int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOptions *opt, BiofemNewtonStats *stats,
+                            void *stream)
+{
+  if (!m || !d_x || !stats) return fail(85, "null argument");
+  if (!m->dm.patch) return fail(58, "host-only handle");
+  BiofemNewtonOptions o;
+  if (opt) o = *opt; else BiofemNewtonDefaults(&o);
+  if (o.gmres_restart < 1 || o.gmres_restart > 1000 || o.max_newton < 0 || o.gmres_max_it < 1)
+    return fail(63, "Newton options out of range");
+  const int n = 3 * m->kp.nt;
+  if (!m->solver || solver_m(m->solver) != o.gmres_restart) {
+    if (m->solver) solver_destroy(m->solver);
+    int rc = 0;
+    m->solver = solver_create(n, m->kp.nt, o.gmres_restart, &rc);
+    if (!m->solver) return fail(55, std::string("Newton work allocation: ") + cudaGetErrorString((cudaError_t)rc));
+  }
+  std::string err;
+  cudaStream_t st = pick_stream(stream);
+  int rc = newton_device(m->dm, m->kp, m->prm.precision != BIOFEM_FP64, m->d_K, m->d_R, d_x, o, *stats, m->solver, st,
+                         newton_residual_cb, newton_jacobian_cb, m, err);
+  if (rc) return fail(rc > 1000 ? 76 : rc, "Newton " + err + " step failed: " + g_last_error);
+  return BiofemGpuSync(m, stream);
+}
+
+int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *opt, BiofemNewtonStats *stats)
+{
+  if (!m || !x || !stats) return fail(85, "null argument");
+  if (!m->dm.patch) return fail(58, "host-only handle");
+  BiofemNewtonOptions o;
+  if (opt) o = *opt; else BiofemNewtonDefaults(&o);
+  const size_t n = 3 * (size_t)m->kp.nt;
+  if (!m->solver || solver_m(m->solver) != o.gmres_restart) {
+    if (m->solver) solver_destroy(m->solver);
+    int rc = 0;
+    m->solver = solver_create((int)n, m->kp.nt, o.gmres_restart, &rc);
+    if (!m->solver) return fail(55, std::string("Newton work allocation: ") + cudaGetErrorString((cudaError_t)rc));
+  }
+  double *dx = solver_xbuf(m->solver);
+  CUDA_TRY(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, g_stream));
+  int rc = RunGpuNewtonSolveDevice(m, dx, &o, stats, g_stream);
+  if (rc) return rc;
+  CUDA_TRY(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
+  CUDA_TRY(cudaStreamSynchronize(g_stream));
+  return 0;
 }
 
 /* Basis-derivative tables (regular + irregular valences 3..10), 11*5*16. */

@@ -19,7 +19,7 @@ ROOT = PKG.parent
 LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libbiofem_gpu.so"
 OBJ_DIR = LIB_DIR / "obj"
-CUDA_SOURCES = ["kernels.cu", "bridge.cu", "noalloc.cu"]
+CUDA_SOURCES = ["kernels.cu", "bridge.cu", "noalloc.cu", "solver.cu"]
 CXX_SOURCES = ["topology.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
@@ -50,7 +50,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
         else:
-            cmd = ["g++", *CXX_FLAGS, "-c", str(HERE / src), "-o", str(obj)]
+            cuda_inc = Path(nvcc()).resolve().parent.parent / "include"
+            cmd = ["g++", *CXX_FLAGS, "-I", str(cuda_inc), "-c", str(HERE / src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -132,6 +132,33 @@ int BiofemGpuSync(BiofemGpuMesh *m, void *stream);
    any stream capture. */
 int RunGpuResidualNoAlloc(BiofemGpuMesh *m, const double *d_x, double *d_R, void *stream);
 
+/* One quasi-static load step: Newton on R(x) = 0 with the assembled tangent
+   (new: replaces the matrix-free SNES newtonls/MFFD/GMRES solve of
+   main.c:461-551).  Linear solves: restarted GMRES(gmres_restart) with right
+   block-Jacobi(3x3) preconditioning, FP64 vectors on the device.  x (host,
+   n_dof entries) holds the start on entry and the solution on exit. */
+typedef struct {
+  double  rtol;              /* stop when ||R|| <= rtol ||R0||  (1e-10) */
+  double  atol;              /* or ||R|| <= atol (0 = off) */
+  int32_t max_newton;        /* Newton iterations (20) */
+  int32_t gmres_restart;     /* Krylov subspace size m (100) */
+  int32_t gmres_max_it;      /* total GMRES iterations per solve (5000) */
+  double  gmres_rtol;        /* relative linear tolerance (1e-9) */
+  int32_t line_search;       /* 1 = backtracking on ||R|| */
+} BiofemNewtonOptions;
+
+typedef struct {
+  int32_t newton_its, gmres_its_total, gmres_its_last, residual_evals, jacobian_evals, converged;
+  double  r0, rfinal, gmres_relres_last;
+  double  rhist[64];         /* ||R|| after each Newton iteration (rhist[0] = ||R0||) */
+} BiofemNewtonStats;
+
+void BiofemNewtonDefaults(BiofemNewtonOptions *o);
+int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *opt, BiofemNewtonStats *stats);
+/* Same on a device vector d_x (updated in place). */
+int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOptions *opt, BiofemNewtonStats *stats,
+                            void *stream);
+
 /* SNES-callback-shaped wrappers (main.c:120 FormFunctionFEM(SNES, Vec, Vec,
    void*) and the Jacobian slot SNESSetJacobian, main.c:462-466) taking host
    arrays; ctx is the BiofemGpuMesh*.  `snes` is passed through unused. */

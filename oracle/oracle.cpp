@@ -895,6 +895,24 @@ int oracle_jvp(const double *x, const double *v, double *R, double *Jv)
   return 0;
 }
 
+/* J V for up to 8 directions V (8 x ndof, row major), JV the same layout. */
+int oracle_jmv8(const double *x, const double *V, int nvec, double *JV)
+{
+  if (!g_body || !g_body->ready) return 58;
+  if (nvec < 1 || nvec > 8) return 63;
+  const int ndof = 3 * (g_body->m.n_v + g_body->m.n_ghosts);
+  std::vector<Dual<8>> xd(ndof), Rd(ndof);
+  for (int i = 0; i < ndof; i++) {
+    xd[i] = Dual<8>(x[i]);
+    for (int k = 0; k < nvec; k++) xd[i].d[k] = V[(size_t)k * ndof + i];
+  }
+  int rc = residual<Dual<8>>(*g_body, xd.data(), Rd.data());
+  if (rc) return rc;
+  for (int k = 0; k < nvec; k++)
+    for (int i = 0; i < ndof; i++) JV[(size_t)k * ndof + i] = Rd[i].d[k];
+  return 0;
+}
+
 /* Dense Jacobian (column major, ndof x ndof) for small meshes, 8 columns per pass. */
 int oracle_jacobian_dense(const double *x, double *J)
 {

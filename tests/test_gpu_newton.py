@@ -1,0 +1,52 @@
+"""One quasi-static load step on the GPU (Newton + GMRES/block-Jacobi on the
+assembled tangent) against the oracle's converged state.
+
+tests/golden/C1_flat_32x24_newton.npz holds the oracle's converged C1 load
+step (exact sparse Jacobian + direct solve, ||R|| <= 1e-10 ||R0||, made by
+tests/golden/make_newton_golden.py).  The converged state depends only on R,
+so the GPU solution must agree to the conditioning of the problem:
+  ||x_gpu - x_oracle||_2 <= 1e-7 ||x_oracle - x0||_2.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from biofem import configs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32_bulk"])
+def test_newton_C1_matches_oracle(precision):
+    from biofem.gpu import GpuShell
+    d = np.load(GOLDEN / "C1_flat_32x24_newton.npz")
+    w = configs.C1
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=precision)
+    x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+    np.testing.assert_array_equal(x0, d["x0"])
+    x, st = sh.newton(x0, rtol=1e-10)
+    assert st["converged"] == 1, st
+    assert st["newton_its"] <= 8, st
+    dx_ref = d["x"] - d["x0"]
+    assert np.linalg.norm(x - d["x"]) <= 1e-7 * np.linalg.norm(dx_ref), (np.linalg.norm(x - d["x"]), st)
+    R = sh.form_function(x)
+    assert np.linalg.norm(R) <= 1e-10 * st["r0"] * 1.0001
+    sh.close()
+
+
+def test_newton_64x48_solution_is_a_root_of_the_oracle_residual(oracle_lib):
+    from biofem.gpu import GpuShell
+    w = configs.Workload("flat_64x48", 64, 48, z_sigma=1e-3, activation="smooth", index=80, pressure=2e-4)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    t = sh.topology()
+    x0 = w.initial_x(m, t["xyz0_full"])
+    x, st = sh.newton(x0, rtol=1e-10)
+    assert st["converged"] == 1, st
+    o = oracle_lib.setup_given_topology(m, w, t, configs.MU, configs.BULK, configs.H0)
+    o.set_threads(8)
+    R0 = o.residual(x0)
+    R = o.residual(x)
+    assert np.linalg.norm(R) <= 2e-10 * np.linalg.norm(R0), (np.linalg.norm(R), np.linalg.norm(R0), st)
+    sh.close()
