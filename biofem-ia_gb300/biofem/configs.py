@@ -34,6 +34,7 @@ class Workload:
     lambda_a: float = 0.9
     disp_rel: float = 0.0            # displacement amplitude / edge length h
     index: int = 0
+    theta: float = 0.0               # fibre angle from e_x (uniform activation)
 
     @property
     def seed(self) -> int:
@@ -46,7 +47,7 @@ class Workload:
     def build_mesh(self) -> meshmod.Mesh:
         m = meshmod.flat_membrane(self.nx, self.ny, z_sigma=self.z_sigma, seed=self.seed)
         if self.activation == "uniform":
-            meshmod.set_uniform_activation(m, self.lambda_a)
+            meshmod.set_uniform_activation(m, self.lambda_a, (np.cos(self.theta), np.sin(self.theta), 0.0))
         elif self.activation == "smooth":
             meshmod.set_smooth_activation(m)
         elif self.activation == "random":
@@ -63,9 +64,9 @@ class Workload:
 
 # C1: 32x24 cells (825 nodes, 1536 triangles), z perturbed N(0,1e-3), lambda_a 0.9 along e_x.
 C1 = Workload("C1_flat_32x24", 32, 24, z_sigma=1e-3, activation="uniform", lambda_a=0.9, index=0)
-# C2: 256x192 cells (49,665 nodes, 98,304 triangles), smooth lambda_a field, displacement 1e-2 h.
+# C2: 256x192 cells (49,601 nodes, 98,304 triangles), smooth lambda_a field, displacement 1e-2 h.
 C2 = Workload("C2_flat_256x192", 256, 192, activation="smooth", disp_rel=1e-2, index=1)
-# C3: 1024x768 cells (787,425 nodes, 1,572,864 triangles), random fibre angle and lambda_a.
+# C3: 1024x768 cells (788,225 nodes, 1,572,864 triangles), random fibre angle and lambda_a.
 C3 = Workload("C3_flat_1024x768", 1024, 768, activation="random", index=2)
 
 ALL = {w.name: w for w in (C1, C2, C3)}
@@ -76,3 +77,21 @@ def small(nx: int, ny: int, **kw) -> Workload:
     args = dict(z_sigma=1e-3, activation="smooth", disp_rel=1e-2, index=10)
     args.update(kw)
     return Workload(f"flat_{nx}x{ny}", nx, ny, **args)
+
+
+SERVE_SEED = meshmod.SEED_BASE + 500
+
+
+def serve_request(i: int, nx_lo: int = 16, nx_hi: int = 256) -> Workload:
+    """Request i of the load-step serving stream (the `biofem sweep` case mix):
+    nx = round(exp U[ln nx_lo, ln nx_hi]), ny = round(0.75 nx), z ~ N(0, 1e-3),
+    lambda_a ~ U[0.85, 1] and fibre angle ~ U[0, pi) uniform over the sheet,
+    follower pressure ~ U[1e-5, 1e-3], starting from the reference state."""
+    rng = np.random.default_rng(SERVE_SEED + i)
+    nx = int(round(np.exp(rng.uniform(np.log(nx_lo), np.log(nx_hi)))))
+    ny = max(2, int(round(0.75 * nx)))
+    lam = float(rng.uniform(0.85, 1.0))
+    theta = float(rng.uniform(0.0, np.pi))
+    p = float(rng.uniform(1e-5, 1e-3))
+    return Workload(f"serve_{i}_{nx}x{ny}", nx, ny, pressure=p, z_sigma=1e-3, activation="uniform",
+                    lambda_a=lam, index=1000 + i, theta=theta)

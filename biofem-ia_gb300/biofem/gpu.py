@@ -83,7 +83,8 @@ EXPORTS = ["InitGpuWorkspace", "DestroyGpuWorkspace", "PrepareGpuMesh", "Destroy
            "FormJacobianFEMGpu", "GetGpuLaunchCounts", "BuildHostMesh", "DestroyHostMesh",
            "GetGpuBasisTables", "BiofemGpuLastError", "EnableGpuKernelTiming", "GetGpuKernelTimes",
            "GetGpuGhostMap", "RunGpuResidualNoAlloc", "BiofemNewtonDefaults", "RunGpuNewtonSolve",
-           "RunGpuNewtonSolveDevice"]
+           "RunGpuNewtonSolveDevice", "PrepareGpuMeshOnStream", "ServeCreate", "ServeSubmit", "ServeWait",
+           "ServeStatsGet", "ServeDestroy", "BiofemServeEstimateBytes"]
 
 
 def load_library(path: Path | str | None = None) -> ctypes.CDLL:
@@ -100,6 +101,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
     lib.BiofemGpuLastError.restype = ctypes.c_char_p
     lib.PrepareGpuMesh.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(vp)]
     lib.BuildHostMesh.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(vp)]
+    lib.PrepareGpuMeshOnStream.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), vp, ctypes.POINTER(vp)]
     for name in ("DestroyGpuMesh", "DestroyHostMesh"):
         getattr(lib, name).argtypes = [vp]
     lib.GetGpuMeshInfo.argtypes = [vp, ctypes.POINTER(MeshInfo)]
@@ -120,6 +122,13 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
     lib.GetGpuBasisTables.argtypes = [vp]
     lib.EnableGpuKernelTiming.argtypes = [vp, ctypes.c_int]
     lib.GetGpuKernelTimes.argtypes = [vp, vp, ctypes.c_int32, vp]
+    lib.ServeCreate.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(vp)]
+    lib.ServeSubmit.argtypes = [vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(NewtonOptions),
+                                vp, ctypes.POINTER(ctypes.c_int64)]
+    lib.ServeWait.argtypes = [vp, ctypes.c_int64, vp, ctypes.POINTER(NewtonStats), vp]
+    lib.ServeStatsGet.argtypes = [vp, vp]
+    lib.ServeDestroy.argtypes = [vp]
+    lib.BiofemServeEstimateBytes.argtypes = [ctypes.c_int32] * 5 + [ctypes.POINTER(ctypes.c_int64)]
     if path is None:
         _LIB = lib
     return lib
@@ -310,3 +319,70 @@ def FormJacobianFEM(snes, x: np.ndarray, J: np.ndarray, P, ctx: GpuShell) -> int
     _, K = ctx.form_jacobian(x)
     J[...] = K
     return 0
+
+
+def mesh_desc(mesh):
+    """(MeshDesc, arrays to keep alive) for a biofem.mesh.Mesh."""
+    a = dict(tri=np.ascontiguousarray(mesh.tri, dtype=np.int32), xyz0=np.ascontiguousarray(mesh.xyz0, dtype=np.float64),
+             nb=np.ascontiguousarray(mesh.n_bnodes, dtype=np.int32), bn=np.ascontiguousarray(mesh.bnodes, dtype=np.int32),
+             fib=np.ascontiguousarray(mesh.fib, dtype=np.float64),
+             gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64))
+    d = MeshDesc(mesh.n_v, mesh.n_elmt, mesh.n_edge, a["tri"].ctypes.data_as(_i32p), a["xyz0"].ctypes.data_as(_f64p),
+                 a["nb"].ctypes.data_as(_i32p), a["bn"].ctypes.data_as(_i32p), a["fib"].ctypes.data_as(_f64p),
+                 a["gs"].ctypes.data_as(_f64p))
+    return d, a
+
+
+class Serve:
+    """ServeCreate / ServeSubmit / ServeWait: the continuous-batching load-step service."""
+
+    def __init__(self, hbm_budget_bytes: int, max_slots: int):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.ServeCreate(int(hbm_budget_bytes), int(max_slots), ctypes.byref(h)))
+        self.handle = h
+        self._ndof = {}
+
+    def submit(self, mesh, workload, mu, bulk, h0, x0, gamma=1.0, clamp_edge=0, precision=BIOFEM_FP64, **newton):
+        d, keep = mesh_desc(mesh)
+        prm = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure, clamp_edge, precision)
+        o = NewtonOptions()
+        self.lib.BiofemNewtonDefaults(ctypes.byref(o))
+        for k, v in newton.items():
+            setattr(o, k, v)
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        t = ctypes.c_int64()
+        _check(self.lib, self.lib.ServeSubmit(self.handle, ctypes.byref(d), ctypes.byref(prm), ctypes.byref(o),
+                                              _ptr(x0), ctypes.byref(t)))
+        self._ndof[t.value] = x0.size
+        return t.value
+
+    def wait(self, ticket: int):
+        x = np.empty(self._ndof.pop(ticket))
+        st = NewtonStats()
+        times = np.zeros(3)
+        _check(self.lib, self.lib.ServeWait(self.handle, ctypes.c_int64(ticket), _ptr(x), ctypes.byref(st), _ptr(times)))
+        return x, st.as_dict(), times
+
+    def stats(self):
+        out = np.zeros(6, np.int64)
+        _check(self.lib, self.lib.ServeStatsGet(self.handle, _ptr(out)))
+        return dict(zip(["in_use", "peak_in_use", "active", "peak_active", "queued", "completed"], out.tolist()))
+
+    def close(self):
+        if self.handle:
+            self.lib.ServeDestroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def estimate_bytes(n_v, n_elmt, n_ghosts, precision=BIOFEM_FP64, gmres_restart=0) -> int:
+    lib = load_library()
+    b = ctypes.c_int64()
+    _check(lib, lib.BiofemServeEstimateBytes(n_v, n_elmt, n_ghosts, precision, gmres_restart, ctypes.byref(b)))
+    return b.value

@@ -38,6 +38,9 @@ struct KParams {
   double theta[kMaxQp], w[kMaxQp];
   double pressure;
   double gamma;
+  /* FP32 copies for the FP32-bulk kernels (filled on the host) */
+  float muf, Kf, hhalff, pres6f;
+  float thetaf[kMaxQp], wf[kMaxQp];
 };
 
 /* Device views of one mesh handle. */
@@ -49,6 +52,7 @@ struct DevMesh {
   const double *eref;        /* (kRefPerQp*nq + kRefPerElem) * ne, SoA */
   const float *erefF;        /* the same in FP32 (FP32-bulk handles only) */
   const double *ntab;        /* kNumTables * 5 * 16 basis-derivative tables */
+  const float *ntabF;        /* the same in FP32, followed by the kNumTables*5 row sums */
   const int *etri;           /* 3*ne triangle corners (pressure) */
   const int *ghost3;         /* 3*ng (nv1, nv2, nv3) */
   const long long *kofs;     /* ne: first Ke block of the element */
@@ -88,7 +92,7 @@ int upload_tables(double *d_ntab);
 
 /* device Newton / GMRES (solver.cu) */
 struct SolverWork;
-SolverWork *solver_create(int n, int nb, int m, int *rc);
+SolverWork *solver_create(int n, int nb, int m, void *stream, int *rc);
 void solver_destroy(SolverWork *w);
 double *solver_xbuf(SolverWork *w);
 int solver_m(const SolverWork *w);

@@ -22,7 +22,7 @@
 
 namespace biofem {
 
-static std::string g_last_error;
+static thread_local std::string g_last_error;
 static std::mutex g_mu;
 static cudaStream_t g_stream = nullptr;
 static bool g_init = false;
@@ -149,10 +149,12 @@ struct BiofemGpuMesh_ {
   double *d_x = nullptr, *d_R = nullptr;   /* staging for host-array calls */
   void *d_K = nullptr;                      /* K values: double (FP64) or float (FP32-bulk) */
   SolverWork *solver = nullptr;             /* Newton/GMRES work, created on first solve */
+  cudaStream_t st = nullptr;                /* stream of the host-array calls and of setup/teardown */
   KernelTimer timer;
 };
 
 static std::set<BiofemGpuMesh *> g_meshes;
+static std::mutex g_meshes_mu;
 
 namespace biofem {
 /* accessors for the no-allocation residual (noalloc.cu) */
@@ -179,8 +181,8 @@ template <class T>
 static int dalloc(BiofemGpuMesh *m, T **p, size_t n)
 {
   void *q = nullptr;
-  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
-  if (e != cudaSuccess) return fail(55, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(n, 1) * sizeof(T), m->st);
+  if (e != cudaSuccess) return fail(55, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
   m->allocs.push_back(q);
   m->bytes += std::max<size_t>(n, 1) * sizeof(T);
   *p = reinterpret_cast<T *>(q);
@@ -192,16 +194,18 @@ static int dupload(BiofemGpuMesh *m, T **p, const std::vector<T> &h)
 {
   int rc = dalloc(m, p, h.size());
   if (rc) return rc;
-  if (!h.empty()) CUDA_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  if (!h.empty()) CUDA_TRY(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, m->st));
   return 0;
 }
 
 static void free_mesh(BiofemGpuMesh *m)
 {
+  if (m->st) cudaStreamSynchronize(m->st);
   if (m->solver) solver_destroy(m->solver);
   for (int i = 0; i <= kMaxTimed; i++) if (m->timer.ev[i]) cudaEventDestroy(m->timer.ev[i]);
-  for (void *p : m->allocs) cudaFree(p);
+  for (void *p : m->allocs) cudaFreeAsync(p, m->st);
   m->allocs.clear();
+  if (m->st) cudaStreamSynchronize(m->st);
   delete m;
 }
 
@@ -410,6 +414,14 @@ int InitGpuWorkspace(void)
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev == 0) return fail(76, std::string("no CUDA device: ") + cudaGetErrorString(e));
   CUDA_TRY(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+  /* keep freed handle memory in the stream-ordered pool for reuse (serving
+     creates and destroys handles continuously) */
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
   g_init = true;
   return 0;
 }
@@ -417,8 +429,11 @@ int InitGpuWorkspace(void)
 int DestroyGpuWorkspace(void)
 {
   std::lock_guard<std::mutex> lk(g_mu);
-  for (BiofemGpuMesh *m : g_meshes) free_mesh(m);
-  g_meshes.clear();
+  {
+    std::lock_guard<std::mutex> lk2(g_meshes_mu);
+    for (BiofemGpuMesh *m : g_meshes) free_mesh(m);
+    g_meshes.clear();
+  }
   if (g_stream) cudaStreamDestroy(g_stream);
   g_stream = nullptr;
   g_init = false;
@@ -449,12 +464,19 @@ int DestroyHostMesh(BiofemGpuMesh *m) { delete m; return 0; }
 
 int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, BiofemGpuMesh **out)
 {
+  if (!g_init) { int rc = InitGpuWorkspace(); if (rc) return rc; }
+  return PrepareGpuMeshOnStream(mesh, params, g_stream, out);
+}
+
+int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *params, void *stream, BiofemGpuMesh **out)
+{
   if (!mesh || !params || !out) return fail(85, "null argument");
   int rc = check_params(*params);
   if (rc) return rc;
   if (!g_init) { rc = InitGpuWorkspace(); if (rc) return rc; }
   BiofemGpuMesh *m = new BiofemGpuMesh();
   m->prm = *params;
+  m->st = stream ? (cudaStream_t)stream : g_stream;
   std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx, blkrow, cidx;
   std::vector<long long> kofs, cptr;
   std::vector<unsigned char> rowkind;
@@ -468,6 +490,8 @@ int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofe
   kp.mu = params->mu; kp.K = params->bulk_modulus; kp.hhalf = 0.5 * params->h0;
   kp.pressure = params->pressure; kp.gamma = params->gamma;
   gauss(params->n_qp, kp.theta, kp.w);
+  kp.muf = (float)kp.mu; kp.Kf = (float)kp.K; kp.hhalff = (float)kp.hhalf; kp.pres6f = (float)(kp.pressure / 6.0);
+  for (int q = 0; q < kMaxQp; q++) { kp.thetaf[q] = (float)kp.theta[q]; kp.wf[q] = (float)kp.w[q]; }
 
   DevMesh &dm = m->dm;
   std::vector<int> ghost3(3 * (size_t)ng);
@@ -475,10 +499,17 @@ int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofe
   std::vector<int> etri(T.tri_all.begin(), T.tri_all.begin() + 3 * (size_t)ne);
   std::vector<double> tabs(kNumTables * 80);
   host_tables(tabs.data());
+  std::vector<float> tabsF(kNumTables * 85);
+  for (int i = 0; i < kNumTables * 80; i++) tabsF[i] = (float)tabs[i];
+  for (int i = 0; i < kNumTables * 5; i++) {
+    double acc = 0.0;
+    for (int k = 0; k < 16; k++) acc += tabs[i * 16 + k];
+    tabsF[kNumTables * 80 + i] = (float)acc;
+  }
   std::vector<double> fib(mesh->n_fib, mesh->n_fib + 3 * (size_t)ne), gsc(mesh->gamma_scale, mesh->gamma_scale + ne);
 
 #define UP(field, vec) do { rc = dupload(m, const_cast<std::remove_const<std::remove_pointer<decltype(dm.field)>::type>::type **>(&dm.field), vec); if (rc) { free_mesh(m); return rc; } } while (0)
-  UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(etri, etri); UP(ghost3, ghost3); UP(kofs, kofs);
+  UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3); UP(kofs, kofs);
   UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(pptr, pptr); UP(pidx, pidx);
   UP(rowptr, m->rowptr); UP(colind, m->colind); UP(blkrow, blkrow); UP(cptr, cptr); UP(cidx, cidx);
 #undef UP
@@ -507,20 +538,23 @@ int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofe
   }
   dm.eref = d_eref;
   dm.erefF = d_erefF;
-  CUDA_TRY(cudaMemset(dm.status, 0, sizeof(int)));
-  CUDA_TRY(cudaMemset(dm.fp, 0, 3 * sizeof(double) * (size_t)ne));
+  CUDA_TRY(cudaMemsetAsync(dm.status, 0, sizeof(int), m->st));
+  CUDA_TRY(cudaMemsetAsync(dm.fp, 0, 3 * sizeof(double) * (size_t)ne, m->st));
   /* reference positions (ghosts included) -> one-time reference geometry */
-  if ((rc = launch_positions(dm, kp, dm.X, g_stream)) || (rc = launch_ref_prep(dm, kp, d_fib, d_gsc, d_eref, g_stream))) {
+  if ((rc = launch_positions(dm, kp, dm.X, m->st)) || (rc = launch_ref_prep(dm, kp, d_fib, d_gsc, d_eref, m->st))) {
     free_mesh(m);
     return fail(76, std::string("reference preparation launch: ") + cudaGetErrorString((cudaError_t)rc));
   }
-  if (d_erefF && (rc = launch_to_float(d_eref, d_erefF, (long long)nref, g_stream))) {
+  if (d_erefF && (rc = launch_to_float(d_eref, d_erefF, (long long)nref, m->st))) {
     free_mesh(m);
     return fail(76, std::string("reference conversion launch: ") + cudaGetErrorString((cudaError_t)rc));
   }
-  cudaError_t e = cudaStreamSynchronize(g_stream);
+  cudaError_t e = cudaStreamSynchronize(m->st);
   if (e != cudaSuccess) { free_mesh(m); return fail(76, std::string("reference preparation: ") + cudaGetErrorString(e)); }
-  g_meshes.insert(m);
+  {
+    std::lock_guard<std::mutex> lk(g_meshes_mu);
+    g_meshes.insert(m);
+  }
   *out = m;
   return 0;
 }
@@ -528,7 +562,12 @@ int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofe
 int DestroyGpuMesh(BiofemGpuMesh *m)
 {
   if (!m) return 0;
-  if (g_meshes.erase(m)) free_mesh(m);
+  bool mine = false;
+  {
+    std::lock_guard<std::mutex> lk(g_meshes_mu);
+    mine = g_meshes.erase(m) > 0;
+  }
+  if (mine) free_mesh(m);
   return 0;
 }
 
@@ -674,9 +713,10 @@ int BiofemGpuSync(BiofemGpuMesh *m, void *stream)
   cudaStream_t st = pick_stream(stream);
   CUDA_TRY(cudaStreamSynchronize(st));
   int status = 0;
-  CUDA_TRY(cudaMemcpy(&status, m->dm.status, sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpyAsync(&status, m->dm.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
   if (status) {
-    CUDA_TRY(cudaMemset(m->dm.status, 0, sizeof(int)));
+    CUDA_TRY(cudaMemsetAsync(m->dm.status, 0, sizeof(int), st));
     return fail(72, "CC3333 too small in the C33 solve (ModElemC33, active_strain.c:1676)");
   }
   return 0;
@@ -686,11 +726,11 @@ int RunGpuResidual(BiofemGpuMesh *m, const double *x, double *R)
 {
   if (!m || !x || !R) return fail(85, "null argument");
   const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
-  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, g_stream));
-  int rc = RunGpuResidualDevice(m, m->d_x, m->d_R, g_stream);
+  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
+  int rc = RunGpuResidualDevice(m, m->d_x, m->d_R, m->st);
   if (rc) return rc;
-  CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
-  return BiofemGpuSync(m, g_stream);
+  CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
+  return BiofemGpuSync(m, m->st);
 }
 
 int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K)
@@ -698,12 +738,12 @@ int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K
   if (!m || !x || !K) return fail(85, "null argument");
   const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
   const size_t kbytes = 9 * (size_t)m->nnzb * (m->prm.precision == BIOFEM_FP64 ? sizeof(double) : sizeof(float));
-  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, g_stream));
-  int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, m->d_K, g_stream);
+  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
+  int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, m->d_K, m->st);
   if (rc) return rc;
-  if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
-  CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, g_stream));
-  return BiofemGpuSync(m, g_stream);
+  if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
+  CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, m->st));
+  return BiofemGpuSync(m, m->st);
 }
 
 int FormFunctionFEMGpu(void *snes, const double *x, double *R, void *ctx)
@@ -722,7 +762,7 @@ void BiofemNewtonDefaults(BiofemNewtonOptions *o)
 {
   if (!o) return;
   o->rtol = 1e-10; o->atol = 0.0; o->max_newton = 20;
-  o->gmres_restart = 100; o->gmres_max_it = 5000; o->gmres_rtol = 1e-9; o->line_search = 1;
+  o->gmres_restart = 0; o->gmres_max_it = 20000; o->gmres_rtol = 1e-9; o->line_search = 1;
 }
 
 static int newton_residual_cb(void *ctx, const double *x, double *R, void *stream)
@@ -742,13 +782,14 @@ int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOpt
   if (!m->dm.patch) return fail(58, "host-only handle");
   BiofemNewtonOptions o;
   if (opt) o = *opt; else BiofemNewtonDefaults(&o);
-  if (o.gmres_restart < 1 || o.gmres_restart > 1000 || o.max_newton < 0 || o.gmres_max_it < 1)
+  if (o.gmres_restart == 0) o.gmres_restart = 3 * m->kp.nt > 50000 ? 100 : 30;   /* auto */
+  if (o.gmres_restart < 1 || o.gmres_restart > 200 || o.max_newton < 0 || o.gmres_max_it < 1)
     return fail(63, "Newton options out of range");
   const int n = 3 * m->kp.nt;
   if (!m->solver || solver_m(m->solver) != o.gmres_restart) {
     if (m->solver) solver_destroy(m->solver);
     int rc = 0;
-    m->solver = solver_create(n, m->kp.nt, o.gmres_restart, &rc);
+    m->solver = solver_create(n, m->kp.nt, o.gmres_restart, (void *)pick_stream(stream), &rc);
     if (!m->solver) return fail(55, std::string("Newton work allocation: ") + cudaGetErrorString((cudaError_t)rc));
   }
   std::string err;
@@ -766,18 +807,19 @@ int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *op
   BiofemNewtonOptions o;
   if (opt) o = *opt; else BiofemNewtonDefaults(&o);
   const size_t n = 3 * (size_t)m->kp.nt;
+  if (o.gmres_restart == 0) o.gmres_restart = n > 50000 ? 100 : 30;   /* auto */
   if (!m->solver || solver_m(m->solver) != o.gmres_restart) {
     if (m->solver) solver_destroy(m->solver);
     int rc = 0;
-    m->solver = solver_create((int)n, m->kp.nt, o.gmres_restart, &rc);
+    m->solver = solver_create((int)n, m->kp.nt, o.gmres_restart, (void *)m->st, &rc);
     if (!m->solver) return fail(55, std::string("Newton work allocation: ") + cudaGetErrorString((cudaError_t)rc));
   }
   double *dx = solver_xbuf(m->solver);
-  CUDA_TRY(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, g_stream));
-  int rc = RunGpuNewtonSolveDevice(m, dx, &o, stats, g_stream);
+  CUDA_TRY(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
+  int rc = RunGpuNewtonSolveDevice(m, dx, &o, stats, m->st);
   if (rc) return rc;
-  CUDA_TRY(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, g_stream));
-  CUDA_TRY(cudaStreamSynchronize(g_stream));
+  CUDA_TRY(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
+  CUDA_TRY(cudaStreamSynchronize(m->st));
   return 0;
 }
 

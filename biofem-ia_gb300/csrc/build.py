@@ -20,10 +20,10 @@ LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libbiofem_gpu.so"
 OBJ_DIR = LIB_DIR / "obj"
 CUDA_SOURCES = ["kernels.cu", "bridge.cu", "noalloc.cu", "solver.cu"]
-CXX_SOURCES = ["topology.cpp"]
+CXX_SOURCES = ["topology.cpp", "serve.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17"]
+CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-pthread"]
 
 
 def nvcc() -> str:
@@ -64,7 +64,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     with ThreadPoolExecutor(max_workers=4) as ex:
         objs = list(ex.map(compile_one, CUDA_SOURCES + CXX_SOURCES))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc(), *GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"linking failed:\n{r.stdout}\n{r.stderr}")

@@ -101,11 +101,20 @@ template <class R> struct EPar {
   int nq, iters;
 };
 
-template <class R> __host__ __device__ __forceinline__ EPar<R> epar(const KParams &p)
+template <class R> __host__ __device__ __forceinline__ EPar<R> epar(const KParams &p);
+template <> __host__ __device__ __forceinline__ EPar<double> epar<double>(const KParams &p)
 {
-  EPar<R> e;
-  e.mu = (R)p.mu; e.K = (R)p.K; e.hhalf = (R)p.hhalf; e.nq = p.nq; e.iters = p.iters;
-  for (int q = 0; q < kMaxQp; q++) { e.theta[q] = (R)p.theta[q]; e.w[q] = (R)p.w[q]; }
+  EPar<double> e;
+  e.mu = p.mu; e.K = p.K; e.hhalf = p.hhalf; e.nq = p.nq; e.iters = p.iters;
+  for (int q = 0; q < kMaxQp; q++) { e.theta[q] = p.theta[q]; e.w[q] = p.w[q]; }
+  return e;
+}
+/* FP32 parameters were converted on the host: no FP64 work in FP32 kernels */
+template <> __host__ __device__ __forceinline__ EPar<float> epar<float>(const KParams &p)
+{
+  EPar<float> e;
+  e.mu = p.muf; e.K = p.Kf; e.hhalf = p.hhalff; e.nq = p.nq; e.iters = p.iters;
+  for (int q = 0; q < kMaxQp; q++) { e.theta[q] = p.thetaf[q]; e.w[q] = p.wf[q]; }
   return e;
 }
 

@@ -339,17 +339,14 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
    element-size digits; the shift is put back through (sum_i N_r[i]) * x_c,
    which is not zero for the truncated second-derivative rows (their rows sum
    to -1e-4 / -1e-4 / +2e-4).  Element matrices are written in FP32. */
-__global__ void __launch_bounds__(128) k_elem_tangent_f32(DevMesh m, KParams p)
+__global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams p)
 {
   __shared__ float tabs[kNumTables * 80];
   __shared__ float tsum[kNumTables * 5];
   __shared__ float Dsh[kTanElemsPerCta][15 * 16];
   __shared__ float Tsh[kTanElemsPerCta][15 * 48];
-  for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = (float)m.ntab[i];
-  for (int i = threadIdx.x; i < kNumTables * 5; i += blockDim.x) {
-    double sacc = 0.0;
-    for (int k = 0; k < 16; k++) sacc += m.ntab[i * 16 + k];
-    tsum[i] = (float)sacc;
+  for (int i = threadIdx.x; i < kNumTables * 85; i += blockDim.x) {
+    if (i < kNumTables * 80) tabs[i] = m.ntabF[i]; else tsum[i - kNumTables * 80] = m.ntabF[i];
   }
   __syncthreads();
   const int lane = threadIdx.x & 15;
@@ -425,7 +422,7 @@ __global__ void __launch_bounds__(128) k_elem_tangent_f32(DevMesh m, KParams p)
     const float av[3] = {xk[1][0] - xk[0][0], xk[1][1] - xk[0][1], xk[1][2] - xk[0][2]};
     const float bv[3] = {xk[2][0] - xk[0][0], xk[2][1] - xk[0][1], xk[2][2] - xk[0][2]};
     const float vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
-    const float sc = (float)(-p.pressure / 6.0);
+    const float sc = -p.pres6f;
     for (int k = 0; k < 3; k++) {
       const float *v = vv[k];
       dc[k][0][0] = 0.f;        dc[k][0][1] = -sc * v[2]; dc[k][0][2] = sc * v[1];
@@ -442,7 +439,7 @@ __global__ void __launch_bounds__(128) k_elem_tangent_f32(DevMesh m, KParams p)
     float sacc = 0.f;
 #pragma unroll
     for (int r = 0; r < 5; r++) sacc = fmaf(tab[r * 16 + a], Tsh[slot][(3 * r + i) * 48 + 3 * b + j], sacc);
-    if (p.pressure != 0.0 && (a == cslot[0] || a == cslot[1] || a == cslot[2])) {
+    if (p.pres6f != 0.f && (a == cslot[0] || a == cslot[1] || a == cslot[2])) {
       for (int k = 0; k < 3; k++)
         if (b == cslot[k]) sacc += dc[k][i][j];
     }

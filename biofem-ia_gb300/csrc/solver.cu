@@ -28,10 +28,15 @@ namespace biofem {
 int noalloc_fail(int code, const std::string &msg);   /* error reporting (bridge.cu) */
 
 /* ---------------- kernels ---------------- */
+struct GmState;
+__device__ __forceinline__ bool gm_done(const GmState *gs);
+
 template <class KT>
 __global__ void k_bsr_matvec(int nb, const int *__restrict__ rowptr, const int *__restrict__ colind,
-                             const KT *__restrict__ K, const double *__restrict__ x, double *__restrict__ y)
+                             const KT *__restrict__ K, const double *__restrict__ x, double *__restrict__ y,
+                             const GmState *__restrict__ gs)
 {
+  if (gs && gm_done(gs)) return;
   /* 4 lanes per block row, lane q takes blocks q, q+4, ... */
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int row = t >> 2, q = t & 3;
@@ -78,8 +83,10 @@ __global__ void k_bj_setup(int nb, const int *__restrict__ rowptr, const int *__
   o[6] = c02 * id; o[7] = (a[1] * a[6] - a[0] * a[7]) * id; o[8] = (a[0] * a[4] - a[1] * a[3]) * id;
 }
 
-__global__ void k_bj_apply(int nb, const double *__restrict__ Dinv, const double *__restrict__ r, double *__restrict__ z)
+__global__ void k_bj_apply(int nb, const double *__restrict__ Dinv, const double *__restrict__ r, double *__restrict__ z,
+                           const GmState *__restrict__ gs)
 {
+  if (gs && gm_done(gs)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb) return;
   const double *d = Dinv + 9 * (size_t)i;
@@ -155,130 +162,305 @@ __global__ void k_zero_ghost(int nv, int nt, double *__restrict__ v)
   if (i < 3 * nt) v[i] = 0.0;
 }
 
+/* ---------------- device-resident GMRES state ---------------- */
+struct GmState {
+  int done;        /* 1 once the cycle has converged or broken down */
+  int jdone;       /* iterations completed in this cycle */
+  double bnorm, tol, resid, inv_hn;
+};
+
+/* multi-dot with early exit: columns 0..nv-1 of V against w, plus w.w as
+   column nv when self; block (c, jb) covers 8 columns and reads w once */
+constexpr int kColsPerBlock = 8;
+__global__ void k_dots_gm(int n, int nv, int self, const double *__restrict__ V, size_t ld, const double *__restrict__ w,
+                          double *__restrict__ part, const GmState *__restrict__ gs)
+{
+  if (gs->done) return;
+  __shared__ double red[kColsPerBlock][8];
+  const int ncol = nv + (self ? 1 : 0);
+  const int j0 = blockIdx.y * kColsPerBlock;
+  const int nj = min(kColsPerBlock, ncol - j0);
+  double acc[kColsPerBlock];
+#pragma unroll
+  for (int k = 0; k < kColsPerBlock; k++) acc[k] = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double wi = w[i];
+#pragma unroll
+    for (int k = 0; k < kColsPerBlock; k++) {
+      if (k < nj) {
+        const int j = j0 + k;
+        const double vi = (j < nv) ? V[(size_t)j * ld + i] : wi;
+        acc[k] += vi * wi;
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kColsPerBlock; k++) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[k][wid] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nj) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += red[threadIdx.x][q];
+    part[(size_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+__global__ void k_reduce_gm(int nparts, const double *__restrict__ part, double *__restrict__ out,
+                            const GmState *__restrict__ gs)
+{
+  if (gs->done) return;
+  const int j = blockIdx.x;
+  double v = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) v += part[(size_t)j * nparts + k];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += sh[k];
+    out[j] = t;
+  }
+}
+
+__global__ void k_axpy_gm(int n, int nv, const double *__restrict__ V, size_t ld, const double *__restrict__ h,
+                          double *__restrict__ w, const GmState *__restrict__ gs)
+{
+  if (gs->done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int j = 0; j < nv; j++) s += V[(size_t)j * ld + i] * h[j];
+  w[i] -= s;
+}
+
+__device__ __forceinline__ bool gm_done(const GmState *gs) { return gs->done != 0; }
+
+/* one Arnoldi column: H[:, j] from the two Gram-Schmidt passes, previous
+   rotations, a new rotation, residual estimate, 1/h_{j+1,j} (one thread) */
+__global__ void k_givens(int j, int m, const double *__restrict__ h1, const double *__restrict__ h2,
+                         double *__restrict__ H, double *__restrict__ cs, double *__restrict__ sn,
+                         double *__restrict__ g, GmState *__restrict__ gs)
+{
+  if (gs->done || threadIdx.x != 0) return;
+  double h2sq = 0.0;
+  for (int i = 0; i <= j; i++) { H[(size_t)i * m + j] = h1[i] + h2[i]; h2sq += h2[i] * h2[i]; }
+  const double ww = h2[j + 1];                   /* w1 . w1 from the second pass */
+  const double hn2 = ww - h2sq;
+  const double hn = hn2 > 0.0 ? sqrt(hn2) : 0.0;
+  double below = hn;                             /* H[j+1][j] before rotation */
+  for (int i = 0; i < j; i++) {
+    const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
+    H[(size_t)i * m + j] = cs[i] * a + sn[i] * b;
+    H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+  }
+  const double a = H[(size_t)j * m + j], b = below;
+  const double r = hypot(a, b);
+  cs[j] = r > 0 ? a / r : 1.0;
+  sn[j] = r > 0 ? b / r : 0.0;
+  H[(size_t)j * m + j] = r;
+  g[j + 1] = -sn[j] * g[j];
+  g[j] = cs[j] * g[j];
+  gs->resid = fabs(g[j + 1]);
+  gs->jdone = j + 1;
+  gs->inv_hn = hn > 0.0 ? 1.0 / hn : 0.0;
+  if (gs->resid <= gs->tol * gs->bnorm || hn == 0.0 || !(hn == hn)) gs->done = 1;
+}
+
+/* v_{j+1} = w2 / h_{j+1,j} (kept even on the converged iteration: unused) */
+__global__ void k_next_basis(int n, const double *__restrict__ w, double *__restrict__ v, const GmState *__restrict__ gs)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = w[i] * gs->inv_hn;
+}
+
+/* y = H^-1 g over the completed iterations (one thread) */
+__global__ void k_backsolve(int m, const double *__restrict__ H, const double *__restrict__ g, double *__restrict__ y,
+                            const GmState *__restrict__ gs)
+{
+  if (threadIdx.x != 0) return;
+  const int k = gs->jdone;
+  for (int i = k - 1; i >= 0; i--) {
+    double s = g[i];
+    for (int c = i + 1; c < k; c++) s -= H[(size_t)i * m + c] * y[c];
+    y[i] = s / H[(size_t)i * m + i];
+  }
+}
+
+/* w = V y over the completed iterations */
+__global__ void k_combine(int n, const double *__restrict__ V, size_t ld, const double *__restrict__ y,
+                          double *__restrict__ w, const GmState *__restrict__ gs)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = gs->jdone;
+  double s = 0.0;
+  for (int j = 0; j < k; j++) s += V[(size_t)j * ld + i] * y[j];
+  w[i] = s;
+}
+
+/* cycle start: beta = sqrt(rr), v0 = r / beta, g = (beta, 0, ...), flags reset */
+__global__ void k_cycle_start(int m, const double *__restrict__ rr, double tol, double bnorm_in, int first,
+                              double *__restrict__ g, GmState *__restrict__ gs)
+{
+  if (threadIdx.x != 0) return;
+  const double beta = sqrt(rr[0]);
+  if (first) gs->bnorm = beta;
+  else if (bnorm_in > 0.0) gs->bnorm = bnorm_in;
+  gs->tol = tol;
+  gs->resid = beta;
+  gs->jdone = 0;
+  gs->inv_hn = beta > 0.0 ? 1.0 / beta : 0.0;
+  gs->done = (beta <= tol * gs->bnorm || beta == 0.0) ? 1 : 0;
+  for (int i = 0; i <= m; i++) g[i] = 0.0;
+  g[0] = beta;
+}
+
 /* ---------------- host side ---------------- */
 static inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 struct SolverWork {
   int n = 0, nb = 0, m = 0;
-  double *V = nullptr, *z = nullptr, *w = nullptr, *dinv = nullptr, *part = nullptr, *dots = nullptr;
+  double *V = nullptr, *z = nullptr, *w = nullptr, *dinv = nullptr, *part = nullptr;
+  double *h1 = nullptr, *h2 = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
   double *dx = nullptr, *xt = nullptr, *Rt = nullptr, *xh = nullptr;
-  double *hdots = nullptr;   /* pinned */
+  GmState *gs = nullptr;
+  GmState *hgs = nullptr;    /* pinned host copy */
+  double *hscal = nullptr;   /* pinned host scalar */
+  cudaEvent_t ev = nullptr;
+  /* captured restart cycle and the arguments it was captured for */
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  const double *g_b = nullptr;
+  double *g_dx = nullptr;
+  const void *g_K = nullptr;
+  double g_rtol = -1.0, g_bnorm = -1.0;
+  cudaStream_t st = nullptr;   /* allocation stream */
 };
 
+/* Restarted GMRES(m) with right block-Jacobi preconditioning; the Arnoldi
+   process, the Givens rotations and the small triangular solve all run on the
+   device.  Kernels skip their work once the cycle has converged, so the host
+   enqueues iterations ahead and only reads the convergence flag every
+   kCheck iterations. */
 class Gmres {
  public:
+  static constexpr int kCheck = 8;
+
   Gmres(const DevMesh &dm, const KParams &kp, bool f32, const void *K, SolverWork &w, cudaStream_t st)
       : dm_(dm), kp_(kp), f32_(f32), K_(K), w_(w), st_(st) {}
 
-  int matvec(const double *x, double *y)
+  void matvec(const double *x, double *y, const GmState *gs)
   {
-    if (f32_) k_bsr_matvec<float><<<nblk(4LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, x, y);
-    else k_bsr_matvec<double><<<nblk(4LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const double *)K_, x, y);
-    return (int)cudaGetLastError();
+    if (f32_) k_bsr_matvec<float><<<nblk(4LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, x, y, gs);
+    else k_bsr_matvec<double><<<nblk(4LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const double *)K_, x, y, gs);
   }
-  int precond(const double *r, double *z)
+  void precond(const double *r, double *z, const GmState *gs)
   {
-    k_bj_apply<<<nblk(w_.nb, 256), 256, 0, st_>>>(w_.nb, w_.dinv, r, z);
-    return (int)cudaGetLastError();
+    k_bj_apply<<<nblk(w_.nb, 256), 256, 0, st_>>>(w_.nb, w_.dinv, r, z, gs);
   }
-  /* h[0..nv) = V[:, 0..nv)^T v, returned on the host */
-  int dots(int nv, const double *v, double *h)
-  {
-    k_multidot<<<dim3(kDotBlocks, nv), 256, 0, st_>>>(w_.n, nv, w_.V, (size_t)w_.n, v, w_.part);
-    k_reduce_parts<<<nv, 128, 0, st_>>>(nv, kDotBlocks, w_.part, w_.dots);
-    cudaMemcpyAsync(w_.hdots, w_.dots, nv * sizeof(double), cudaMemcpyDeviceToHost, st_);
-    cudaError_t e = cudaStreamSynchronize(st_);
-    if (e != cudaSuccess) return (int)e;
-    for (int j = 0; j < nv; j++) h[j] = w_.hdots[j];
-    return 0;
-  }
-  /* dot of two arbitrary vectors (uses the part buffer with V as one column) */
+  /* a . b into a host double (synchronous) */
   int dot2(const double *a, const double *b, double &out)
   {
     k_multidot<<<dim3(kDotBlocks, 1), 256, 0, st_>>>(w_.n, 1, a, (size_t)w_.n, b, w_.part);
-    k_reduce_parts<<<1, 128, 0, st_>>>(1, kDotBlocks, w_.part, w_.dots);
-    cudaMemcpyAsync(w_.hdots, w_.dots, sizeof(double), cudaMemcpyDeviceToHost, st_);
+    k_reduce_parts<<<1, 128, 0, st_>>>(1, kDotBlocks, w_.part, w_.h1);
+    cudaMemcpyAsync(w_.hscal, w_.h1, sizeof(double), cudaMemcpyDeviceToHost, st_);
     cudaError_t e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return (int)e;
-    out = w_.hdots[0];
+    out = *w_.hscal;
     return 0;
   }
 
-  /* solve K dx = b (dx zeroed on entry); returns iterations in *its */
-  int solve(const double *b, double *dx, double rtol, int maxit, int *its, double *relres)
+  /* Enqueue one full GMRES cycle (all m iterations; kernels after
+     convergence do nothing) followed by the update of dx. */
+  void enqueue_cycle(const double *b, double *dx, double rtol, double bnorm_hint, int first)
   {
     const int n = w_.n, m = w_.m;
     double *V = w_.V;
-    std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), h(m + 1), h2(m + 1), y(m);
-    double bnorm2;
-    int rc = dot2(b, b, bnorm2);
-    if (rc) return rc;
-    const double bnorm = std::sqrt(bnorm2);
+    GmState *gs = w_.gs;
+    if (!first) {                      /* r = b - K dx */
+      matvec(dx, w_.w, nullptr);
+      k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, b, -1.0, w_.w);
+    }
+    k_multidot<<<dim3(kDotBlocks, 1), 256, 0, st_>>>(n, 1, w_.w, (size_t)n, w_.w, w_.part);
+    k_reduce_parts<<<1, 128, 0, st_>>>(1, kDotBlocks, w_.part, w_.h1);
+    k_cycle_start<<<1, 32, 0, st_>>>(m, w_.h1, rtol, bnorm_hint, first, w_.g, gs);
+    k_next_basis<<<nblk(n, 256), 256, 0, st_>>>(n, w_.w, V, gs);
+    for (int j = 0; j < m; j++) {
+      double *vj = V + (size_t)j * n, *vn = V + (size_t)(j + 1) * n;
+      precond(vj, w_.z, gs);
+      matvec(w_.z, vn, gs);
+      k_dots_gm<<<dim3(kDotBlocks, (j + 1 + kColsPerBlock - 1) / kColsPerBlock), 256, 0, st_>>>(n, j + 1, 0, V, (size_t)n, vn, w_.part, gs);
+      k_reduce_gm<<<j + 1, 128, 0, st_>>>(kDotBlocks, w_.part, w_.h1, gs);
+      k_axpy_gm<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.h1, vn, gs);
+      k_dots_gm<<<dim3(kDotBlocks, (j + 2 + kColsPerBlock - 1) / kColsPerBlock), 256, 0, st_>>>(n, j + 1, 1, V, (size_t)n, vn, w_.part, gs);
+      k_reduce_gm<<<j + 2, 128, 0, st_>>>(kDotBlocks, w_.part, w_.h2, gs);
+      k_axpy_gm<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.h2, vn, gs);
+      k_givens<<<1, 32, 0, st_>>>(j, m, w_.h1, w_.h2, w_.H, w_.cs, w_.sn, w_.g, gs);
+      k_next_basis<<<nblk(n, 256), 256, 0, st_>>>(n, vn, vn, gs);
+    }
+    k_backsolve<<<1, 32, 0, st_>>>(m, w_.H, w_.g, w_.y, gs);
+    k_combine<<<nblk(n, 256), 256, 0, st_>>>(n, V, (size_t)n, w_.y, w_.w, gs);
+    precond(w_.w, w_.z, nullptr);
+    k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, w_.z, 1.0, dx);
+    cudaMemcpyAsync(w_.hgs, gs, sizeof(GmState), cudaMemcpyDeviceToHost, st_);
+  }
+
+  /* solve K dx = b (dx zeroed on entry); iterations in *its.  The restart
+     cycle is captured once into a CUDA graph and replayed. */
+  int solve(const double *b, double *dx, double rtol, int maxit, int *its, double *relres)
+  {
+    const int n = w_.n;
     *its = 0;
     *relres = 0.0;
     cudaMemsetAsync(dx, 0, n * sizeof(double), st_);
-    if (bnorm == 0.0) return 0;
-    double beta = bnorm;
-    /* r = b - K dx; dx = 0 on the first cycle */
-    k_scale_copy<<<nblk(n, 256), 256, 0, st_>>>(n, b, 1.0, w_.w);
+    double bnorm2;
+    int rc = dot2(b, b, bnorm2);
+    if (rc) return rc;
+    if (bnorm2 == 0.0) return 0;
+    const double bnorm = std::sqrt(bnorm2);
+    k_scale_copy<<<nblk(n, 256), 256, 0, st_>>>(n, b, 1.0, w_.w);       /* r = b */
+    bool first = true;
     while (*its < maxit) {
-      k_scale_copy<<<nblk(n, 256), 256, 0, st_>>>(n, w_.w, 1.0 / beta, V);
-      std::fill(g.begin(), g.end(), 0.0);
-      g[0] = beta;
-      int j = 0;
-      double res = beta;
-      for (; j < m && *its < maxit; j++) {
-        double *vj = V + (size_t)j * n, *vn = V + (size_t)(j + 1) * n;
-        if ((rc = precond(vj, w_.z)) || (rc = matvec(w_.z, vn))) return rc;
-        /* classical Gram-Schmidt, twice */
-        if ((rc = dots(j + 1, vn, h.data()))) return rc;   /* also leaves h in w_.dots */
-        k_multi_axpy<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.dots, vn, -1.0);
-        if ((rc = dots(j + 1, vn, h2.data()))) return rc;
-        k_multi_axpy<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.dots, vn, -1.0);
-        for (int i = 0; i <= j; i++) h[i] += h2[i];
-        double nn;
-        if ((rc = dot2(vn, vn, nn))) return rc;
-        const double hn = std::sqrt(nn);
-        for (int i = 0; i <= j; i++) H[(size_t)i * m + j] = h[i];
-        H[(size_t)(j + 1) * m + j] = hn;
-        for (int i = 0; i < j; i++) {
-          const double a = H[(size_t)i * m + j], bb = H[(size_t)(i + 1) * m + j];
-          H[(size_t)i * m + j] = cs[i] * a + sn[i] * bb;
-          H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * bb;
-        }
-        const double a = H[(size_t)j * m + j], bb = H[(size_t)(j + 1) * m + j];
-        const double r = std::hypot(a, bb);
-        cs[j] = r > 0 ? a / r : 1.0; sn[j] = r > 0 ? bb / r : 0.0;
-        H[(size_t)j * m + j] = r; H[(size_t)(j + 1) * m + j] = 0.0;
-        g[j + 1] = -sn[j] * g[j]; g[j] = cs[j] * g[j];
-        (*its)++;
-        res = std::fabs(g[j + 1]);
-        if (hn > 0) k_scale_copy<<<nblk(n, 256), 256, 0, st_>>>(n, vn, 1.0 / hn, vn);
-        if (res <= rtol * bnorm || hn == 0.0) { j++; break; }
+      if (first) {
+        enqueue_cycle(b, dx, rtol, bnorm, 1);
+      } else if (st_ == nullptr) {
+        enqueue_cycle(b, dx, rtol, bnorm, 0);   /* the legacy default stream cannot be captured */
+      } else {
+        rc = replay_restart_cycle(b, dx, rtol, bnorm);
+        if (rc) return rc;
       }
-      /* y = H^-1 g, dx += M^-1 V y */
-      for (int i = j - 1; i >= 0; i--) {
-        double s = g[i];
-        for (int k = i + 1; k < j; k++) s -= H[(size_t)i * m + k] * y[k];
-        y[i] = s / H[(size_t)i * m + i];
-      }
-      cudaMemcpyAsync(w_.dots, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, st_);
-      cudaMemsetAsync(w_.w, 0, n * sizeof(double), st_);
-      k_multi_axpy<<<nblk(n, 256), 256, 0, st_>>>(n, j, V, (size_t)n, w_.dots, w_.w, 1.0);
-      if ((rc = precond(w_.w, w_.z))) return rc;
-      k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, w_.z, 1.0, dx);
-      *relres = res / bnorm;
-      if (res <= rtol * bnorm) break;
-      /* restart: w = b - K dx */
-      if ((rc = matvec(dx, w_.w))) return rc;
-      k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, b, -1.0, w_.w);
-      double rr;
-      if ((rc = dot2(w_.w, w_.w, rr))) return rc;
-      beta = std::sqrt(rr);
-      *relres = beta / bnorm;
-      if (beta <= rtol * bnorm) break;
+      first = false;
+      cudaError_t e = cudaStreamSynchronize(st_);
+      if (e != cudaSuccess) return (int)e;
+      *its += w_.hgs->jdone;
+      *relres = w_.hgs->resid / bnorm;
+      if (w_.hgs->resid <= rtol * bnorm || w_.hgs->jdone == 0) break;
     }
     return (int)cudaGetLastError();
+  }
+
+  /* restart cycles run from a graph captured on first use for this (b, dx, rtol) */
+  int replay_restart_cycle(const double *b, double *dx, double rtol, double bnorm)
+  {
+    if (!w_.graph || w_.g_b != b || w_.g_dx != dx || w_.g_rtol != rtol || w_.g_K != K_ || w_.g_bnorm != bnorm) {
+      if (w_.gexec) { cudaGraphExecDestroy(w_.gexec); w_.gexec = nullptr; }
+      if (w_.graph) { cudaGraphDestroy(w_.graph); w_.graph = nullptr; }
+      cudaStream_t cap = st_;
+      cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return (int)e;
+      enqueue_cycle(b, dx, rtol, bnorm, 0);
+      e = cudaStreamEndCapture(cap, &w_.graph);
+      if (e != cudaSuccess) return (int)e;
+      e = cudaGraphInstantiate(&w_.gexec, w_.graph, 0);
+      if (e != cudaSuccess) return (int)e;
+      w_.g_b = b; w_.g_dx = dx; w_.g_rtol = rtol; w_.g_K = K_; w_.g_bnorm = bnorm;
+    }
+    return (int)cudaGraphLaunch(w_.gexec, st_);
   }
 
  private:
@@ -290,23 +472,28 @@ class Gmres {
   cudaStream_t st_;
 };
 
-SolverWork *solver_create(int n, int nb, int m, int *rc)
+SolverWork *solver_create(int n, int nb, int m, void *stream, int *rc)
 {
   SolverWork *w = new SolverWork();
   w->n = n; w->nb = nb; w->m = m;
+  w->st = (cudaStream_t)stream;
   cudaError_t e = cudaSuccess;
   const size_t dn = sizeof(double) * (size_t)n;
-  if (e == cudaSuccess) e = cudaMalloc(&w->V, dn * (size_t)(m + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&w->z, dn);
-  if (e == cudaSuccess) e = cudaMalloc(&w->w, dn);
-  if (e == cudaSuccess) e = cudaMalloc(&w->dx, dn);
-  if (e == cudaSuccess) e = cudaMalloc(&w->xt, dn);
-  if (e == cudaSuccess) e = cudaMalloc(&w->Rt, dn);
-  if (e == cudaSuccess) e = cudaMalloc(&w->xh, dn);
-  if (e == cudaSuccess) e = cudaMalloc(&w->dinv, sizeof(double) * 9 * (size_t)nb);
-  if (e == cudaSuccess) e = cudaMalloc(&w->part, sizeof(double) * (size_t)(m + 1) * kDotBlocks);
-  if (e == cudaSuccess) e = cudaMalloc(&w->dots, sizeof(double) * (m + 1));
-  if (e == cudaSuccess) e = cudaMallocHost(&w->hdots, sizeof(double) * (m + 1));
+  auto A = [&](void **p, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(p, bytes, w->st); };
+  A((void **)&w->V, dn * (size_t)(m + 1));
+  A((void **)&w->z, dn); A((void **)&w->w, dn); A((void **)&w->dx, dn); A((void **)&w->xt, dn);
+  A((void **)&w->Rt, dn); A((void **)&w->xh, dn);
+  A((void **)&w->dinv, sizeof(double) * 9 * (size_t)nb);
+  A((void **)&w->part, sizeof(double) * (size_t)(m + 2) * kDotBlocks);
+  A((void **)&w->h1, sizeof(double) * (m + 2)); A((void **)&w->h2, sizeof(double) * (m + 2));
+  A((void **)&w->H, sizeof(double) * (size_t)(m + 1) * m);
+  A((void **)&w->cs, sizeof(double) * m); A((void **)&w->sn, sizeof(double) * m);
+  A((void **)&w->g, sizeof(double) * (m + 1)); A((void **)&w->y, sizeof(double) * m);
+  A((void **)&w->gs, sizeof(GmState));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->hgs, sizeof(GmState));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->hscal, sizeof(double));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(w->st);
   *rc = (int)e;
   if (e != cudaSuccess) { solver_destroy(w); return nullptr; }
   return w;
@@ -315,8 +502,17 @@ SolverWork *solver_create(int n, int nb, int m, int *rc)
 void solver_destroy(SolverWork *w)
 {
   if (!w) return;
-  cudaFree(w->V); cudaFree(w->z); cudaFree(w->w); cudaFree(w->dx); cudaFree(w->xt); cudaFree(w->Rt);
-  cudaFree(w->xh); cudaFree(w->dinv); cudaFree(w->part); cudaFree(w->dots); cudaFreeHost(w->hdots);
+  cudaStream_t st = w->st;
+  cudaStreamSynchronize(st);
+  void *ptrs[] = {w->V, w->z, w->w, w->dx, w->xt, w->Rt, w->xh, w->dinv, w->part, w->h1, w->h2, w->H,
+                  w->cs, w->sn, w->g, w->y, w->gs};
+  for (void *p : ptrs) if (p) cudaFreeAsync(p, st);
+  cudaStreamSynchronize(st);
+  if (w->hgs) cudaFreeHost(w->hgs);
+  if (w->hscal) cudaFreeHost(w->hscal);
+  if (w->ev) cudaEventDestroy(w->ev);
+  if (w->gexec) cudaGraphExecDestroy(w->gexec);
+  if (w->graph) cudaGraphDestroy(w->graph);
   delete w;
 }
 
@@ -360,7 +556,7 @@ int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, doub
     s.gmres_its_total += its;
     s.gmres_its_last = its;
     s.gmres_relres_last = relres;
-    k_zero_ghost<<<nblk(3LL * (kp.nt - kp.nv), 256), 256, 0, st>>>(kp.nv, kp.nt, w.dx);
+    if (kp.nt > kp.nv) k_zero_ghost<<<nblk(3LL * (kp.nt - kp.nv), 256), 256, 0, st>>>(kp.nv, kp.nt, w.dx);
     /* backtracking on ||R|| */
     double alpha = 1.0, rnew = 0.0;
     for (int ls = 0; ls < 12; ls++) {

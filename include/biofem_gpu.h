@@ -19,7 +19,8 @@
  *     boundary-ring node (io.c:329-345, dmplex_geom.c:836-857).
  *   - The tangent is a 3x3-block CSR (BSR) matrix over the same node
  *     numbering.  Block values are row-major within the block.
- *   - Host-side API is single-threaded per mesh handle.
+ *   - Host-side API is single-threaded per mesh handle; different handles may
+ *     be driven from different host threads (error messages are per thread).
  */
 #ifndef BIOFEM_GPU_H
 #define BIOFEM_GPU_H
@@ -84,6 +85,11 @@ int DestroyGpuWorkspace(void);
    dA0 (main.c:1447-1452), the reference geometry of every element, the
    assembly maps and the tangent pattern, and uploads everything. */
 int PrepareGpuMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, BiofemGpuMesh **out);
+/* Same, with the handle's setup, host-array calls and teardown ordered on
+   `stream` (cudaStream_t; NULL = the workspace stream).  Device memory comes
+   from the stream-ordered pool, so handles can be created and destroyed on
+   concurrent streams without synchronising the device. */
+int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *params, void *stream, BiofemGpuMesh **out);
 int DestroyGpuMesh(BiofemGpuMesh *m);
 int GetGpuMeshInfo(const BiofemGpuMesh *m, BiofemMeshInfo *info);
 
@@ -141,8 +147,8 @@ typedef struct {
   double  rtol;              /* stop when ||R|| <= rtol ||R0||  (1e-10) */
   double  atol;              /* or ||R|| <= atol (0 = off) */
   int32_t max_newton;        /* Newton iterations (20) */
-  int32_t gmres_restart;     /* Krylov subspace size m (100) */
-  int32_t gmres_max_it;      /* total GMRES iterations per solve (5000) */
+  int32_t gmres_restart;     /* Krylov subspace size m, 1..200; 0 = 30 below 50k DOFs, else 100 */
+  int32_t gmres_max_it;      /* total GMRES iterations per solve (20000) */
   double  gmres_rtol;        /* relative linear tolerance (1e-9) */
   int32_t line_search;       /* 1 = backtracking on ||R|| */
 } BiofemNewtonOptions;
@@ -158,6 +164,28 @@ int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *op
 /* Same on a device vector d_x (updated in place). */
 int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOptions *opt, BiofemNewtonStats *stats,
                             void *stream);
+
+/* Serving loop for load-step requests (new; the reference runs each case as
+   a separate batch job, bin/biofem:352-456).  Continuous batching: requests
+   are admitted first-fit in arrival order whenever one of max_slots slots is
+   free and their device-memory estimate fits hbm_budget_bytes; admitted
+   requests run concurrently on their own streams (mesh setup + Newton load
+   step), and finished ones free their slot and memory immediately.
+   ServeSubmit copies the request; requests that can never fit the budget are
+   refused with 55.  ServeWait blocks for one ticket, returns its x, Newton
+   statistics and the submit / admission / finish times (seconds since
+   ServeCreate).  ServeStatsGet: in_use, peak_in_use bytes, active,
+   peak_active, queued, completed. */
+typedef struct BiofemServe_ BiofemServe;
+int ServeCreate(int64_t hbm_budget_bytes, int32_t max_slots, BiofemServe **out);
+int ServeSubmit(BiofemServe *s, const BiofemMeshDesc *mesh, const BiofemParams *params,
+                const BiofemNewtonOptions *opt, const double *x0, int64_t *ticket);
+int ServeWait(BiofemServe *s, int64_t ticket, double *x_out, BiofemNewtonStats *stats, double times[3]);
+int ServeStatsGet(BiofemServe *s, int64_t out[6]);
+int ServeDestroy(BiofemServe *s);
+/* Device-memory estimate the serving loop admits a request by. */
+int BiofemServeEstimateBytes(int32_t n_v, int32_t n_elmt, int32_t n_ghosts, int32_t precision,
+                             int32_t gmres_restart, int64_t *bytes);
 
 /* SNES-callback-shaped wrappers (main.c:120 FormFunctionFEM(SNES, Vec, Vec,
    void*) and the Jacobian slot SNESSetJacobian, main.c:462-466) taking host
