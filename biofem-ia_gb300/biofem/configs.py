@@ -66,8 +66,9 @@ class Workload:
 C1 = Workload("C1_flat_32x24", 32, 24, z_sigma=1e-3, activation="uniform", lambda_a=0.9, index=0)
 # C2: 256x192 cells (49,601 nodes, 98,304 triangles), smooth lambda_a field, displacement 1e-2 h.
 C2 = Workload("C2_flat_256x192", 256, 192, activation="smooth", disp_rel=1e-2, index=1)
-# C3: 1024x768 cells (788,225 nodes, 1,572,864 triangles), random fibre angle and lambda_a.
-C3 = Workload("C3_flat_1024x768", 1024, 768, activation="random", index=2)
+# C3: 1024x768 cells (788,225 nodes, 1,572,864 triangles), random fibre angle and lambda_a,
+# 6 thickness points (an extension: the reference's rule stops at 5).
+C3 = Workload("C3_flat_1024x768", 1024, 768, n_qp=6, activation="random", index=2)
 
 ALL = {w.name: w for w in (C1, C2, C3)}
 

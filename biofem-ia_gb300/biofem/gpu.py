@@ -25,6 +25,8 @@ import numpy as np
 PKG = Path(__file__).resolve().parents[1]
 LIB_PATH = PKG / "lib" / "libbiofem_gpu.so"
 
+BIOFEM_PC_AMG = 0
+BIOFEM_PC_BJACOBI = 1
 BIOFEM_FP64 = 0
 BIOFEM_FP32_BULK = 1
 
@@ -59,7 +61,7 @@ class MeshInfo(ctypes.Structure):
 class NewtonOptions(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("max_newton", ctypes.c_int32),
                 ("gmres_restart", ctypes.c_int32), ("gmres_max_it", ctypes.c_int32), ("gmres_rtol", ctypes.c_double),
-                ("line_search", ctypes.c_int32)]
+                ("line_search", ctypes.c_int32), ("preconditioner", ctypes.c_int32)]
 
 
 class NewtonStats(ctypes.Structure):

@@ -98,8 +98,9 @@ double *solver_xbuf(SolverWork *w);
 int solver_m(const SolverWork *w);
 typedef int (*ResidualFn)(void *ctx, const double *x, double *R, void *stream);
 typedef int (*JacobianFn)(void *ctx, const double *x, double *R, void *K, void *stream);
+struct AmgHier;
 int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, double *dR, double *x,
-                  const BiofemNewtonOptions &o, BiofemNewtonStats &s, SolverWork *w, cudaStream_t st,
+                  const BiofemNewtonOptions &o, BiofemNewtonStats &s, SolverWork *w, AmgHier *amg, cudaStream_t st,
                   ResidualFn residual, JacobianFn jacobian, void *ctx, std::string &err);
 void host_tables(double *out);   /* kNumTables*5*16 host copy of the basis tables */
 

@@ -18,6 +18,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "amg.h"
 #include "biofem_host.h"
 
 namespace biofem {
@@ -149,6 +150,8 @@ struct BiofemGpuMesh_ {
   double *d_x = nullptr, *d_R = nullptr;   /* staging for host-array calls */
   void *d_K = nullptr;                      /* K values: double (FP64) or float (FP32-bulk) */
   SolverWork *solver = nullptr;             /* Newton/GMRES work, created on first solve */
+  AmgHier *amg = nullptr;                   /* multigrid hierarchy, created on first multigrid solve */
+  std::vector<unsigned char> rowkind;       /* host copy: 0 free, 1 clamped, 2 ghost */
   cudaStream_t st = nullptr;                /* stream of the host-array calls and of setup/teardown */
   KernelTimer timer;
 };
@@ -202,6 +205,7 @@ static void free_mesh(BiofemGpuMesh *m)
 {
   if (m->st) cudaStreamSynchronize(m->st);
   if (m->solver) solver_destroy(m->solver);
+  if (m->amg) amg_destroy(m->amg);
   for (int i = 0; i <= kMaxTimed; i++) if (m->timer.ev[i]) cudaEventDestroy(m->timer.ev[i]);
   for (void *p : m->allocs) cudaFreeAsync(p, m->st);
   m->allocs.clear();
@@ -482,6 +486,7 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   std::vector<unsigned char> rowkind;
   rc = build_host_maps(m, *mesh, *params, einfo, ecorner, kofs, rowkind, rptr, ridx, pptr, pidx, blkrow, cptr, cidx);
   if (rc) { delete m; return rc; }
+  m->rowkind = rowkind;
   const HostTopo &T = m->topo;
   const int ne = T.n_elmt, nv = T.n_v, ng = T.n_ghosts, nt = nv + ng;
 
@@ -763,6 +768,7 @@ void BiofemNewtonDefaults(BiofemNewtonOptions *o)
   if (!o) return;
   o->rtol = 1e-10; o->atol = 0.0; o->max_newton = 20;
   o->gmres_restart = 0; o->gmres_max_it = 20000; o->gmres_rtol = 1e-9; o->line_search = 1;
+  o->preconditioner = BIOFEM_PC_AMG;
 }
 
 static int newton_residual_cb(void *ctx, const double *x, double *R, void *stream)
@@ -782,7 +788,10 @@ int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOpt
   if (!m->dm.patch) return fail(58, "host-only handle");
   BiofemNewtonOptions o;
   if (opt) o = *opt; else BiofemNewtonDefaults(&o);
-  if (o.gmres_restart == 0) o.gmres_restart = 3 * m->kp.nt > 50000 ? 100 : 30;   /* auto */
+  if (o.preconditioner != BIOFEM_PC_AMG && o.preconditioner != BIOFEM_PC_BJACOBI)
+    return fail(63, "unknown preconditioner");
+  const bool use_amg = o.preconditioner == BIOFEM_PC_AMG;
+  if (o.gmres_restart == 0) o.gmres_restart = (!use_amg && 3 * m->kp.nt > 50000) ? 100 : 30;   /* auto */
   if (o.gmres_restart < 1 || o.gmres_restart > 200 || o.max_newton < 0 || o.gmres_max_it < 1)
     return fail(63, "Newton options out of range");
   const int n = 3 * m->kp.nt;
@@ -792,9 +801,17 @@ int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOpt
     m->solver = solver_create(n, m->kp.nt, o.gmres_restart, (void *)pick_stream(stream), &rc);
     if (!m->solver) return fail(55, std::string("Newton work allocation: ") + cudaGetErrorString((cudaError_t)rc));
   }
+  if (use_amg && !m->amg) {
+    int rc = 0;
+    m->amg = amg_create(m->kp.nt, m->rowptr, m->colind, m->rowkind, m->topo.xyz0_full, m->topo.tri_all.data(),
+                        m->kp.ne, m->dm.rowptr, m->dm.colind, m->prm.precision != BIOFEM_FP64,
+                        pick_stream(stream), &rc);
+    if (!m->amg) return fail(55, std::string("multigrid allocation: ") + cudaGetErrorString((cudaError_t)rc));
+  }
   std::string err;
   cudaStream_t st = pick_stream(stream);
-  int rc = newton_device(m->dm, m->kp, m->prm.precision != BIOFEM_FP64, m->d_K, m->d_R, d_x, o, *stats, m->solver, st,
+  int rc = newton_device(m->dm, m->kp, m->prm.precision != BIOFEM_FP64, m->d_K, m->d_R, d_x, o, *stats, m->solver,
+                         use_amg ? m->amg : nullptr, st,
                          newton_residual_cb, newton_jacobian_cb, m, err);
   if (rc) return fail(rc > 1000 ? 76 : rc, "Newton " + err + " step failed: " + g_last_error);
   return BiofemGpuSync(m, stream);
@@ -807,14 +824,7 @@ int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *op
   BiofemNewtonOptions o;
   if (opt) o = *opt; else BiofemNewtonDefaults(&o);
   const size_t n = 3 * (size_t)m->kp.nt;
-  if (o.gmres_restart == 0) o.gmres_restart = n > 50000 ? 100 : 30;   /* auto */
-  if (!m->solver || solver_m(m->solver) != o.gmres_restart) {
-    if (m->solver) solver_destroy(m->solver);
-    int rc = 0;
-    m->solver = solver_create((int)n, m->kp.nt, o.gmres_restart, (void *)m->st, &rc);
-    if (!m->solver) return fail(55, std::string("Newton work allocation: ") + cudaGetErrorString((cudaError_t)rc));
-  }
-  double *dx = solver_xbuf(m->solver);
+  double *dx = m->d_x;
   CUDA_TRY(cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
   int rc = RunGpuNewtonSolveDevice(m, dx, &o, stats, m->st);
   if (rc) return rc;

@@ -26,6 +26,10 @@
 
 #include "biofem_host.h"
 
+namespace biofem {
+int noalloc_fail(int code, const std::string &msg);   /* sets the calling thread's last error (bridge.cu) */
+}
+
 namespace {
 
 struct ServeReq {
@@ -120,12 +124,13 @@ int BiofemServeEstimateBytes(int32_t n_v, int32_t n_elmt, int32_t n_ghosts, int3
 {
   if (!bytes) return 85;
   const int64_t nt = (int64_t)n_v + n_ghosts;
-  const int m = gmres_restart > 0 ? gmres_restart : (3 * nt > 50000 ? 100 : 30);
+  const int m = gmres_restart > 0 ? gmres_restart : 30;
   /* per element: element-matrix scratch (144 blocks of 9 values), forces,
      reference constants, assembly map; per node: tangent row (~37 blocks),
-     pattern, GMRES basis */
+     pattern, flexible-GMRES bases V and Z, multigrid hierarchy (FP32 copy of
+     the tangent for FP64 handles, P, A P, the coarse operators) */
   const int64_t per_elem = precision == BIOFEM_FP64 ? 12800 : 7700;
-  const int64_t per_node = (precision == BIOFEM_FP64 ? 3500 : 2100) + (int64_t)(m + 8) * 24;
+  const int64_t per_node = (precision == BIOFEM_FP64 ? 3500 + 1400 : 2100) + (int64_t)(2 * m + 8) * 24 + 3300;
   *bytes = (per_elem * n_elmt + per_node * nt) * 5 / 4 + (8 << 20);
   return 0;
 }
@@ -194,8 +199,9 @@ int ServeWait(BiofemServe *E, int64_t ticket, double *x_out, BiofemNewtonStats *
   if (st) *st = r->st;
   if (times) { times[0] = r->t_submit; times[1] = r->t_start; times[2] = r->t_done; }
   const int rc = r->rc;
+  const std::string err = r->err;
   delete r;
-  return rc;
+  return rc ? biofem::noalloc_fail(rc, "served request: " + err) : 0;
 }
 
 int ServeStatsGet(BiofemServe *E, int64_t out[6])

@@ -6,11 +6,16 @@
  *   Newton:   x <- x + alpha dx,  K(x) dx = -R(x),  backtracking on ||R||
  *             (sufficient decrease 1e-4, halving up to 12 times), stop at
  *             ||R|| <= rtol ||R0|| (or atol).
- *   Linear:   restarted GMRES(m) with right block-Jacobi(3x3) preconditioning,
- *             classical Gram-Schmidt applied twice, Givens rotations on the
- *             host; all vectors, the BSR matvec and the dot products on the
- *             device in FP64 (the tangent values may be FP32 for an
- *             FP32-bulk handle).
+ *   Linear:   restarted flexible GMRES(m) (the preconditioned directions are
+ *             kept), preconditioned by smoothed-aggregation multigrid (FP32
+ *             V-cycle, amg.cu) or by block-Jacobi(3x3); classical
+ *             Gram-Schmidt applied twice, Givens rotations and the small
+ *             triangular solve on the device; all Krylov vectors, the BSR
+ *             matvec and the dot products in FP64 (the tangent values may be
+ *             FP32 for an FP32-bulk handle).  One iteration: preconditioner,
+ *             matvec, two projection passes (dot products with an in-kernel
+ *             deterministic reduction, the second also doing the Givens
+ *             step), and two updates.
  * Ghost rows of K are identity and their residual is zero, so ghost entries
  * of x never move.
  */
@@ -21,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "amg.h"
 #include "biofem_host.h"
 
 namespace biofem {
@@ -37,21 +43,26 @@ __global__ void k_bsr_matvec(int nb, const int *__restrict__ rowptr, const int *
                              const GmState *__restrict__ gs)
 {
   if (gs && gm_done(gs)) return;
-  /* 4 lanes per block row, lane q takes blocks q, q+4, ... */
+  /* one half-warp per block row; lane q of the half takes whole 3x3 blocks
+     q, q+16, ... so every lane issues its block's nine value loads and its
+     column's three x loads independently of the others */
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int row = t >> 2, q = t & 3;
+  const int row = t >> 4, q = t & 15;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   if (row < nb) {
-    for (int k = rowptr[row] + q; k < rowptr[row + 1]; k += 4) {
+    const int k1 = rowptr[row + 1];
+    for (int k = rowptr[row] + q; k < k1; k += 16) {
       const int c = colind[k];
-      const double x0 = x[3 * (size_t)c], x1 = x[3 * (size_t)c + 1], x2 = x[3 * (size_t)c + 2];
       const KT *b = K + 9 * (size_t)k;
-      s0 += (double)b[0] * x0 + (double)b[1] * x1 + (double)b[2] * x2;
-      s1 += (double)b[3] * x0 + (double)b[4] * x1 + (double)b[5] * x2;
-      s2 += (double)b[6] * x0 + (double)b[7] * x1 + (double)b[8] * x2;
+      const double a0 = (double)b[0], a1 = (double)b[1], a2 = (double)b[2], a3 = (double)b[3], a4 = (double)b[4];
+      const double a5 = (double)b[5], a6 = (double)b[6], a7 = (double)b[7], a8 = (double)b[8];
+      const double x0 = x[3 * (size_t)c], x1 = x[3 * (size_t)c + 1], x2 = x[3 * (size_t)c + 2];
+      s0 += a0 * x0 + a1 * x1 + a2 * x2;
+      s1 += a3 * x0 + a4 * x1 + a5 * x2;
+      s2 += a6 * x0 + a7 * x1 + a8 * x2;
     }
   }
-  for (int o = 1; o < 4; o <<= 1) {
+  for (int o = 1; o < 16; o <<= 1) {
     s0 += __shfl_xor_sync(0xffffffffu, s0, o);
     s1 += __shfl_xor_sync(0xffffffffu, s1, o);
     s2 += __shfl_xor_sync(0xffffffffu, s2, o);
@@ -169,34 +180,50 @@ struct GmState {
   double bnorm, tol, resid, inv_hn;
 };
 
-/* multi-dot with early exit: columns 0..nv-1 of V against w, plus w.w as
-   column nv when self; block (c, jb) covers 8 columns and reads w once */
-constexpr int kColsPerBlock = 8;
-__global__ void k_dots_gm(int n, int nv, int self, const double *__restrict__ V, size_t ld, const double *__restrict__ w,
-                          double *__restrict__ part, const GmState *__restrict__ gs)
+/* Gram-Schmidt projections.  k_gs_dots forms the partial dot products of w
+   with columns 0..nv-1 of V (plus w.w as column nv on the second pass), 8
+   columns per grid row and kGsChunks strided row chunks per column; the last
+   block to finish (counted on an atomic ticket, the partials made visible by
+   a fence) reduces the partials of every column in a fixed order, so the
+   result does not depend on block scheduling.  On the second pass the same
+   block completes the Arnoldi column: H[:, j] = h1 + h2, the previous Givens
+   rotations, a new rotation, the residual estimate and 1/h_{j+1,j}. */
+constexpr int kGsChunks = 304;      /* 2 x 152 SMs */
+constexpr int kGsCols = 8;
+constexpr int kMaxRestart = 200;
+
+__global__ void __launch_bounds__(256) k_gs_dots(int n, int nv, int pass2, const double *__restrict__ V, size_t ld,
+                                                 const double *__restrict__ w, double *__restrict__ part,
+                                                 unsigned *__restrict__ ticket, double *__restrict__ out,
+                                                 const double *__restrict__ h1, int j, int m, double *__restrict__ H,
+                                                 double *__restrict__ cs, double *__restrict__ sn,
+                                                 double *__restrict__ g, GmState *__restrict__ gs)
 {
   if (gs->done) return;
-  __shared__ double red[kColsPerBlock][8];
-  const int ncol = nv + (self ? 1 : 0);
-  const int j0 = blockIdx.y * kColsPerBlock;
-  const int nj = min(kColsPerBlock, ncol - j0);
-  double acc[kColsPerBlock];
+  __shared__ double red[kGsCols][8];
+  __shared__ double hs[kMaxRestart + 2];
+  __shared__ double col[kMaxRestart + 2], css[kMaxRestart], sns[kMaxRestart];
+  __shared__ int last;
+  const int ncol = nv + (pass2 ? 1 : 0);
+  const int j0 = blockIdx.y * kGsCols;
+  const int nj = min(kGsCols, ncol - j0);
+  double acc[kGsCols];
 #pragma unroll
-  for (int k = 0; k < kColsPerBlock; k++) acc[k] = 0.0;
+  for (int k = 0; k < kGsCols; k++) acc[k] = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double wi = w[i];
 #pragma unroll
-    for (int k = 0; k < kColsPerBlock; k++) {
+    for (int k = 0; k < kGsCols; k++) {
       if (k < nj) {
-        const int j = j0 + k;
-        const double vi = (j < nv) ? V[(size_t)j * ld + i] : wi;
+        const int c = j0 + k;
+        const double vi = (c < nv) ? V[(size_t)c * ld + i] : wi;
         acc[k] += vi * wi;
       }
     }
   }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int k = 0; k < kColsPerBlock; k++) {
+  for (int k = 0; k < kGsCols; k++) {
     double v = acc[k];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) red[k][wid] = v;
@@ -204,27 +231,52 @@ __global__ void k_dots_gm(int n, int nv, int self, const double *__restrict__ V,
   __syncthreads();
   if (threadIdx.x < nj) {
     double t = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += red[threadIdx.x][q];
+    for (int q = 0; q < nw; q++) t += red[threadIdx.x][q];
     part[(size_t)(j0 + threadIdx.x) * gridDim.x + blockIdx.x] = t;
+    __threadfence();
   }
-}
-
-__global__ void k_reduce_gm(int nparts, const double *__restrict__ part, double *__restrict__ out,
-                            const GmState *__restrict__ gs)
-{
-  if (gs->done) return;
-  const int j = blockIdx.x;
-  double v = 0.0;
-  for (int k = threadIdx.x; k < nparts; k += blockDim.x) v += part[(size_t)j * nparts + k];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __shared__ double sh[32];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x * gridDim.y - 1;
+  __syncthreads();
+  if (!last) return;
+  /* the last block: fixed-order reduction of every column */
+  for (int c = wid; c < ncol; c += nw) {
+    double v = 0.0;
+    for (int p = lane; p < (int)gridDim.x; p += 32) v += __ldcg(part + (size_t)c * gridDim.x + p);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) hs[c] = v;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+  __syncthreads();
+  for (int c = threadIdx.x; c < ncol; c += blockDim.x) out[c] = hs[c];
+  if (!pass2) return;
+  for (int i = threadIdx.x; i <= j; i += blockDim.x) col[i] = h1[i] + hs[i];
+  for (int i = threadIdx.x; i < j; i += blockDim.x) { css[i] = cs[i]; sns[i] = sn[i]; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += sh[k];
-    out[j] = t;
+    double h2sq = 0.0;
+    for (int i = 0; i <= j; i++) h2sq += hs[i] * hs[i];
+    const double hn2 = hs[j + 1] - h2sq;       /* w1.w1 - |h2|^2 = |w2|^2 */
+    const double hn = hn2 > 0.0 ? sqrt(hn2) : 0.0;
+    for (int i = 0; i < j; i++) {
+      const double a = col[i], b = col[i + 1];
+      col[i] = css[i] * a + sns[i] * b;
+      col[i + 1] = -sns[i] * a + css[i] * b;
+    }
+    const double a = col[j], b = hn;
+    const double r = hypot(a, b);
+    cs[j] = r > 0 ? a / r : 1.0;
+    sn[j] = r > 0 ? b / r : 0.0;
+    col[j] = r;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    gs->resid = fabs(g[j + 1]);
+    gs->jdone = j + 1;
+    gs->inv_hn = hn > 0.0 ? 1.0 / hn : 0.0;
+    if (gs->resid <= gs->tol * gs->bnorm || hn == 0.0 || !(hn == hn)) gs->done = 1;
   }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= j; i += blockDim.x) H[(size_t)i * m + j] = col[i];
 }
 
 __global__ void k_axpy_gm(int n, int nv, const double *__restrict__ V, size_t ld, const double *__restrict__ h,
@@ -240,42 +292,18 @@ __global__ void k_axpy_gm(int n, int nv, const double *__restrict__ V, size_t ld
 
 __device__ __forceinline__ bool gm_done(const GmState *gs) { return gs->done != 0; }
 
-/* one Arnoldi column: H[:, j] from the two Gram-Schmidt passes, previous
-   rotations, a new rotation, residual estimate, 1/h_{j+1,j} (one thread) */
-__global__ void k_givens(int j, int m, const double *__restrict__ h1, const double *__restrict__ h2,
-                         double *__restrict__ H, double *__restrict__ cs, double *__restrict__ sn,
-                         double *__restrict__ g, GmState *__restrict__ gs)
+/* Second projection and normalisation in one pass: v = (w - V h) / h_{j+1,j}.
+   With nv = 0 it starts a cycle: v0 = r / beta.  Skipped once the cycle has
+   converged (the next basis vector is unused). */
+__global__ void k_gs_update(int n, int nv, const double *__restrict__ V, size_t ld, const double *__restrict__ h,
+                            const double *__restrict__ w, double *__restrict__ v, const GmState *__restrict__ gs)
 {
-  if (gs->done || threadIdx.x != 0) return;
-  double h2sq = 0.0;
-  for (int i = 0; i <= j; i++) { H[(size_t)i * m + j] = h1[i] + h2[i]; h2sq += h2[i] * h2[i]; }
-  const double ww = h2[j + 1];                   /* w1 . w1 from the second pass */
-  const double hn2 = ww - h2sq;
-  const double hn = hn2 > 0.0 ? sqrt(hn2) : 0.0;
-  double below = hn;                             /* H[j+1][j] before rotation */
-  for (int i = 0; i < j; i++) {
-    const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
-    H[(size_t)i * m + j] = cs[i] * a + sn[i] * b;
-    H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
-  }
-  const double a = H[(size_t)j * m + j], b = below;
-  const double r = hypot(a, b);
-  cs[j] = r > 0 ? a / r : 1.0;
-  sn[j] = r > 0 ? b / r : 0.0;
-  H[(size_t)j * m + j] = r;
-  g[j + 1] = -sn[j] * g[j];
-  g[j] = cs[j] * g[j];
-  gs->resid = fabs(g[j + 1]);
-  gs->jdone = j + 1;
-  gs->inv_hn = hn > 0.0 ? 1.0 / hn : 0.0;
-  if (gs->resid <= gs->tol * gs->bnorm || hn == 0.0 || !(hn == hn)) gs->done = 1;
-}
-
-/* v_{j+1} = w2 / h_{j+1,j} (kept even on the converged iteration: unused) */
-__global__ void k_next_basis(int n, const double *__restrict__ w, double *__restrict__ v, const GmState *__restrict__ gs)
-{
+  if (gs->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) v[i] = w[i] * gs->inv_hn;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int k = 0; k < nv; k++) s += V[(size_t)k * ld + i] * h[k];
+  v[i] = (w[i] - s) * gs->inv_hn;
 }
 
 /* y = H^-1 g over the completed iterations (one thread) */
@@ -291,16 +319,17 @@ __global__ void k_backsolve(int m, const double *__restrict__ H, const double *_
   }
 }
 
-/* w = V y over the completed iterations */
-__global__ void k_combine(int n, const double *__restrict__ V, size_t ld, const double *__restrict__ y,
-                          double *__restrict__ w, const GmState *__restrict__ gs)
+/* dx += Z y over the completed iterations (flexible GMRES keeps the
+   preconditioned directions Z) */
+__global__ void k_combine(int n, const double *__restrict__ Z, size_t ld, const double *__restrict__ y,
+                          double *__restrict__ dx, const GmState *__restrict__ gs)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int k = gs->jdone;
   double s = 0.0;
-  for (int j = 0; j < k; j++) s += V[(size_t)j * ld + i] * y[j];
-  w[i] = s;
+  for (int j = 0; j < k; j++) s += Z[(size_t)j * ld + i] * y[j];
+  dx[i] += s;
 }
 
 /* cycle start: beta = sqrt(rr), v0 = r / beta, g = (beta, 0, ...), flags reset */
@@ -325,12 +354,14 @@ static inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
 struct SolverWork {
   int n = 0, nb = 0, m = 0;
-  double *V = nullptr, *z = nullptr, *w = nullptr, *dinv = nullptr, *part = nullptr;
+  double *V = nullptr, *Z = nullptr, *w = nullptr, *dinv = nullptr, *part = nullptr;
   double *h1 = nullptr, *h2 = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *y = nullptr;
   double *dx = nullptr, *xt = nullptr, *Rt = nullptr, *xh = nullptr;
   GmState *gs = nullptr;
+  unsigned *ticket = nullptr;  /* last-block counter of k_gs_dots (returns to 0 after each launch) */
   GmState *hgs = nullptr;    /* pinned host copy */
   double *hscal = nullptr;   /* pinned host scalar */
+  int *hstat = nullptr;      /* pinned host copy of the element status word */
   cudaEvent_t ev = nullptr;
   /* captured restart cycle and the arguments it was captured for */
   cudaGraph_t graph = nullptr;
@@ -351,17 +382,19 @@ class Gmres {
  public:
   static constexpr int kCheck = 8;
 
-  Gmres(const DevMesh &dm, const KParams &kp, bool f32, const void *K, SolverWork &w, cudaStream_t st)
-      : dm_(dm), kp_(kp), f32_(f32), K_(K), w_(w), st_(st) {}
+  Gmres(const DevMesh &dm, const KParams &kp, bool f32, const void *K, SolverWork &w, AmgHier *amg, cudaStream_t st)
+      : dm_(dm), kp_(kp), f32_(f32), K_(K), w_(w), amg_(amg), st_(st) {}
 
   void matvec(const double *x, double *y, const GmState *gs)
   {
-    if (f32_) k_bsr_matvec<float><<<nblk(4LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, x, y, gs);
-    else k_bsr_matvec<double><<<nblk(4LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const double *)K_, x, y, gs);
+    if (f32_) k_bsr_matvec<float><<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, x, y, gs);
+    else k_bsr_matvec<double><<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const double *)K_, x, y, gs);
   }
+  /* z = M^-1 r: smoothed-aggregation V-cycle, or block-Jacobi */
   void precond(const double *r, double *z, const GmState *gs)
   {
-    k_bj_apply<<<nblk(w_.nb, 256), 256, 0, st_>>>(w_.nb, w_.dinv, r, z, gs);
+    if (amg_) amg_apply(amg_, r, z, reinterpret_cast<const int *>(gs), st_);
+    else k_bj_apply<<<nblk(w_.nb, 256), 256, 0, st_>>>(w_.nb, w_.dinv, r, z, gs);
   }
   /* a . b into a host double (synchronous) */
   int dot2(const double *a, const double *b, double &out)
@@ -389,24 +422,22 @@ class Gmres {
     k_multidot<<<dim3(kDotBlocks, 1), 256, 0, st_>>>(n, 1, w_.w, (size_t)n, w_.w, w_.part);
     k_reduce_parts<<<1, 128, 0, st_>>>(1, kDotBlocks, w_.part, w_.h1);
     k_cycle_start<<<1, 32, 0, st_>>>(m, w_.h1, rtol, bnorm_hint, first, w_.g, gs);
-    k_next_basis<<<nblk(n, 256), 256, 0, st_>>>(n, w_.w, V, gs);
+    k_gs_update<<<nblk(n, 256), 256, 0, st_>>>(n, 0, V, (size_t)n, w_.h2, w_.w, V, gs);
+    const int nch = std::min(kGsChunks, nblk(n, 256));       /* row chunks per column */
     for (int j = 0; j < m; j++) {
-      double *vj = V + (size_t)j * n, *vn = V + (size_t)(j + 1) * n;
-      precond(vj, w_.z, gs);
-      matvec(w_.z, vn, gs);
-      k_dots_gm<<<dim3(kDotBlocks, (j + 1 + kColsPerBlock - 1) / kColsPerBlock), 256, 0, st_>>>(n, j + 1, 0, V, (size_t)n, vn, w_.part, gs);
-      k_reduce_gm<<<j + 1, 128, 0, st_>>>(kDotBlocks, w_.part, w_.h1, gs);
+      double *vn = V + (size_t)(j + 1) * n, *zj = w_.Z + (size_t)j * n;
+      precond(V + (size_t)j * n, zj, gs);                     /* z_j = M^-1 v_j */
+      matvec(zj, vn, gs);                                     /* w = K z_j */
+      const dim3 g1(nch, (j + 1 + kGsCols - 1) / kGsCols), g2(nch, (j + 2 + kGsCols - 1) / kGsCols);
+      k_gs_dots<<<g1, 256, 0, st_>>>(n, j + 1, 0, V, (size_t)n, vn, w_.part, w_.ticket, w_.h1, nullptr, j, m,
+                                     w_.H, w_.cs, w_.sn, w_.g, gs);
       k_axpy_gm<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.h1, vn, gs);
-      k_dots_gm<<<dim3(kDotBlocks, (j + 2 + kColsPerBlock - 1) / kColsPerBlock), 256, 0, st_>>>(n, j + 1, 1, V, (size_t)n, vn, w_.part, gs);
-      k_reduce_gm<<<j + 2, 128, 0, st_>>>(kDotBlocks, w_.part, w_.h2, gs);
-      k_axpy_gm<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.h2, vn, gs);
-      k_givens<<<1, 32, 0, st_>>>(j, m, w_.h1, w_.h2, w_.H, w_.cs, w_.sn, w_.g, gs);
-      k_next_basis<<<nblk(n, 256), 256, 0, st_>>>(n, vn, vn, gs);
+      k_gs_dots<<<g2, 256, 0, st_>>>(n, j + 1, 1, V, (size_t)n, vn, w_.part, w_.ticket, w_.h2, w_.h1, j, m,
+                                     w_.H, w_.cs, w_.sn, w_.g, gs);
+      k_gs_update<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.h2, vn, vn, gs);
     }
     k_backsolve<<<1, 32, 0, st_>>>(m, w_.H, w_.g, w_.y, gs);
-    k_combine<<<nblk(n, 256), 256, 0, st_>>>(n, V, (size_t)n, w_.y, w_.w, gs);
-    precond(w_.w, w_.z, nullptr);
-    k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, w_.z, 1.0, dx);
+    k_combine<<<nblk(n, 256), 256, 0, st_>>>(n, w_.Z, (size_t)n, w_.y, dx, gs);
     cudaMemcpyAsync(w_.hgs, gs, sizeof(GmState), cudaMemcpyDeviceToHost, st_);
   }
 
@@ -469,6 +500,7 @@ class Gmres {
   bool f32_;
   const void *K_;
   SolverWork &w_;
+  AmgHier *amg_;
   cudaStream_t st_;
 };
 
@@ -481,17 +513,20 @@ SolverWork *solver_create(int n, int nb, int m, void *stream, int *rc)
   const size_t dn = sizeof(double) * (size_t)n;
   auto A = [&](void **p, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(p, bytes, w->st); };
   A((void **)&w->V, dn * (size_t)(m + 1));
-  A((void **)&w->z, dn); A((void **)&w->w, dn); A((void **)&w->dx, dn); A((void **)&w->xt, dn);
+  A((void **)&w->Z, dn * (size_t)m); A((void **)&w->w, dn); A((void **)&w->dx, dn); A((void **)&w->xt, dn);
   A((void **)&w->Rt, dn); A((void **)&w->xh, dn);
   A((void **)&w->dinv, sizeof(double) * 9 * (size_t)nb);
-  A((void **)&w->part, sizeof(double) * (size_t)(m + 2) * kDotBlocks);
+  A((void **)&w->part, sizeof(double) * (size_t)(m + 2) * std::max(kDotBlocks, kGsChunks));
   A((void **)&w->h1, sizeof(double) * (m + 2)); A((void **)&w->h2, sizeof(double) * (m + 2));
   A((void **)&w->H, sizeof(double) * (size_t)(m + 1) * m);
   A((void **)&w->cs, sizeof(double) * m); A((void **)&w->sn, sizeof(double) * m);
   A((void **)&w->g, sizeof(double) * (m + 1)); A((void **)&w->y, sizeof(double) * m);
   A((void **)&w->gs, sizeof(GmState));
+  A((void **)&w->ticket, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemsetAsync(w->ticket, 0, sizeof(unsigned), w->st);
   if (e == cudaSuccess) e = cudaMallocHost(&w->hgs, sizeof(GmState));
   if (e == cudaSuccess) e = cudaMallocHost(&w->hscal, sizeof(double));
+  if (e == cudaSuccess) e = cudaMallocHost(&w->hstat, sizeof(int));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaStreamSynchronize(w->st);
   *rc = (int)e;
@@ -504,12 +539,13 @@ void solver_destroy(SolverWork *w)
   if (!w) return;
   cudaStream_t st = w->st;
   cudaStreamSynchronize(st);
-  void *ptrs[] = {w->V, w->z, w->w, w->dx, w->xt, w->Rt, w->xh, w->dinv, w->part, w->h1, w->h2, w->H,
-                  w->cs, w->sn, w->g, w->y, w->gs};
+  void *ptrs[] = {w->V, w->Z, w->w, w->dx, w->xt, w->Rt, w->xh, w->dinv, w->part, w->h1, w->h2, w->H,
+                  w->cs, w->sn, w->g, w->y, w->gs, w->ticket};
   for (void *p : ptrs) if (p) cudaFreeAsync(p, st);
   cudaStreamSynchronize(st);
   if (w->hgs) cudaFreeHost(w->hgs);
   if (w->hscal) cudaFreeHost(w->hscal);
+  if (w->hstat) cudaFreeHost(w->hstat);
   if (w->ev) cudaEventDestroy(w->ev);
   if (w->gexec) cudaGraphExecDestroy(w->gexec);
   if (w->graph) cudaGraphDestroy(w->graph);
@@ -521,13 +557,13 @@ int solver_m(const SolverWork *w) { return w->m; }
 
 /* Newton on device data; x is a device vector (updated in place). */
 int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, double *dR, double *x,
-                  const BiofemNewtonOptions &o, BiofemNewtonStats &s, SolverWork *wp, cudaStream_t st,
+                  const BiofemNewtonOptions &o, BiofemNewtonStats &s, SolverWork *wp, AmgHier *amg, cudaStream_t st,
                   ResidualFn residual, JacobianFn jacobian, void *ctx,
                   std::string &err)
 {
   const int n = 3 * kp.nt, nb = kp.nt;
   SolverWork &w = *wp;
-  Gmres gm(dm, kp, f32, dK, w, st);
+  Gmres gm(dm, kp, f32, dK, w, amg, st);
   int rc;
   auto norm = [&](const double *v, double &out) -> int {
     double d2;
@@ -535,19 +571,37 @@ int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, doub
     out = std::sqrt(d2);
     return r;
   };
+  /* ||R|| of the residual just evaluated, and whether every element's C33
+     solve stayed in its domain (status bit 1 clear).  The word is cleared
+     after reading; bit 2 (a singular diagonal block, replaced by the
+     identity in the preconditioner) needs no action. */
+  auto checked_norm = [&](const double *v, double &out, bool &in_domain) -> int {
+    cudaMemcpyAsync(w.hstat, dm.status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    int r = norm(v, out);                 /* synchronises the stream */
+    in_domain = (*w.hstat & 1) == 0;
+    if (*w.hstat) cudaMemsetAsync(dm.status, 0, sizeof(int), st);
+    return r;
+  };
   s = BiofemNewtonStats();
   if ((rc = residual(ctx, x, dR, (void *)st))) { err = "residual"; return rc; }
   s.residual_evals++;
   double rn;
-  if ((rc = norm(dR, rn))) { err = "norm"; return rc; }
+  bool ok = true;
+  if ((rc = checked_norm(dR, rn, ok))) { err = "norm"; return rc; }
+  if (!ok) { err = "CC3333 too small in the C33 solve at the initial state (ModElemC33, active_strain.c:1676)"; return 72; }
   s.r0 = rn;
   s.rhist[0] = rn;
   for (int it = 0; it < o.max_newton; it++) {
     if (rn <= o.rtol * s.r0 || rn <= o.atol) { s.converged = 1; break; }
     if ((rc = jacobian(ctx, x, dR, dK, (void *)st))) { err = "jacobian"; return rc; }
     s.jacobian_evals++;
-    if (f32) k_bj_setup<float><<<nblk(nb, 256), 256, 0, st>>>(nb, dm.rowptr, dm.colind, (const float *)dK, w.dinv, dm.status);
-    else k_bj_setup<double><<<nblk(nb, 256), 256, 0, st>>>(nb, dm.rowptr, dm.colind, (const double *)dK, w.dinv, dm.status);
+    if (amg) {
+      if ((rc = amg_numeric(amg, dK, f32, st))) { err = "multigrid setup"; return rc; }
+    } else if (f32) {
+      k_bj_setup<float><<<nblk(nb, 256), 256, 0, st>>>(nb, dm.rowptr, dm.colind, (const float *)dK, w.dinv, dm.status);
+    } else {
+      k_bj_setup<double><<<nblk(nb, 256), 256, 0, st>>>(nb, dm.rowptr, dm.colind, (const double *)dK, w.dinv, dm.status);
+    }
     /* rhs = -R */
     k_scale_copy<<<nblk(n, 256), 256, 0, st>>>(n, dR, -1.0, w.Rt);
     int its = 0;
@@ -564,10 +618,14 @@ int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, doub
       k_axpby<<<nblk(n, 256), 256, 0, st>>>(n, alpha, w.dx, 1.0, w.xt);
       if ((rc = residual(ctx, w.xt, dR, (void *)st))) { err = "residual"; return rc; }
       s.residual_evals++;
-      if ((rc = norm(dR, rnew))) { err = "norm"; return rc; }
+      if ((rc = checked_norm(dR, rnew, ok))) { err = "norm"; return rc; }
+      /* a trial state outside the C33 solve's domain is a failed step:
+         shorten it, as a line search does on a function-domain error */
+      if (!ok) { rnew = INFINITY; alpha *= 0.5; continue; }
       if (!o.line_search || rnew <= (1.0 - 1e-4 * alpha) * rn || !std::isfinite(rn)) break;
       alpha *= 0.5;
     }
+    if (!ok) { err = "CC3333 too small in the C33 solve on every trial step (ModElemC33, active_strain.c:1676)"; return 72; }
     k_scale_copy<<<nblk(n, 256), 256, 0, st>>>(n, w.xt, 1.0, x);
     rn = rnew;
     s.newton_its++;

@@ -151,7 +151,15 @@ typedef struct {
   int32_t gmres_max_it;      /* total GMRES iterations per solve (20000) */
   double  gmres_rtol;        /* relative linear tolerance (1e-9) */
   int32_t line_search;       /* 1 = backtracking on ||R|| */
+  int32_t preconditioner;    /* BIOFEM_PC_AMG (default) or BIOFEM_PC_BJACOBI */
 } BiofemNewtonOptions;
+
+/* Preconditioners of the Newton linear solve: smoothed-aggregation multigrid
+   (rigid-body near-null space, FP32 V-cycle) or block-Jacobi on the 3x3
+   diagonal blocks.  The reference's matrix-free SNES has neither (no
+   assembled operator to precondition with). */
+#define BIOFEM_PC_AMG 0
+#define BIOFEM_PC_BJACOBI 1
 
 typedef struct {
   int32_t newton_its, gmres_its_total, gmres_its_last, residual_evals, jacobian_evals, converged;

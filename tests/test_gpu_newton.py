@@ -50,3 +50,23 @@ def test_newton_64x48_solution_is_a_root_of_the_oracle_residual(oracle_lib):
     R = o.residual(x)
     assert np.linalg.norm(R) <= 2e-10 * np.linalg.norm(R0), (np.linalg.norm(R), np.linalg.norm(R0), st)
     sh.close()
+
+
+def test_multigrid_and_block_jacobi_reach_the_same_root():
+    """The preconditioner changes the Krylov path, not the Newton root: both
+    solves end within the stated tolerance of each other, and the multigrid
+    solve takes several times fewer GMRES iterations.  Repeated multigrid
+    solves are bitwise identical (deterministic setup and V-cycle)."""
+    from biofem.gpu import GpuShell, BIOFEM_PC_AMG, BIOFEM_PC_BJACOBI
+    w = configs.Workload("flat_48x36", 48, 36, z_sigma=1e-3, activation="smooth", index=81, pressure=3e-4)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+    xa, sa = sh.newton(x0, rtol=1e-10, preconditioner=BIOFEM_PC_AMG)
+    xa2, _ = sh.newton(x0, rtol=1e-10, preconditioner=BIOFEM_PC_AMG)
+    xb, sb = sh.newton(x0, rtol=1e-10, preconditioner=BIOFEM_PC_BJACOBI)
+    assert sa["converged"] == 1 and sb["converged"] == 1, (sa, sb)
+    np.testing.assert_array_equal(xa, xa2)
+    assert np.linalg.norm(xa - xb) <= 1e-7 * np.linalg.norm(xb - x0)
+    assert 4 * sa["gmres_its_total"] <= sb["gmres_its_total"], (sa["gmres_its_total"], sb["gmres_its_total"])
+    sh.close()
