@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="C2_flat_256x192")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solve", action="store_true", help="skip the Newton and serving measurements")
+    ap.add_argument("--serve-requests", type=int, default=128)
     return ap.parse_args()
 
 
@@ -140,6 +142,111 @@ def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0):
         if s >= warmup:
             times.append(dt)
     return n_elems * len(times) / sum(times), sum(times), n_elems
+
+
+def newton_bench(reps=3):
+    """One quasi-static load step (Newton + multigrid-preconditioned device
+    GMRES to ||R|| <= 1e-10 ||R0||) on C1 and C2, FP64 and FP32-bulk tangents;
+    wall time of RunGpuNewtonSolve (host x in and out), best of reps."""
+    from biofem import configs
+    from biofem.gpu import GpuShell
+    out = {}
+    for w in (configs.C1, configs.C2):
+        m = w.build_mesh()
+        for prec, tag in ((0, "fp64"), (1, "fp32_bulk")):
+            sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=prec)
+            x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+            best, st = None, None
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                x, st = sh.newton(x0, rtol=1e-10)
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            out[f"{w.name}_{tag}"] = {"ms": best * 1e3, "newton_its": st["newton_its"],
+                                      "gmres_its": st["gmres_its_total"], "converged": st["converged"],
+                                      "rel_residual": st["rfinal"] / st["r0"]}
+            sh.close()
+    return out
+
+
+def serve_bench(n_req=128, slots=16, budget=40 << 30, load=0.8):
+    """Load-step serving stream (C5): flat sheets with nx log-uniform in
+    [16, 256], ny = round(0.75 nx), seeded smooth imperfection, lambda_a,
+    fibre angle and pressure per request; 5 Newton iterations at most, each to
+    ||R|| <= 1e-10 ||R0||.  Sequential plain FP64 solves (mesh preparation +
+    load step, one after another) against the serving loop (continuous
+    batching, FP32-bulk tangents) run to capacity and under Poisson arrivals
+    at `load` x capacity."""
+    from biofem import configs
+    from biofem.gpu import GpuShell, Serve, BIOFEM_FP64, BIOFEM_FP32_BULK
+    newton = dict(max_newton=5, rtol=1e-10, forcing=1)
+    reqs = []
+    for i in range(n_req):
+        w = configs.serve_request(i)
+        m = w.build_mesh()
+        h = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+        reqs.append((w, m, w.initial_x(m, h.topology()["xyz0_full"])))
+        h.close()
+    w, m, x0 = reqs[0]
+    for prec in (BIOFEM_FP64, BIOFEM_FP32_BULK):         # warm-up
+        sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=prec)
+        sh.newton(x0, **newton)
+        sh.close()
+    t0 = time.perf_counter()
+    seq = []
+    for w, m, x0 in reqs:
+        sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=BIOFEM_FP64)
+        seq.append(sh.newton(x0, **newton))
+        sh.close()
+    seq_s = time.perf_counter() - t0
+
+    def served(prec, arrivals=None):
+        srv = Serve(budget, slots)
+        t_start = time.perf_counter()
+        tickets = []
+        for k, (w, m, x0) in enumerate(reqs):
+            if arrivals is not None:
+                wait = arrivals[k] - (time.perf_counter() - t_start)
+                if wait > 0:
+                    time.sleep(wait)
+            tickets.append(srv.submit(m, w, configs.MU, configs.BULK, configs.H0, x0, precision=prec, **newton))
+        res = [srv.wait(t) for t in tickets]
+        stats = srv.stats()
+        srv.close()
+        t_sub = np.array([r[2][0] for r in res])
+        t_end = np.array([r[2][2] for r in res])
+        return res, float(t_end.max() - t_sub.min()), t_end - t_sub, stats
+
+    res32, span32, _, st32 = served(BIOFEM_FP32_BULK)
+    cap32 = n_req / span32
+    res64, span64, _, _ = served(BIOFEM_FP64)
+    rng = np.random.default_rng(20261203 + 5)
+    arrivals = np.cumsum(rng.exponential(1.0 / (load * cap32), size=n_req))
+    arrivals -= arrivals[0]
+    resp, spanp, lat, stp = served(BIOFEM_FP32_BULK, arrivals)
+    conv_seq = [s[1]["converged"] for s in seq]
+    conv32 = [r[1]["converged"] for r in res32]
+    diffs = [np.linalg.norm(r[0] - s[0]) / max(np.linalg.norm(s[0] - q[2]), 1e-300)
+             for r, s, q in zip(res32, seq, reqs) if r[1]["converged"] and s[1]["converged"]]
+    same64 = all(np.array_equal(r[0], s[0]) for r, s in zip(res64, seq))
+    return {
+        "requests": n_req, "slots": slots, "hbm_budget_gb": budget / 2**30,
+        "mesh_sizes_nx": [q[0].nx for q in reqs],
+        "newton": "at most 5 iterations to ||R|| <= 1e-10 ||R0||, multigrid-preconditioned device GMRES, "
+                  "Eisenstat-Walker forcing terms (both arms)",
+        "sequential_fp64_load_steps_per_s": n_req / seq_s,
+        "served_fp32_bulk_capacity_load_steps_per_s": cap32,
+        "served_fp64_capacity_load_steps_per_s": n_req / span64,
+        "speedup_served_fp32_vs_sequential_fp64": cap32 / (n_req / seq_s),
+        "poisson": {"offered_load": load, "arrival_rate_per_s": load * cap32,
+                    "throughput_load_steps_per_s": n_req / spanp,
+                    "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                    "peak_active": stp["peak_active"]},
+        "peak_hbm_bytes_admitted": st32["peak_in_use"], "peak_active_capacity_run": st32["peak_active"],
+        "converged_sequential_fp64": int(sum(conv_seq)), "converged_served_fp32_bulk": int(sum(conv32)),
+        "max_rel_diff_fp32_served_vs_fp64_sequential_converged": float(max(diffs)) if diffs else None,
+        "served_fp64_equals_sequential_fp64_bitwise": bool(same64),
+    }
 
 
 def run_reference(args):
@@ -316,6 +423,9 @@ def run_ours(args):
             dist.destroy_process_group()
         return
 
+    newton = newton_bench() if not args.no_solve else None
+    serving = serve_bench(n_req=args.serve_requests) if not args.no_solve else None
+
     info = sh.info
     ne = info.n_elmt
     value = world * ne / (ms * 1e-3)
@@ -367,6 +477,10 @@ def run_ours(args):
         "gpu_launches": n_launch_jac * args.steps,
         "clocks": clk,
     }
+    if newton:
+        line["newton_load_step"] = newton
+    if serving:
+        line["serving"] = serving
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

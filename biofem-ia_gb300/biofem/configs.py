@@ -35,6 +35,7 @@ class Workload:
     disp_rel: float = 0.0            # displacement amplitude / edge length h
     index: int = 0
     theta: float = 0.0               # fibre angle from e_x (uniform activation)
+    z_smooth: bool = False           # smooth imperfection instead of per-node noise
 
     @property
     def seed(self) -> int:
@@ -45,7 +46,7 @@ class Workload:
         return 2 * self.nx * self.ny
 
     def build_mesh(self) -> meshmod.Mesh:
-        m = meshmod.flat_membrane(self.nx, self.ny, z_sigma=self.z_sigma, seed=self.seed)
+        m = meshmod.flat_membrane(self.nx, self.ny, z_sigma=self.z_sigma, seed=self.seed, z_smooth=self.z_smooth)
         if self.activation == "uniform":
             meshmod.set_uniform_activation(m, self.lambda_a, (np.cos(self.theta), np.sin(self.theta), 0.0))
         elif self.activation == "smooth":
@@ -85,9 +86,11 @@ SERVE_SEED = meshmod.SEED_BASE + 500
 
 def serve_request(i: int, nx_lo: int = 16, nx_hi: int = 256) -> Workload:
     """Request i of the load-step serving stream (the `biofem sweep` case mix):
-    nx = round(exp U[ln nx_lo, ln nx_hi]), ny = round(0.75 nx), z ~ N(0, 1e-3),
-    lambda_a ~ U[0.85, 1] and fibre angle ~ U[0, pi) uniform over the sheet,
-    follower pressure ~ U[1e-5, 1e-3], starting from the reference state."""
+    nx = round(exp U[ln nx_lo, ln nx_hi]), ny = round(0.75 nx), a seeded
+    smooth z imperfection of peak 1e-3 (per-node noise of that size folds the
+    shell at the finer meshes of the range), lambda_a ~ U[0.85, 1] and fibre
+    angle ~ U[0, pi) uniform over the sheet, follower pressure
+    ~ U[1e-5, 1e-3], starting from the reference state."""
     rng = np.random.default_rng(SERVE_SEED + i)
     nx = int(round(np.exp(rng.uniform(np.log(nx_lo), np.log(nx_hi)))))
     ny = max(2, int(round(0.75 * nx)))
@@ -95,4 +98,4 @@ def serve_request(i: int, nx_lo: int = 16, nx_hi: int = 256) -> Workload:
     theta = float(rng.uniform(0.0, np.pi))
     p = float(rng.uniform(1e-5, 1e-3))
     return Workload(f"serve_{i}_{nx}x{ny}", nx, ny, pressure=p, z_sigma=1e-3, activation="uniform",
-                    lambda_a=lam, index=1000 + i, theta=theta)
+                    lambda_a=lam, index=1000 + i, theta=theta, z_smooth=True)

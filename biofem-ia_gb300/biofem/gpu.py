@@ -61,7 +61,7 @@ class MeshInfo(ctypes.Structure):
 class NewtonOptions(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double), ("max_newton", ctypes.c_int32),
                 ("gmres_restart", ctypes.c_int32), ("gmres_max_it", ctypes.c_int32), ("gmres_rtol", ctypes.c_double),
-                ("line_search", ctypes.c_int32), ("preconditioner", ctypes.c_int32)]
+                ("line_search", ctypes.c_int32), ("preconditioner", ctypes.c_int32), ("forcing", ctypes.c_int32)]
 
 
 class NewtonStats(ctypes.Structure):
@@ -250,12 +250,17 @@ class GpuShell:
         return o
 
     def newton(self, x: np.ndarray, **kw):
-        """RunGpuNewtonSolve: Newton + GMRES/block-Jacobi load step from x.
-        Returns (x_converged, stats dict)."""
+        """RunGpuNewtonSolve: Newton + preconditioned GMRES load step from x.
+        Returns (x_converged, stats dict); a failure raises BiofemError with
+        the statistics gathered so far in its ``stats`` attribute."""
         x = np.array(x, dtype=np.float64, copy=True)
         o = self.newton_options(**kw)
         st = NewtonStats()
-        _check(self.lib, self.lib.RunGpuNewtonSolve(self.handle, _ptr(x), ctypes.byref(o), ctypes.byref(st)))
+        rc = self.lib.RunGpuNewtonSolve(self.handle, _ptr(x), ctypes.byref(o), ctypes.byref(st))
+        if rc:
+            err = BiofemError(rc, self.lib.BiofemGpuLastError().decode())
+            err.stats = st.as_dict()
+            raise err
         return x, st.as_dict()
 
     def newton_device(self, d_x: int, stream: int = 0, **kw):

@@ -59,13 +59,19 @@ class Mesh:
 
 
 def flat_membrane(nx: int, ny: int, lx: float = 1.0, ly: float = 0.75,
-                  z_sigma: float = 0.0, seed: int | None = None) -> Mesh:
+                  z_sigma: float = 0.0, seed: int | None = None, z_smooth: bool = False) -> Mesh:
     """Structured nx-by-ny-cell rectangle, 2 triangles per cell, CCW triangles.
 
     Node (i, j) has index j*(nx+1)+i.  Cells are ordered row-major and each
     cell emits its two triangles in order.  The single boundary ring runs
     counter-clockwise from node 0.  ``z_sigma`` > 0 adds seeded N(0, z_sigma)
-    to the z coordinate of every real node.
+    to the z coordinate of every real node; with ``z_smooth`` the
+    perturbation is instead a seeded combination of the 9 lowest sine modes
+    sin(k pi x/lx) sin(l pi y/ly), k, l = 1..3, scaled to peak z_sigma.  A
+    mesh-independent imperfection keeps the reference surface's curvature
+    bounded: per-node noise of fixed size gives curvatures ~ z_sigma / h^2,
+    which for h below ~5e-3 exceed 2/h0 and fold the shell's outer
+    thickness points.
     """
     if nx < 2 or ny < 2:
         raise ValueError("flat_membrane needs at least 2x2 cells")
@@ -77,7 +83,15 @@ def flat_membrane(nx: int, ny: int, lx: float = 1.0, ly: float = 0.75,
     xyz0[:, 1] = Y.ravel()
     if z_sigma > 0.0:
         rng = np.random.Generator(np.random.PCG64(SEED_BASE if seed is None else seed))
-        xyz0[:, 2] = rng.normal(0.0, z_sigma, size=xyz0.shape[0])
+        if z_smooth:
+            coef = rng.standard_normal((3, 3))
+            z = np.zeros(xyz0.shape[0])
+            for k in range(3):
+                for l in range(3):
+                    z += coef[k, l] * np.sin((k + 1) * np.pi * xyz0[:, 0] / lx) * np.sin((l + 1) * np.pi * xyz0[:, 1] / ly)
+            xyz0[:, 2] = z_sigma * z / max(np.abs(z).max(), 1e-300)
+        else:
+            xyz0[:, 2] = rng.normal(0.0, z_sigma, size=xyz0.shape[0])
 
     i = np.arange(nx)
     j = np.arange(ny)
@@ -104,7 +118,7 @@ def flat_membrane(nx: int, ny: int, lx: float = 1.0, ly: float = 0.75,
     fib[:, 0] = 1.0
     return Mesh(xyz0=xyz0, tri=tri, n_bnodes=np.array([ring.size], dtype=np.int32),
                 bnodes=ring, fib=fib, gamma_scale=np.zeros(n_e),
-                meta=dict(kind="flat", nx=nx, ny=ny, lx=lx, ly=ly, z_sigma=z_sigma, seed=seed))
+                meta=dict(kind="flat", nx=nx, ny=ny, lx=lx, ly=ly, z_sigma=z_sigma, seed=seed, z_smooth=z_smooth))
 
 
 def element_centroids(mesh: Mesh) -> np.ndarray:

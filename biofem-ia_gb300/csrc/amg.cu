@@ -334,15 +334,19 @@ __global__ void k_tvals(long long nnzt, const int *__restrict__ tblkrow, const i
 }
 
 /* Ac_IJ = sum_{i in P^T row I} P_iI^T T_iJ, plus 1 on the diagonal of dead
-   coarse unknowns */
+   coarse unknowns: one warp per coarse block, lanes take the fine rows in
+   turn, fixed xor-tree reduction of the 36 partial sums */
 template <int BS>
-__global__ void k_cvals(long long nnzc, const int *__restrict__ cblkrow, const int *__restrict__ ccol,
-                        const int *__restrict__ rrow, const int *__restrict__ rcol, const int *__restrict__ rmap,
-                        const float *__restrict__ P, const int *__restrict__ trow, const int *__restrict__ tcol,
-                        const float *__restrict__ T, const unsigned char *__restrict__ dead, float *__restrict__ Ac)
+__global__ void __launch_bounds__(256) k_cvals(long long nnzc, const int *__restrict__ cblkrow, const int *__restrict__ ccol,
+                                               const int *__restrict__ rrow, const int *__restrict__ rcol,
+                                               const int *__restrict__ rmap, const float *__restrict__ P,
+                                               const int *__restrict__ trow, const int *__restrict__ tcol,
+                                               const float *__restrict__ T, const unsigned char *__restrict__ dead,
+                                               float *__restrict__ Ac)
 {
-  const long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (b >= nnzc) return;
+  const long long b = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (b >= nnzc) return;                           /* whole warps leave together */
   constexpr int C = kAmgCoarseBs;
   const int I = cblkrow[b], J = ccol[b];
   float acc[C][C];
@@ -350,7 +354,7 @@ __global__ void k_cvals(long long nnzc, const int *__restrict__ cblkrow, const i
   for (int r = 0; r < C; r++)
 #pragma unroll
     for (int c = 0; c < C; c++) acc[r][c] = 0.f;
-  for (int t = rrow[I]; t < rrow[I + 1]; t++) {
+  for (int t = rrow[I] + lane; t < rrow[I + 1]; t += 32) {
     const int i = rcol[t];
     const int tb = find_col(tcol, trow[i], trow[i + 1], J);
     if (tb < 0) continue;
@@ -365,6 +369,13 @@ __global__ void k_cvals(long long nnzc, const int *__restrict__ cblkrow, const i
         for (int c = 0; c < C; c++) acc[r][c] = fmaf(psr, tt[s * C + c], acc[r][c]);
       }
   }
+#pragma unroll
+  for (int r = 0; r < C; r++)
+#pragma unroll
+    for (int c = 0; c < C; c++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[r][c] += __shfl_xor_sync(0xffffffffu, acc[r][c], o);
+  if (lane != 0) return;
   if (I == J)
 #pragma unroll
     for (int r = 0; r < C; r++)
@@ -553,20 +564,22 @@ __global__ void __launch_bounds__(256) k_resid(int n, const int *__restrict__ ro
   for (int s = 0; s < BS; s++) res[(size_t)row * BS + s] = b[(size_t)row * BS + s] - acc[s];
 }
 
-/* bc_I = sum_{i in P^T row I} P_iI^T res_i */
+/* bc_I = sum_{i in P^T row I} P_iI^T res_i: one warp per coarse node, lanes
+   take the fine rows in turn and a fixed xor-tree adds their partials */
 template <int BS>
-__global__ void k_restrict(int na, const int *__restrict__ rrow, const int *__restrict__ rcol, const int *__restrict__ rmap,
-                           const float *__restrict__ P, const float *__restrict__ res, float *__restrict__ bc,
-                           const int *done)
+__global__ void __launch_bounds__(256) k_restrict(int na, const int *__restrict__ rrow, const int *__restrict__ rcol,
+                                                  const int *__restrict__ rmap, const float *__restrict__ P,
+                                                  const float *__restrict__ res, float *__restrict__ bc, const int *done)
 {
   if (is_done(done)) return;
-  const int I = blockIdx.x * blockDim.x + threadIdx.x;
-  if (I >= na) return;
+  const int I = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (I >= na) return;                              /* whole warps leave together */
   constexpr int C = kAmgCoarseBs;
   float acc[C];
 #pragma unroll
   for (int c = 0; c < C; c++) acc[c] = 0.f;
-  for (int t = rrow[I]; t < rrow[I + 1]; t++) {
+  for (int t = rrow[I] + lane; t < rrow[I + 1]; t += 32) {
     const int i = rcol[t];
     const float *p = P + (size_t)rmap[t] * BS * C;
 #pragma unroll
@@ -577,7 +590,15 @@ __global__ void k_restrict(int na, const int *__restrict__ rrow, const int *__re
     }
   }
 #pragma unroll
-  for (int c = 0; c < C; c++) bc[(size_t)I * C + c] = acc[c];
+  for (int c = 0; c < C; c++)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  if (lane < C) {
+    float v = acc[0];
+#pragma unroll
+    for (int c = 1; c < C; c++) if (lane == c) v = acc[c];
+    bc[(size_t)I * C + lane] = v;
+  }
 }
 
 /* x_i += sum_J P_iJ xc_J */
@@ -654,6 +675,9 @@ struct AmgHier {
   std::vector<void *> allocs;
   long long bytes = 0;
   cudaStream_t st = nullptr;
+  cudaGraph_t num_graph = nullptr;      /* numeric setup, captured for one tangent buffer */
+  cudaGraphExec_t num_exec = nullptr;
+  const void *num_K = nullptr;
 };
 
 namespace {
@@ -697,7 +721,7 @@ void numeric_level(AmgHier *h, int l, cudaStream_t st)
                                                  L.par, L.P);
   k_tvals<BS><<<nblk(L.nnzT, 128), 128, 0, st>>>(L.nnzT, L.tblkrow, L.tcol, L.rowptr, L.colind, L.A, L.prow, L.pcol,
                                                  L.P, L.T);
-  k_cvals<BS><<<nblk(L.nnzC, 128), 128, 0, st>>>(L.nnzC, L.cblkrow, Cn.colind, L.rrow, L.rcol, L.rmap, L.P, L.trow,
+  k_cvals<BS><<<nblk(32LL * L.nnzC, 256), 256, 0, st>>>(L.nnzC, L.cblkrow, Cn.colind, L.rrow, L.rcol, L.rmap, L.P, L.trow,
                                                  L.tcol, L.T, L.dead, Cn.Aown);
 }
 
@@ -725,7 +749,7 @@ void down_to_coarse(AmgHier *h, int l, const int *done, cudaStream_t st)
   AmgLevelDev &Cn = h->L[l + 1];
   smooth_down<BS>(h, l, done, st);
   k_resid<BS><<<nblk(16LL * L.n, 256), 256, 0, st>>>(L.n, L.rowptr, L.colind, L.A, L.b, L.x, L.y, done);
-  k_restrict<BS><<<nblk(L.na, 128), 128, 0, st>>>(L.na, L.rrow, L.rcol, L.rmap, L.P, L.y, Cn.b, done);
+  k_restrict<BS><<<nblk(32LL * L.na, 256), 256, 0, st>>>(L.na, L.rrow, L.rcol, L.rmap, L.P, L.y, Cn.b, done);
 }
 
 template <int BS>
@@ -819,6 +843,8 @@ void amg_destroy(AmgHier *h)
 {
   if (!h) return;
   cudaStreamSynchronize(h->st);
+  if (h->num_exec) cudaGraphExecDestroy(h->num_exec);
+  if (h->num_graph) cudaGraphDestroy(h->num_graph);
   for (void *p : h->allocs) cudaFreeAsync(p, h->st);
   cudaStreamSynchronize(h->st);
   delete h;
@@ -827,13 +853,12 @@ void amg_destroy(AmgHier *h)
 int amg_levels(const AmgHier *h) { return h ? h->nl : 0; }
 long long amg_device_bytes(const AmgHier *h) { return h ? h->bytes : 0; }
 
-int amg_numeric(AmgHier *h, const void *K, bool k_is_f32, cudaStream_t st)
+static void enqueue_numeric(AmgHier *h, const void *K, bool k_is_f32, cudaStream_t st)
 {
   AmgLevelDev &L0 = h->L[0];
   if (k_is_f32) {
     L0.A = (const float *)K;
   } else {
-    if (!h->A0f) return (int)cudaErrorInvalidValue;
     const long long nv = L0.nnzA * 9;
     k_to_f32<<<nblk(nv, 256), 256, 0, st>>>(nv, (const double *)K, h->A0f);
     L0.A = h->A0f;
@@ -849,7 +874,30 @@ int amg_numeric(AmgHier *h, const void *K, bool k_is_f32, cudaStream_t st)
     const size_t smem = ((size_t)h->N * h->N + h->N) * sizeof(float);
     k_dense_invert<<<1, 1024, smem, st>>>(h->N, h->Ad);
   }
-  return (int)cudaGetLastError();
+}
+
+/* The numeric setup is a fixed launch sequence over fixed buffers, so it is
+   captured once per tangent buffer and replayed for every new tangent. */
+int amg_numeric(AmgHier *h, const void *K, bool k_is_f32, cudaStream_t st)
+{
+  if (!k_is_f32 && !h->A0f) return (int)cudaErrorInvalidValue;
+  if (st == nullptr) {                         /* the legacy default stream cannot be captured */
+    enqueue_numeric(h, K, k_is_f32, st);
+    return (int)cudaGetLastError();
+  }
+  if (!h->num_exec || h->num_K != K) {
+    if (h->num_exec) { cudaGraphExecDestroy(h->num_exec); h->num_exec = nullptr; }
+    if (h->num_graph) { cudaGraphDestroy(h->num_graph); h->num_graph = nullptr; }
+    cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return (int)e;
+    enqueue_numeric(h, K, k_is_f32, st);
+    e = cudaStreamEndCapture(st, &h->num_graph);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaGraphInstantiate(&h->num_exec, h->num_graph, 0);
+    if (e != cudaSuccess) return (int)e;
+    h->num_K = K;
+  }
+  return (int)cudaGraphLaunch(h->num_exec, st);
 }
 
 void amg_apply(AmgHier *h, const double *v, double *z, const int *done, cudaStream_t st)

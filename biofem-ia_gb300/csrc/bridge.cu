@@ -334,13 +334,13 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   blkrow.assign(m->nnzb, 0);
   for (int i = 0; i < nt; i++) for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) blkrow[k] = i;
 
-  /* element-block -> tangent-block contributions, element order */
-  auto find_blk = [&](int i, int j) -> long long {
-    const int *b = m->colind.data() + m->rowptr[i], *en = m->colind.data() + m->rowptr[i + 1];
-    const int *p = std::lower_bound(b, en, j);
-    return (p != en && *p == j) ? (long long)(p - m->colind.data()) : -1;
-  };
+  /* element-block -> tangent-block contributions, element order.  Built row
+     by row: the row's (element, slot) list is in increasing element order
+     and a real node fills one slot of a patch, so each block receives its
+     contributions in element order, then slot b, then ghost parent q.  A
+     column -> block table of the current row makes each lookup O(1). */
   cptr.assign(m->nnzb + 1, 0);
+  std::vector<long long> colpos(nt, -1);
   for (int pass = 0; pass < 2; pass++) {
     std::vector<long long> fill;
     if (pass == 1) {
@@ -350,23 +350,25 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
       cidx.assign(m->ncontrib, 0);
       fill.assign(cptr.begin(), cptr.end() - 1);
     }
-    for (int e = 0; e < ne; e++) {
-      const int nen = einfo[e] & 0xff;
-      for (int a = 0; a < nen; a++) {
-        const int i = T.patch[16 * (size_t)e + a];
-        if (i >= nv || rowkind[i] != 0) continue;
+    for (int i = 0; i < nv; i++) {
+      if (rowkind[i] != 0) continue;
+      for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) colpos[m->colind[k]] = k;
+      for (int c = rptr[i]; c < rptr[i + 1]; c++) {
+        const int e = ridx[c] % ne, a = ridx[c] / (3 * ne);
+        const int nen = einfo[e] & 0xff;
         for (int b = 0; b < nen; b++) {
           int cols[3], sg[3];
           const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
           const long long blk_id = kofs[e] + (long long)a * nen + b;
           for (int q = 0; q < k; q++) {
-            const long long kb = find_blk(i, cols[q]);
+            const long long kb = colpos[cols[q]];
             if (kb < 0) return fail(77, "tangent pattern is missing an element block");
             if (pass == 0) cptr[kb + 1]++;
             else cidx[fill[kb]++] = sg[q] > 0 ? (int)blk_id : (int)(-(blk_id + 1));
           }
         }
       }
+      for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) colpos[m->colind[k]] = -1;
     }
   }
   /* dA0 on the host too (GetGpuTopology); same expression as AreaNormal */
@@ -769,6 +771,7 @@ void BiofemNewtonDefaults(BiofemNewtonOptions *o)
   o->rtol = 1e-10; o->atol = 0.0; o->max_newton = 20;
   o->gmres_restart = 0; o->gmres_max_it = 20000; o->gmres_rtol = 1e-9; o->line_search = 1;
   o->preconditioner = BIOFEM_PC_AMG;
+  o->forcing = 0;
 }
 
 static int newton_residual_cb(void *ctx, const double *x, double *R, void *stream)
@@ -790,6 +793,7 @@ int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOpt
   if (opt) o = *opt; else BiofemNewtonDefaults(&o);
   if (o.preconditioner != BIOFEM_PC_AMG && o.preconditioner != BIOFEM_PC_BJACOBI)
     return fail(63, "unknown preconditioner");
+  if (o.forcing != 0 && o.forcing != 1) return fail(63, "unknown forcing-term rule");
   const bool use_amg = o.preconditioner == BIOFEM_PC_AMG;
   if (o.gmres_restart == 0) o.gmres_restart = (!use_amg && 3 * m->kp.nt > 50000) ? 100 : 30;   /* auto */
   if (o.gmres_restart < 1 || o.gmres_restart > 200 || o.max_newton < 0 || o.gmres_max_it < 1)

@@ -5,7 +5,8 @@
  *
  *   Newton:   x <- x + alpha dx,  K(x) dx = -R(x),  backtracking on ||R||
  *             (sufficient decrease 1e-4, halving up to 12 times), stop at
- *             ||R|| <= rtol ||R0|| (or atol).
+ *             ||R|| <= rtol ||R0|| (or atol); linear solves to a fixed
+ *             relative tolerance or to Eisenstat-Walker forcing terms.
  *   Linear:   restarted flexible GMRES(m) (the preconditioned directions are
  *             kept), preconditioned by smoothed-aggregation multigrid (FP32
  *             V-cycle, amg.cu) or by block-Jacobi(3x3); classical
@@ -333,20 +334,27 @@ __global__ void k_combine(int n, const double *__restrict__ Z, size_t ld, const 
 }
 
 /* cycle start: beta = sqrt(rr), v0 = r / beta, g = (beta, 0, ...), flags reset */
-__global__ void k_cycle_start(int m, const double *__restrict__ rr, double tol, double bnorm_in, int first,
-                              double *__restrict__ g, GmState *__restrict__ gs)
+__global__ void k_cycle_start(int m, const double *__restrict__ rr, double *__restrict__ g, GmState *__restrict__ gs)
 {
   if (threadIdx.x != 0) return;
   const double beta = sqrt(rr[0]);
-  if (first) gs->bnorm = beta;
-  else if (bnorm_in > 0.0) gs->bnorm = bnorm_in;
-  gs->tol = tol;
+  if (gs->bnorm < 0.0) gs->bnorm = beta;       /* first cycle: dx = 0, r = b */
   gs->resid = beta;
   gs->jdone = 0;
   gs->inv_hn = beta > 0.0 ? 1.0 / beta : 0.0;
-  gs->done = (beta <= tol * gs->bnorm || beta == 0.0) ? 1 : 0;
+  gs->done = (beta <= gs->tol * gs->bnorm || beta == 0.0) ? 1 : 0;
   for (int i = 0; i <= m; i++) g[i] = 0.0;
   g[0] = beta;
+}
+
+/* solve start: tolerance in, ||b|| unknown until the first cycle */
+__global__ void k_solve_begin(double tol, GmState *__restrict__ gs)
+{
+  if (threadIdx.x != 0) return;
+  gs->tol = tol;
+  gs->bnorm = -1.0;
+  gs->done = 0;
+  gs->jdone = 0;
 }
 
 /* ---------------- host side ---------------- */
@@ -369,7 +377,7 @@ struct SolverWork {
   const double *g_b = nullptr;
   double *g_dx = nullptr;
   const void *g_K = nullptr;
-  double g_rtol = -1.0, g_bnorm = -1.0;
+  const void *g_pc = nullptr;   /* preconditioner the graph was captured with (null: block-Jacobi) */
   cudaStream_t st = nullptr;   /* allocation stream */
 };
 
@@ -409,19 +417,20 @@ class Gmres {
   }
 
   /* Enqueue one full GMRES cycle (all m iterations; kernels after
-     convergence do nothing) followed by the update of dx. */
-  void enqueue_cycle(const double *b, double *dx, double rtol, double bnorm_hint, int first)
+     convergence do nothing) followed by the update of dx.  The cycle starts
+     from r = b - K dx (dx = 0 on the first cycle), and the tolerance and ||b||
+     live in the device state, so one captured graph serves every cycle of
+     every solve with the same buffers. */
+  void enqueue_cycle(const double *b, double *dx)
   {
     const int n = w_.n, m = w_.m;
     double *V = w_.V;
     GmState *gs = w_.gs;
-    if (!first) {                      /* r = b - K dx */
-      matvec(dx, w_.w, nullptr);
-      k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, b, -1.0, w_.w);
-    }
+    matvec(dx, w_.w, nullptr);
+    k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, b, -1.0, w_.w);
     k_multidot<<<dim3(kDotBlocks, 1), 256, 0, st_>>>(n, 1, w_.w, (size_t)n, w_.w, w_.part);
     k_reduce_parts<<<1, 128, 0, st_>>>(1, kDotBlocks, w_.part, w_.h1);
-    k_cycle_start<<<1, 32, 0, st_>>>(m, w_.h1, rtol, bnorm_hint, first, w_.g, gs);
+    k_cycle_start<<<1, 32, 0, st_>>>(m, w_.h1, w_.g, gs);
     k_gs_update<<<nblk(n, 256), 256, 0, st_>>>(n, 0, V, (size_t)n, w_.h2, w_.w, V, gs);
     const int nch = std::min(kGsChunks, nblk(n, 256));       /* row chunks per column */
     for (int j = 0; j < m; j++) {
@@ -441,55 +450,45 @@ class Gmres {
     cudaMemcpyAsync(w_.hgs, gs, sizeof(GmState), cudaMemcpyDeviceToHost, st_);
   }
 
-  /* solve K dx = b (dx zeroed on entry); iterations in *its.  The restart
-     cycle is captured once into a CUDA graph and replayed. */
+  /* solve K dx = b (dx zeroed on entry); iterations in *its.  Each cycle
+     runs from a graph captured on first use for these buffers and replayed
+     for every later cycle and solve; one host synchronisation per cycle
+     reads the convergence state. */
   int solve(const double *b, double *dx, double rtol, int maxit, int *its, double *relres)
   {
     const int n = w_.n;
     *its = 0;
     *relres = 0.0;
     cudaMemsetAsync(dx, 0, n * sizeof(double), st_);
-    double bnorm2;
-    int rc = dot2(b, b, bnorm2);
-    if (rc) return rc;
-    if (bnorm2 == 0.0) return 0;
-    const double bnorm = std::sqrt(bnorm2);
-    k_scale_copy<<<nblk(n, 256), 256, 0, st_>>>(n, b, 1.0, w_.w);       /* r = b */
-    bool first = true;
+    k_solve_begin<<<1, 32, 0, st_>>>(rtol, w_.gs);
+    int rc = 0;
     while (*its < maxit) {
-      if (first) {
-        enqueue_cycle(b, dx, rtol, bnorm, 1);
-      } else if (st_ == nullptr) {
-        enqueue_cycle(b, dx, rtol, bnorm, 0);   /* the legacy default stream cannot be captured */
-      } else {
-        rc = replay_restart_cycle(b, dx, rtol, bnorm);
-        if (rc) return rc;
-      }
-      first = false;
+      if (st_ == nullptr) enqueue_cycle(b, dx);   /* the legacy default stream cannot be captured */
+      else if ((rc = replay_cycle(b, dx))) return rc;
       cudaError_t e = cudaStreamSynchronize(st_);
       if (e != cudaSuccess) return (int)e;
-      *its += w_.hgs->jdone;
-      *relres = w_.hgs->resid / bnorm;
-      if (w_.hgs->resid <= rtol * bnorm || w_.hgs->jdone == 0) break;
+      const GmState &h = *w_.hgs;
+      *its += h.jdone;
+      *relres = h.bnorm > 0.0 ? h.resid / h.bnorm : 0.0;
+      if (h.bnorm == 0.0 || h.resid <= rtol * h.bnorm || h.jdone == 0) break;
     }
     return (int)cudaGetLastError();
   }
 
-  /* restart cycles run from a graph captured on first use for this (b, dx, rtol) */
-  int replay_restart_cycle(const double *b, double *dx, double rtol, double bnorm)
+  int replay_cycle(const double *b, double *dx)
   {
-    if (!w_.graph || w_.g_b != b || w_.g_dx != dx || w_.g_rtol != rtol || w_.g_K != K_ || w_.g_bnorm != bnorm) {
+    if (!w_.graph || w_.g_b != b || w_.g_dx != dx || w_.g_K != K_ || w_.g_pc != (const void *)amg_) {
       if (w_.gexec) { cudaGraphExecDestroy(w_.gexec); w_.gexec = nullptr; }
       if (w_.graph) { cudaGraphDestroy(w_.graph); w_.graph = nullptr; }
       cudaStream_t cap = st_;
       cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return (int)e;
-      enqueue_cycle(b, dx, rtol, bnorm, 0);
+      enqueue_cycle(b, dx);
       e = cudaStreamEndCapture(cap, &w_.graph);
       if (e != cudaSuccess) return (int)e;
       e = cudaGraphInstantiate(&w_.gexec, w_.graph, 0);
       if (e != cudaSuccess) return (int)e;
-      w_.g_b = b; w_.g_dx = dx; w_.g_rtol = rtol; w_.g_K = K_; w_.g_bnorm = bnorm;
+      w_.g_b = b; w_.g_dx = dx; w_.g_K = K_; w_.g_pc = amg_;
     }
     return (int)cudaGraphLaunch(w_.gexec, st_);
   }
@@ -591,8 +590,23 @@ int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, doub
   if (!ok) { err = "CC3333 too small in the C33 solve at the initial state (ModElemC33, active_strain.c:1676)"; return 72; }
   s.r0 = rn;
   s.rhist[0] = rn;
+  const double target = std::max(o.rtol * s.r0, o.atol);
+  double eta = 0.3, rn_prev = rn;
   for (int it = 0; it < o.max_newton; it++) {
     if (rn <= o.rtol * s.r0 || rn <= o.atol) { s.converged = 1; break; }
+    double ksp_rtol = o.gmres_rtol;
+    if (o.forcing == 1) {            /* Eisenstat-Walker, version 2 */
+      const double alpha = 1.6180339887498949, gamma = 1.0;
+      if (it > 0) {
+        double e = gamma * std::pow(rn / rn_prev, alpha);
+        const double guard = gamma * std::pow(eta, alpha);
+        if (guard > 0.1) e = std::max(e, guard);
+        eta = e;
+      }
+      eta = std::min(eta, 0.9);
+      ksp_rtol = std::max(std::max(eta, o.gmres_rtol), std::min(0.9, 0.5 * target / rn));
+    }
+    rn_prev = rn;
     if ((rc = jacobian(ctx, x, dR, dK, (void *)st))) { err = "jacobian"; return rc; }
     s.jacobian_evals++;
     if (amg) {
@@ -606,7 +620,7 @@ int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, doub
     k_scale_copy<<<nblk(n, 256), 256, 0, st>>>(n, dR, -1.0, w.Rt);
     int its = 0;
     double relres = 0.0;
-    if ((rc = gm.solve(w.Rt, w.dx, o.gmres_rtol, o.gmres_max_it, &its, &relres))) { err = "gmres"; return rc; }
+    if ((rc = gm.solve(w.Rt, w.dx, ksp_rtol, o.gmres_max_it, &its, &relres))) { err = "gmres"; return rc; }
     s.gmres_its_total += its;
     s.gmres_its_last = its;
     s.gmres_relres_last = relres;

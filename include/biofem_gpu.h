@@ -152,6 +152,9 @@ typedef struct {
   double  gmres_rtol;        /* relative linear tolerance (1e-9) */
   int32_t line_search;       /* 1 = backtracking on ||R|| */
   int32_t preconditioner;    /* BIOFEM_PC_AMG (default) or BIOFEM_PC_BJACOBI */
+  int32_t forcing;           /* 0: every linear solve to gmres_rtol; 1: Eisenstat-Walker (version 2) forcing
+                                terms, as PETSc's -snes_ksp_ew: eta_0 = 0.3, eta_k = (|R_k|/|R_k-1|)^1.618,
+                                safeguarded, at most 0.9, at least gmres_rtol and 0.5 (Newton target)/|R_k| */
 } BiofemNewtonOptions;
 
 /* Preconditioners of the Newton linear solve: smoothed-aggregation multigrid

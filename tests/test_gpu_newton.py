@@ -70,3 +70,21 @@ def test_multigrid_and_block_jacobi_reach_the_same_root():
     assert np.linalg.norm(xa - xb) <= 1e-7 * np.linalg.norm(xb - x0)
     assert 4 * sa["gmres_its_total"] <= sb["gmres_its_total"], (sa["gmres_its_total"], sb["gmres_its_total"])
     sh.close()
+
+
+def test_eisenstat_walker_forcing_reaches_the_same_root():
+    """Inexact Newton (Eisenstat-Walker forcing terms) stops every linear
+    solve early; the Newton target ||R|| <= 1e-10 ||R0|| and the root stay the
+    same, with fewer GMRES iterations in total."""
+    from biofem.gpu import GpuShell
+    w = configs.Workload("flat_48x36", 48, 36, z_sigma=1e-3, activation="smooth", index=82, pressure=3e-4)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+    xf, sf = sh.newton(x0, rtol=1e-10, forcing=0)
+    xe, se = sh.newton(x0, rtol=1e-10, forcing=1, max_newton=30)
+    assert sf["converged"] == 1 and se["converged"] == 1, (sf, se)
+    assert se["rfinal"] <= 1e-10 * se["r0"]
+    assert np.linalg.norm(xe - xf) <= 1e-7 * np.linalg.norm(xf - x0)
+    assert se["gmres_its_total"] < sf["gmres_its_total"], (se["gmres_its_total"], sf["gmres_its_total"])
+    sh.close()
