@@ -229,6 +229,8 @@ def serve_bench(n_req=128, slots=16, budget=40 << 30, load=0.8):
     diffs = [np.linalg.norm(r[0] - s[0]) / max(np.linalg.norm(s[0] - q[2]), 1e-300)
              for r, s, q in zip(res32, seq, reqs) if r[1]["converged"] and s[1]["converged"]]
     same64 = all(np.array_equal(r[0], s[0]) for r, s in zip(res64, seq))
+    rel_seq = np.array([s[1]["rfinal"] / s[1]["r0"] for s in seq])
+    rel32 = np.array([r[1]["rfinal"] / r[1]["r0"] for r in res32])
     return {
         "requests": n_req, "slots": slots, "hbm_budget_gb": budget / 2**30,
         "mesh_sizes_nx": [q[0].nx for q in reqs],
@@ -244,6 +246,8 @@ def serve_bench(n_req=128, slots=16, budget=40 << 30, load=0.8):
                     "peak_active": stp["peak_active"]},
         "peak_hbm_bytes_admitted": st32["peak_in_use"], "peak_active_capacity_run": st32["peak_active"],
         "converged_sequential_fp64": int(sum(conv_seq)), "converged_served_fp32_bulk": int(sum(conv32)),
+        "final_rel_residual_p50_p90_sequential_fp64": [float(np.percentile(rel_seq, 50)), float(np.percentile(rel_seq, 90))],
+        "final_rel_residual_p50_p90_served_fp32_bulk": [float(np.percentile(rel32, 50)), float(np.percentile(rel32, 90))],
         "max_rel_diff_fp32_served_vs_fp64_sequential_converged": float(max(diffs)) if diffs else None,
         "served_fp64_equals_sequential_fp64_bitwise": bool(same64),
     }

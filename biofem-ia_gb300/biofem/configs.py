@@ -36,6 +36,8 @@ class Workload:
     index: int = 0
     theta: float = 0.0               # fibre angle from e_x (uniform activation)
     z_smooth: bool = False           # smooth imperfection instead of per-node noise
+    basis: int = 0                   # 0 reference four-decimal basis tables, 1 exact (extension)
+    tnormal: int = 0                 # 1: thickness metric from n,alpha only (extension)
 
     @property
     def seed(self) -> int:
@@ -68,8 +70,11 @@ C1 = Workload("C1_flat_32x24", 32, 24, z_sigma=1e-3, activation="uniform", lambd
 # C2: 256x192 cells (49,601 nodes, 98,304 triangles), smooth lambda_a field, displacement 1e-2 h.
 C2 = Workload("C2_flat_256x192", 256, 192, activation="smooth", disp_rel=1e-2, index=1)
 # C3: 1024x768 cells (788,225 nodes, 1,572,864 triangles), random fibre angle and lambda_a,
-# 6 thickness points (an extension: the reference's rule stops at 5).
-C3 = Workload("C3_flat_1024x768", 1024, 768, n_qp=6, activation="random", index=2)
+# 6 thickness points (an extension: the reference's rule stops at 5).  With h ~ h0/10 the
+# reference's four-decimal basis tables fold the outer thickness points of every element
+# (their second-derivative rows do not sum to zero), and the normal part of a3,alpha folds
+# them on the ghost-reflected side patches, so C3 uses the exact tables and n,alpha.
+C3 = Workload("C3_flat_1024x768", 1024, 768, n_qp=6, activation="random", index=2, basis=1, tnormal=1)
 
 ALL = {w.name: w for w in (C1, C2, C3)}
 

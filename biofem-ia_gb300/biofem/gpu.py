@@ -25,6 +25,8 @@ import numpy as np
 PKG = Path(__file__).resolve().parents[1]
 LIB_PATH = PKG / "lib" / "libbiofem_gpu.so"
 
+BIOFEM_BASIS_REFERENCE = 0
+BIOFEM_BASIS_EXACT = 1
 BIOFEM_PC_AMG = 0
 BIOFEM_PC_BJACOBI = 1
 BIOFEM_FP64 = 0
@@ -49,7 +51,8 @@ class MeshDesc(ctypes.Structure):
 class Params(ctypes.Structure):
     _fields_ = [("n_qp", ctypes.c_int32), ("c33_subitr_nums", ctypes.c_int32), ("mu", ctypes.c_double),
                 ("bulk_modulus", ctypes.c_double), ("h0", ctypes.c_double), ("gamma", ctypes.c_double),
-                ("pressure", ctypes.c_double), ("clamp_edge", ctypes.c_int32), ("precision", ctypes.c_int32)]
+                ("pressure", ctypes.c_double), ("clamp_edge", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("basis", ctypes.c_int32), ("thickness_normal", ctypes.c_int32)]
 
 
 class MeshInfo(ctypes.Structure):
@@ -86,7 +89,7 @@ EXPORTS = ["InitGpuWorkspace", "DestroyGpuWorkspace", "PrepareGpuMesh", "Destroy
            "GetGpuBasisTables", "BiofemGpuLastError", "EnableGpuKernelTiming", "GetGpuKernelTimes",
            "GetGpuGhostMap", "RunGpuResidualNoAlloc", "BiofemNewtonDefaults", "RunGpuNewtonSolve",
            "RunGpuNewtonSolveDevice", "PrepareGpuMeshOnStream", "ServeCreate", "ServeSubmit", "ServeWait",
-           "ServeStatsGet", "ServeDestroy", "BiofemServeEstimateBytes"]
+           "ServeStatsGet", "ServeDestroy", "BiofemServeEstimateBytes", "GetGpuBasisTablesKind"]
 
 
 def load_library(path: Path | str | None = None) -> ctypes.CDLL:
@@ -124,6 +127,7 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
     lib.GetGpuBasisTables.argtypes = [vp]
     lib.EnableGpuKernelTiming.argtypes = [vp, ctypes.c_int]
     lib.GetGpuKernelTimes.argtypes = [vp, vp, ctypes.c_int32, vp]
+    lib.GetGpuBasisTablesKind.argtypes = [ctypes.c_int32, vp]
     lib.ServeCreate.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(vp)]
     lib.ServeSubmit.argtypes = [vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(NewtonOptions),
                                 vp, ctypes.POINTER(ctypes.c_int64)]
@@ -172,7 +176,8 @@ class GpuShell:
                              a["nb"].ctypes.data_as(_i32p), a["bn"].ctypes.data_as(_i32p),
                              a["fib"].ctypes.data_as(_f64p), a["gs"].ctypes.data_as(_f64p))
         self.params = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure,
-                             clamp_edge, precision)
+                             clamp_edge, precision, getattr(workload, "basis", BIOFEM_BASIS_REFERENCE),
+                             getattr(workload, "tnormal", 0))
         self.host_only = host_only
         h = ctypes.c_void_p()
         fn = self.lib.BuildHostMesh if host_only else self.lib.PrepareGpuMesh
@@ -352,7 +357,8 @@ class Serve:
 
     def submit(self, mesh, workload, mu, bulk, h0, x0, gamma=1.0, clamp_edge=0, precision=BIOFEM_FP64, **newton):
         d, keep = mesh_desc(mesh)
-        prm = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure, clamp_edge, precision)
+        prm = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure, clamp_edge, precision,
+                     getattr(workload, "basis", BIOFEM_BASIS_REFERENCE), getattr(workload, "tnormal", 0))
         o = NewtonOptions()
         self.lib.BiofemNewtonDefaults(ctypes.byref(o))
         for k, v in newton.items():

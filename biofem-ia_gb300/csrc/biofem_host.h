@@ -34,6 +34,7 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err);
 /* Parameters every element kernel needs (passed by value). */
 struct KParams {
   int ne, nt, nv, ng, nq, iters;
+  int tnormal;               /* thickness metric from the tangential part of a3,alpha */
   double mu, K, hhalf;
   double theta[kMaxQp], w[kMaxQp];
   double pressure;
@@ -102,7 +103,7 @@ struct AmgHier;
 int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, double *dR, double *x,
                   const BiofemNewtonOptions &o, BiofemNewtonStats &s, SolverWork *w, AmgHier *amg, cudaStream_t st,
                   ResidualFn residual, JacobianFn jacobian, void *ctx, std::string &err);
-void host_tables(double *out);   /* kNumTables*5*16 host copy of the basis tables */
+void host_tables(double *out, int basis);   /* kNumTables*5*16 host copy of the basis tables */
 
 } /* namespace biofem */
 

@@ -87,12 +87,19 @@ static void subpatch_rows(int v, int rows[12])
   for (int i = 0; i < 12; i++) rows[i] = r[i];
 }
 
-void host_tables(double *out)
+/* basis BIOFEM_BASIS_REFERENCE: the four-decimal constants above;
+   BIOFEM_BASIS_EXACT: the rationals they round (k/324 for the first
+   derivatives, k/108 for the second), whose rows sum to zero, so that a flat
+   uniform patch has exactly zero second derivatives.  The irregular tables
+   are built from whichever regular table is chosen. */
+void host_tables(double *out, int basis)
 {
   std::fill(out, out + kNumTables * 80, 0.0);
   for (int i = 0; i < 12; i++) {
-    out[0 * 16 + i] = kNaC[0][i]; out[1 * 16 + i] = kNaC[1][i];
-    out[2 * 16 + i] = kNabC[0][i]; out[3 * 16 + i] = kNabC[1][i]; out[4 * 16 + i] = kNabC[2][i];
+    for (int r = 0; r < 2; r++)
+      out[r * 16 + i] = basis ? std::nearbyint(kNaC[r][i] * 324.0) / 324.0 : kNaC[r][i];
+    for (int r = 0; r < 3; r++)
+      out[(2 + r) * 16 + i] = basis ? std::nearbyint(kNabC[r][i] * 108.0) / 108.0 : kNabC[r][i];
   }
   const double pi = 3.14159265358979323846264338327950288419716939937510582;
   for (int v = 3; v < kNumTables; v++) {
@@ -110,7 +117,7 @@ void host_tables(double *out)
     }
     int rows[12];
     subpatch_rows(v, rows);
-    const double *Nrow[5] = {kNaC[0], kNaC[1], kNabC[0], kNabC[1], kNabC[2]};
+    const double *Nrow[5] = {out, out + 16, out + 32, out + 48, out + 64};   /* the chosen regular table */
     const double scale[5] = {-2.0, -2.0, 4.0, 4.0, 4.0};
     for (int rr = 0; rr < 5; rr++)
       for (int j = 0; j < nen; j++) {
@@ -390,6 +397,8 @@ static int check_params(const BiofemParams &p)
   if (p.c33_subitr_nums < 1) return fail(62, "C33_subitr_nums must be >= 1");
   if (!(p.h0 > 0.0)) return fail(62, "h0 must be positive");
   if (p.precision != BIOFEM_FP64 && p.precision != BIOFEM_FP32_BULK) return fail(62, "unknown precision");
+  if (p.basis != BIOFEM_BASIS_REFERENCE && p.basis != BIOFEM_BASIS_EXACT) return fail(62, "unknown basis tables");
+  if (p.thickness_normal != 0 && p.thickness_normal != 1) return fail(62, "thickness_normal must be 0 or 1");
   return 0;
 }
 
@@ -494,6 +503,7 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
 
   KParams &kp = m->kp;
   kp.ne = ne; kp.nt = nt; kp.nv = nv; kp.ng = ng; kp.nq = params->n_qp; kp.iters = params->c33_subitr_nums;
+  kp.tnormal = params->thickness_normal;
   kp.mu = params->mu; kp.K = params->bulk_modulus; kp.hhalf = 0.5 * params->h0;
   kp.pressure = params->pressure; kp.gamma = params->gamma;
   gauss(params->n_qp, kp.theta, kp.w);
@@ -505,7 +515,7 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   for (int g = 0; g < ng; g++) { ghost3[3 * g] = T.ghost_nv1[g]; ghost3[3 * g + 1] = T.ghost_nv2[g]; ghost3[3 * g + 2] = T.ghost_nv3[g]; }
   std::vector<int> etri(T.tri_all.begin(), T.tri_all.begin() + 3 * (size_t)ne);
   std::vector<double> tabs(kNumTables * 80);
-  host_tables(tabs.data());
+  host_tables(tabs.data(), params->basis);
   std::vector<float> tabsF(kNumTables * 85);
   for (int i = 0; i < kNumTables * 80; i++) tabsF[i] = (float)tabs[i];
   for (int i = 0; i < kNumTables * 5; i++) {
@@ -841,7 +851,15 @@ int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *op
 int GetGpuBasisTables(double *out)
 {
   if (!out) return fail(85, "null argument");
-  host_tables(out);
+  host_tables(out, BIOFEM_BASIS_REFERENCE);
+  return 0;
+}
+
+int GetGpuBasisTablesKind(int32_t basis, double *out)
+{
+  if (!out) return fail(85, "null argument");
+  if (basis != BIOFEM_BASIS_REFERENCE && basis != BIOFEM_BASIS_EXACT) return fail(63, "unknown basis tables");
+  host_tables(out, basis);
   return 0;
 }
 

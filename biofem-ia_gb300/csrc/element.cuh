@@ -99,13 +99,14 @@ template <class R> struct EPar {
   R mu, K, hhalf;
   R theta[kMaxQp], w[kMaxQp];
   int nq, iters;
+  int tnormal;   /* 1: thickness metric from the tangential part of a3,alpha (extension) */
 };
 
 template <class R> __host__ __device__ __forceinline__ EPar<R> epar(const KParams &p);
 template <> __host__ __device__ __forceinline__ EPar<double> epar<double>(const KParams &p)
 {
   EPar<double> e;
-  e.mu = p.mu; e.K = p.K; e.hhalf = p.hhalf; e.nq = p.nq; e.iters = p.iters;
+  e.mu = p.mu; e.K = p.K; e.hhalf = p.hhalf; e.nq = p.nq; e.iters = p.iters; e.tnormal = p.tnormal;
   for (int q = 0; q < kMaxQp; q++) { e.theta[q] = p.theta[q]; e.w[q] = p.w[q]; }
   return e;
 }
@@ -113,7 +114,7 @@ template <> __host__ __device__ __forceinline__ EPar<double> epar<double>(const 
 template <> __host__ __device__ __forceinline__ EPar<float> epar<float>(const KParams &p)
 {
   EPar<float> e;
-  e.mu = p.muf; e.K = p.Kf; e.hhalf = p.hhalff; e.nq = p.nq; e.iters = p.iters;
+  e.mu = p.muf; e.K = p.Kf; e.hhalf = p.hhalff; e.nq = p.nq; e.iters = p.iters; e.tnormal = p.tnormal;
   for (int q = 0; q < kMaxQp; q++) { e.theta[q] = p.thetaf[q]; e.w[q] = p.wf[q]; }
   return e;
 }
@@ -216,8 +217,12 @@ __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R
   const V3<T> gc1 = scl(one / dot(a1, t1), t1);
   const V3<T> t2 = cross(n, a1);
   const V3<T> gc2 = scl(one / dot(a2, t2), t2);
-  const V3<T> a31 = scl(icn, cross(Aaa, a2) + cross(a1, Aab));
-  const V3<T> a32 = scl(icn, cross(Aab, a2) + cross(a1, Abb));
+  V3<T> a31 = scl(icn, cross(Aaa, a2) + cross(a1, Aab));
+  V3<T> a32 = scl(icn, cross(Aab, a2) + cross(a1, Abb));
+  if (p.tnormal) {   /* n_,alpha: drop the J_,alpha / J n part of the unnormalised derivative */
+    a31 = a31 - scl(dot(a31, n), n);
+    a32 = a32 - scl(dot(a32, n), n);
+  }
 
   const int nq = p.nq;
   const R gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];

@@ -127,6 +127,10 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
   V3<double> a31 = cross(Aaa, a2) + cross(a1, Aab), a32 = cross(Aab, a2) + cross(a1, Abb);
   a31 = {a31.x / cn, a31.y / cn, a31.z / cn};
   a32 = {a32.x / cn, a32.y / cn, a32.z / cn};
+  if (p.tnormal) {
+    a31 = a31 - scl(dot(a31, n), n);
+    a32 = a32 - scl(dot(a32, n), n);
+  }
   const V3<double> f = {fib[3 * (size_t)e], fib[3 * (size_t)e + 1], fib[3 * (size_t)e + 2]};
   const double gam = p.gamma * gscale[e];
   const double phi = dot(f, f);

@@ -57,9 +57,22 @@ typedef struct {
   double  pressure;            /* follower normal pressure P (external.c:589), 0 = none */
   int32_t clamp_edge;          /* ring clamped in x,y,z by EdgeDirectionalFix (external.c:1706); -1 = none */
   int32_t precision;           /* BIOFEM_FP64 or BIOFEM_FP32_BULK */
+  int32_t basis;               /* BIOFEM_BASIS_REFERENCE (default) or BIOFEM_BASIS_EXACT */
+  int32_t thickness_normal;    /* 0 (reference): g_alpha = a_alpha + theta3 a3,alpha with a3,alpha the derivative of
+                                  a1 x a2 over |a1 x a2| (active_strain.c:745-762, 896-982); 1 (extension): its
+                                  tangential part n,alpha only.  The two agree where |a1 x a2| is uniform; on
+                                  non-uniform patches (ghost-reflected boundary patches of a fine mesh) the
+                                  normal part J,alpha/J n folds the thickness points once h << h0 */
 } BiofemParams;
 
 enum { BIOFEM_FP64 = 0, BIOFEM_FP32_BULK = 1 };
+/* Centroid basis-derivative tables.  REFERENCE: the four-decimal values of
+   active_strain.c:69-88 (parity with the reference).  EXACT (extension): the
+   rationals they round; the four-decimal second-derivative rows sum to
+   -1e-4, -1e-4, 2e-4 instead of 0, so a flat sheet acquires a curvature
+   ~1e-4 |x| / h^2 at the thickness points, which folds them once the mesh
+   is much finer than the shell (h below ~h0/4). */
+enum { BIOFEM_BASIS_REFERENCE = 0, BIOFEM_BASIS_EXACT = 1 };
 
 typedef struct {
   int32_t n_v, n_ghosts, n_elmt, n_dof;
@@ -226,6 +239,8 @@ int DestroyHostMesh(BiofemGpuMesh *m);
    (table 0 = regular patch, active_strain.c:69-88; table v = the one-step
    subdivision weights of valence v, active_strain.c:594-666). */
 int GetGpuBasisTables(double *out);
+/* The same for either table kind. */
+int GetGpuBasisTablesKind(int32_t basis, double *out);
 
 const char *BiofemGpuLastError(void);
 

@@ -118,13 +118,29 @@ template <class G, class T> inline void RaiseIndices2(const G g[3][3], const T a
 /* ---------------- element tables ---------------- */
 /* Centroid derivatives of the 12 regular box-spline basis functions,
    four-decimal values as tabulated in active_strain.c:69-88. */
-static const double kNa[2][12] = {
+static const double kNaRef[2][12] = {
   {-0.0247, -0.0309, 0.0000, -0.4815, -0.1852, 0.0247, 0.4815, 0.0000, -0.0062, 0.0309, 0.1852, 0.0062},
   {-0.0309, -0.0247, -0.1852, -0.4815, 0.0000, -0.0062, 0.0000, 0.4815, 0.0247, 0.0062, 0.1852, 0.0309}};
-static const double kNab[3][12] = {
+static const double kNabRef[3][12] = {
   {0.1111, 0.2222, -0.2222, -0.2222, 0.4444, 0.1111, -0.2222, -0.8889, 0.0000, 0.2222, 0.4444, 0.0000},
   {0.2222, 0.1111, 0.4444, -0.2222, -0.2222, 0.0000, -0.8889, -0.2222, 0.1111, 0.0000, 0.4444, 0.2222},
   {0.1667, 0.1667, -0.1111, 0.2222, -0.1111, -0.0556, -0.4444, -0.4444, -0.0556, 0.0556, 0.5556, 0.0556}};
+
+/* Active tables: the reference's four-decimal values (default), or, as an
+   extension for meshes much finer than the shell thickness, the exact
+   rationals they round (first derivatives k/324, second derivatives k/108,
+   rows summing to zero).  Set by oracle_set_basis before oracle_setup. */
+static double kNa[2][12], kNab[3][12];
+static int set_basis_tables(int kind)
+{
+  if (kind != 0 && kind != 1) return 63;
+  for (int r = 0; r < 2; r++) for (int i = 0; i < 12; i++)
+    kNa[r][i] = kind ? std::nearbyint(kNaRef[r][i] * 324.0) / 324.0 : kNaRef[r][i];
+  for (int r = 0; r < 3; r++) for (int i = 0; i < 12; i++)
+    kNab[r][i] = kind ? std::nearbyint(kNabRef[r][i] * 108.0) / 108.0 : kNabRef[r][i];
+  return 0;
+}
+static const int g_tables_init = set_basis_tables(0);
 
 /* Gauss-Legendre points/weights on [-1,1] (active_strain.c:174-230 for n = 1..5;
    n = 6 is an extension of this build, the reference stops at 5). */
@@ -427,6 +443,11 @@ static int elem_geom(const Mesh &m, int ec, const T *xb, const T *yb, const T *z
   return 0;
 }
 
+/* 1: the thickness metric uses the tangential part of a3,alpha (n,alpha), an
+   extension; 0: the reference's unnormalised derivative.  Set by
+   oracle_set_thickness_normal before oracle_setup. */
+static int g_tnormal = 0;
+
 /* Compute_a3_alpha_, active_strain.c:745-762 */
 template <class T>
 static void a3_alpha(const Geom<T> &G, V3<T> &a31, V3<T> &a32)
@@ -436,6 +457,11 @@ static void a3_alpha(const Geom<T> &G, V3<T> &a31, V3<T> &a32)
   a32 = PLUS(CROSS(G.Aab, G.a2), CROSS(G.a1, G.Abb));
   a31.x /= s; a31.y /= s; a31.z /= s;
   a32.x /= s; a32.y /= s; a32.z /= s;
+  if (g_tnormal) {
+    const T d1 = DOT(a31, G.n), d2 = DOT(a32, G.n);
+    a31 = MINUS(a31, AMULT(d1, G.n));
+    a32 = MINUS(a32, AMULT(d2, G.n));
+  }
 }
 
 template <class T> inline void metric(const V3<T> g[3], T gm[3][3])
@@ -958,6 +984,15 @@ int oracle_elem_state(const double *x, int ec, double *S, double *C33, double *g
 }
 
 /* IN arrays of the one-step subdivision for valence v (5 x (v+6), row major). */
+int oracle_set_basis(int kind) { (void)g_tables_init; return set_basis_tables(kind); }
+
+int oracle_set_thickness_normal(int on)
+{
+  if (on != 0 && on != 1) return 63;
+  g_tnormal = on;
+  return 0;
+}
+
 int oracle_irregular_weights(int v, double *out)
 {
   const int nen = v + 6;

@@ -41,6 +41,21 @@ class _Base:
     def _fn(self, name):
         return getattr(self.lib, f"{self.prefix}_{name}")
 
+    def _select_basis(self, kind: int, tnormal: int = 0):
+        """Basis-derivative tables (0 the reference's four-decimal values, 1 the
+        exact rationals) and thickness metric (0 the reference's a3,alpha, 1
+        its tangential part): extensions only the restated oracle has."""
+        for name, val in (("set_basis", kind), ("set_thickness_normal", tnormal)):
+            fn = getattr(self.lib, f"{self.prefix}_{name}", None)
+            if fn is None:
+                if val:
+                    raise RuntimeError(f"the reference build has no {name} extension")
+                continue
+            fn.argtypes = [_c_int]
+            rc = fn(int(val))
+            if rc:
+                raise RuntimeError(f"{self.prefix}_{name} failed with code {rc}")
+
     def setup(self, mesh, w, mu: float, bulk: float, h0: float, gamma: float = 1.0, clamp: bool = True):
         from_mesh = dict(
             tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),
@@ -51,6 +66,7 @@ class _Base:
             gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64),
         )
         self._keep = from_mesh
+        self._select_basis(getattr(w, "basis", 0), getattr(w, "tnormal", 0))
         f = self._fn("setup")
         f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp,
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
@@ -104,6 +120,7 @@ class Oracle(_Base):
                     fib=np.ascontiguousarray(mesh.fib, dtype=np.float64),
                     gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64))
         self._keep = keep
+        self._select_basis(getattr(w, "basis", 0), getattr(w, "tnormal", 0))
         f = self.lib.oracle_setup_given_topology
         f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]

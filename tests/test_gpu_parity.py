@@ -68,7 +68,10 @@ def test_residual_is_deterministic():
 @pytest.mark.parametrize("wl", [configs.small(8, 6, index=40), configs.small(9, 7, activation="random", index=41, n_qp=4, c33_iters=2),
                                 configs.small(12, 8, activation="uniform", lambda_a=0.85, index=42, pressure=1e-3, n_qp=5, c33_iters=1),
                                 configs.small(10, 8, activation="random", index=44, n_qp=6, pressure=1e-4),
-                                configs.C1], ids=lambda w: w.name)
+                                configs.small(11, 8, activation="random", index=45, n_qp=6, basis=1),
+                                configs.small(12, 9, index=46, basis=1, tnormal=1, pressure=1e-3),
+                                configs.C1],
+                         ids=lambda w: w.name + ("_exact" if w.basis else "") + ("_tnormal" if w.tnormal else ""))
 def test_tangent_matches_oracle_directional_derivative(wl, oracle_lib):
     m = wl.build_mesh()
     o = oracle_lib.setup(m, wl, configs.MU, configs.BULK, configs.H0)
