@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--workload", default="C2_flat_256x192")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the Newton and serving measurements")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 1024x768 (C3) measurement")
     ap.add_argument("--serve-requests", type=int, default=128)
     return ap.parse_args()
 
@@ -166,6 +167,66 @@ def newton_bench(reps=3):
                                       "gmres_its": st["gmres_its_total"], "converged": st["converged"],
                                       "rel_residual": st["rfinal"] / st["r0"]}
             sh.close()
+    return out
+
+
+def c3_bench(steps=5, warmup=2):
+    """C3: 1024x768 cells (1,572,864 triangles), 6 thickness points, random
+    fibre angle and lambda_a, exact basis tables and tangential thickness
+    metric (extensions that keep this resolution well posed).  R+K time of
+    the FP64 and FP32-bulk forms (device pointers, L2 flushed between steps),
+    a warm Newton load step with each, and their agreement."""
+    import torch
+    from biofem import configs
+    from biofem.gpu import GpuShell, BIOFEM_FP64, BIOFEM_FP32_BULK
+    w = configs.C3
+    m = w.build_mesh()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    out, keep = {}, {}
+    for prec, tag, kt in ((BIOFEM_FP64, "fp64", torch.float64), (BIOFEM_FP32_BULK, "fp32_bulk", torch.float32)):
+        t0 = time.perf_counter()
+        sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=prec)
+        prep = time.perf_counter() - t0
+        x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+        dx = torch.tensor(x0, device=dev)
+        dR = torch.empty_like(dx)
+        dK = torch.empty(9 * sh.nnzb, dtype=kt, device=dev)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = []
+        with torch.cuda.stream(stream):
+            for i in range(warmup + steps):
+                flush.zero_()
+                ev0.record(stream)
+                sh.jacobian_device(dx.data_ptr(), dR.data_ptr(), dK.data_ptr(), sp)
+                ev1.record(stream)
+                ev1.synchronize()
+                if i >= warmup:
+                    ms.append(ev0.elapsed_time(ev1))
+            sh.sync(sp)
+        best = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            x, st = sh.newton(x0, rtol=1e-10)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        out[tag] = {"rk_ms": min(ms), "rk_elems_per_s": m.n_elmt / (min(ms) * 1e-3), "prep_s": prep,
+                    "newton_ms": best * 1e3, "newton_its": st["newton_its"], "gmres_its": st["gmres_its_total"],
+                    "converged": st["converged"], "rel_residual": st["rfinal"] / st["r0"]}
+        keep[tag] = (dK.double() if kt == torch.float32 else dK, dR.clone(), torch.tensor(x - x0, device=dev))
+        sh.close()
+        del dx, dR, dK
+    K64, R64, u64 = keep["fp64"]
+    K32, R32, u32 = keep["fp32_bulk"]
+    out["K_frobenius_rel_err_fp32_vs_fp64"] = float(torch.linalg.norm(K32 - K64) / torch.linalg.norm(K64))
+    out["R_bit_identical"] = bool(torch.equal(R32, R64))
+    out["displacement_rel_err_fp32_vs_fp64"] = float(torch.linalg.norm(u32 - u64) / torch.linalg.norm(u64))
+    out["workload"] = (f"{w.name}: {m.n_elmt} triangles, {m.n_v} nodes, q={w.n_qp}, random fibre angle and "
+                       f"lambda_a, exact basis tables + tangential thickness metric")
+    del keep, K64, K32
+    torch.cuda.empty_cache()
     return out
 
 
@@ -428,6 +489,7 @@ def run_ours(args):
         return
 
     newton = newton_bench() if not args.no_solve else None
+    c3 = c3_bench() if not args.no_c3 else None
     serving = serve_bench(n_req=args.serve_requests) if not args.no_solve else None
 
     info = sh.info
@@ -485,6 +547,8 @@ def run_ours(args):
         line["newton_load_step"] = newton
     if serving:
         line["serving"] = serving
+    if c3:
+        line["C3"] = c3
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
