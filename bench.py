@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--workload", default="C2_flat_256x192")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the Newton and serving measurements")
-    ap.add_argument("--no-c3", action="store_true", help="skip the 1024x768 (C3) measurement")
+    ap.add_argument("--no-c3", action="store_true", help="skip the C3 (1024x768) and C4 (ellipsoid) measurements")
     ap.add_argument("--serve-requests", type=int, default=128)
     return ap.parse_args()
 
@@ -170,16 +170,18 @@ def newton_bench(reps=3):
     return out
 
 
-def c3_bench(steps=5, warmup=2):
-    """C3: 1024x768 cells (1,572,864 triangles), 6 thickness points, random
-    fibre angle and lambda_a, exact basis tables and tangential thickness
-    metric (extensions that keep this resolution well posed).  R+K time of
-    the FP64 and FP32-bulk forms (device pointers, L2 flushed between steps),
-    a warm Newton load step with each, and their agreement."""
+def case_bench(w, steps=5, warmup=2):
+    """One large workload: R+K time of the FP64 and FP32-bulk forms (device
+    pointers, L2 flushed between steps), a warm Newton load step with each,
+    and their agreement (K Frobenius error, residual identity, displacement).
+    C3: 1024x768 cells, 1,572,864 triangles, 6 thickness points, random fibre
+    angle and lambda_a, exact basis tables and tangential thickness metric
+    (extensions that keep this resolution well posed).  C4: the ~200k-triangle
+    truncated ellipsoid with isolated valence-5/7 vertices, helix fibres,
+    internal pressure, reference tables."""
     import torch
     from biofem import configs
     from biofem.gpu import GpuShell, BIOFEM_FP64, BIOFEM_FP32_BULK
-    w = configs.C3
     m = w.build_mesh()
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.Stream(device=dev)
@@ -190,6 +192,7 @@ def c3_bench(steps=5, warmup=2):
         t0 = time.perf_counter()
         sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=prec)
         prep = time.perf_counter() - t0
+        n_irregular = int(sh.info.n_irregular)
         x0 = w.initial_x(m, sh.topology()["xyz0_full"])
         dx = torch.tensor(x0, device=dev)
         dR = torch.empty_like(dx)
@@ -209,7 +212,7 @@ def c3_bench(steps=5, warmup=2):
         best = None
         for _ in range(2):
             t0 = time.perf_counter()
-            x, st = sh.newton(x0, rtol=1e-10)
+            x, st = sh.newton(x0, rtol=1e-10, max_newton=12, gmres_max_it=1000)
             dt = time.perf_counter() - t0
             best = dt if best is None else min(best, dt)
         out[tag] = {"rk_ms": min(ms), "rk_elems_per_s": m.n_elmt / (min(ms) * 1e-3), "prep_s": prep,
@@ -223,8 +226,10 @@ def c3_bench(steps=5, warmup=2):
     out["K_frobenius_rel_err_fp32_vs_fp64"] = float(torch.linalg.norm(K32 - K64) / torch.linalg.norm(K64))
     out["R_bit_identical"] = bool(torch.equal(R32, R64))
     out["displacement_rel_err_fp32_vs_fp64"] = float(torch.linalg.norm(u32 - u64) / torch.linalg.norm(u64))
-    out["workload"] = (f"{w.name}: {m.n_elmt} triangles, {m.n_v} nodes, q={w.n_qp}, random fibre angle and "
-                       f"lambda_a, exact basis tables + tangential thickness metric")
+    out["workload"] = (f"{w.name}: {m.n_elmt} triangles, {m.n_v} nodes, {m.n_ghosts} ghosts, q={w.n_qp}, "
+                       f"basis tables {'exact' if w.basis else 'reference'}, thickness metric "
+                       f"{'n,alpha' if w.tnormal else 'reference'}")
+    out["irregular_elements"] = n_irregular
     del keep, K64, K32
     torch.cuda.empty_cache()
     return out
@@ -489,7 +494,9 @@ def run_ours(args):
         return
 
     newton = newton_bench() if not args.no_solve else None
-    c3 = c3_bench() if not args.no_c3 else None
+    from biofem import configs as _cfg
+    c3 = case_bench(_cfg.C3) if not args.no_c3 else None
+    c4 = case_bench(_cfg.C4) if not args.no_c3 else None
     serving = serve_bench(n_req=args.serve_requests) if not args.no_solve else None
 
     info = sh.info
@@ -549,6 +556,8 @@ def run_ours(args):
         line["serving"] = serving
     if c3:
         line["C3"] = c3
+    if c4:
+        line["C4"] = c4
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

@@ -76,7 +76,42 @@ C2 = Workload("C2_flat_256x192", 256, 192, activation="smooth", disp_rel=1e-2, i
 # them on the ghost-reflected side patches, so C3 uses the exact tables and n,alpha.
 C3 = Workload("C3_flat_1024x768", 1024, 768, n_qp=6, activation="random", index=2, basis=1, tnormal=1)
 
-ALL = {w.name: w for w in (C1, C2, C3)}
+@dataclass(frozen=True)
+class LVWorkload:
+    """Truncated prolate spheroid shell (the LV loader's geometry), see
+    mesh.lv_ellipsoid: semi-axes (1, 1, 2), cut at z = 0.5, helix -60 deg at
+    the base to +60 deg at the apex, lambda_a uniform, internal follower
+    pressure, base ring clamped, starting from the reference state."""
+    name: str
+    freq: int
+    index: int = 0
+    n_qp: int = 3
+    c33_iters: int = 3
+    pressure: float = 1e-3
+    lambda_a: float = 0.88
+    nflip: int = 4
+    jitter: float = 0.1
+    basis: int = 0
+    tnormal: int = 0
+
+    @property
+    def seed(self) -> int:
+        return meshmod.SEED_BASE + self.index
+
+    def build_mesh(self) -> meshmod.Mesh:
+        m = meshmod.lv_ellipsoid(self.freq, self.seed, nflip=self.nflip, jitter=self.jitter, lambda_a=self.lambda_a)
+        m.meta["workload"] = self.name
+        return m
+
+    def initial_x(self, m: meshmod.Mesh, xyz0_full: np.ndarray) -> np.ndarray:
+        return meshmod.initial_state(m, xyz0_full)
+
+
+# C4: ~200k triangles (frequency-41 geodesic cap: 200,614 triangles, 100,761 nodes, 20
+# extraordinary interior vertices of valence 5/7, a jagged cut rim of boundary valence 5/6/7).
+C4 = LVWorkload("C4_lv_ellipsoid", 41, index=3)
+
+ALL = {w.name: w for w in (C1, C2, C3, C4)}
 
 
 def small(nx: int, ny: int, **kw) -> Workload:

@@ -203,3 +203,202 @@ def read_input_files(in_dir: str | Path, ibi: int = 0) -> Mesh:
     fib[:, 0] = 1.0
     return Mesh(xyz0=xyz0, tri=tri, n_bnodes=n_bnodes, bnodes=bnodes, fib=fib,
                 gamma_scale=np.zeros(n_e), meta=dict(kind="file", path=str(d)))
+
+
+# ---- truncated ellipsoid shell (C4; the LV loader's geometry, lv_geometry_unstructured.c) ----
+def _icosahedron():
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    V = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+                  (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], dtype=float)
+    F = np.array([(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+                  (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+                  (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)], dtype=np.int64)
+    return V / np.linalg.norm(V, axis=1)[:, None], F
+
+
+def _orient_outward(V, F):
+    c = V[F].mean(1)
+    n = np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]])
+    flip = (n * c).sum(1) < 0
+    F = F.copy()
+    F[flip] = F[flip][:, [0, 2, 1]]
+    return F
+
+
+def _midpoint_refine(V, F):
+    key = {}
+    Vl = list(V)
+    def mid(a, b):
+        k = (min(a, b), max(a, b))
+        if k not in key:
+            p = V[a] + V[b]
+            key[k] = len(Vl)
+            Vl.append(p / np.linalg.norm(p))
+        return key[k]
+    out = []
+    for a, b, c in F:
+        ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+        out += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+    return np.array(Vl), np.array(out, dtype=np.int64)
+
+
+def _flip_edges(V, F, nflip, rng, zmin):
+    """Flip nflip edges of the base sphere whose two ends and two opposite
+    corners all have valence 6 (ends become 5, opposite corners 7), each
+    vertex used once, all four corners above zmin."""
+    F = [list(f) for f in F]
+    used = set()
+    done = 0
+    for _ in range(2000):
+        if done == nflip:
+            break
+        val = np.bincount(np.array(F).ravel(), minlength=len(V))
+        fi = int(rng.integers(len(F)))
+        k = int(rng.integers(3))
+        a, b = F[fi][k], F[fi][(k + 1) % 3]
+        c = F[fi][(k + 2) % 3]
+        fj = [j for j, f in enumerate(F) if j != fi and a in f and b in f]
+        if len(fj) != 1:
+            continue
+        fj = fj[0]
+        d = [v for v in F[fj] if v not in (a, b)][0]
+        quad = (a, b, c, d)
+        if any(v in used for v in quad) or any(val[v] != 6 for v in quad) or any(V[v, 2] < zmin for v in quad):
+            continue
+        F[fi] = [c, a, d]
+        F[fj] = [d, b, c]
+        used.update(quad)
+        done += 1
+    return np.array(F, dtype=np.int64)
+
+
+def _geodesic(V, F, n):
+    """Frequency-n subdivision of every base face, points pushed to the unit
+    sphere; base vertices keep their valence, all new vertices get 6."""
+    key, pts, tris = {}, [], []
+    def vid(f, i, j):
+        a, b, c = F[f]
+        if i == 0 and j == 0:
+            k = ("v", a)
+        elif i == n and j == 0:
+            k = ("v", b)
+        elif i == 0 and j == n:
+            k = ("v", c)
+        elif j == 0:
+            k = ("e", a, b, i) if a < b else ("e", b, a, n - i)
+        elif i == 0:
+            k = ("e", a, c, j) if a < c else ("e", c, a, n - j)
+        elif i + j == n:
+            k = ("e", b, c, j) if b < c else ("e", c, b, i)
+        else:
+            k = ("f", f, i, j)
+        if k not in key:
+            p = V[a] + (V[b] - V[a]) * (i / n) + (V[c] - V[a]) * (j / n)
+            key[k] = len(pts)
+            pts.append(p / np.linalg.norm(p))
+        return key[k]
+    for f in range(len(F)):
+        for j in range(n):
+            for i in range(n - j):
+                tris.append((vid(f, i, j), vid(f, i + 1, j), vid(f, i, j + 1)))
+                if i + j < n - 1:
+                    tris.append((vid(f, i + 1, j), vid(f, i + 1, j + 1), vid(f, i, j + 1)))
+    return np.array(pts), np.array(tris, dtype=np.int64)
+
+
+def _clean_cap(F):
+    """Drop triangles until the cut boundary is one simple ring: no pinched
+    boundary vertex and no triangle with two boundary edges."""
+    while True:
+        e = np.sort(np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1)
+        u, inv, cnt = np.unique(e, axis=0, return_inverse=True, return_counts=True)
+        bmask = (cnt == 1)[inv.ravel()].reshape(3, -1).T          # (nf, 3) edge is on the boundary
+        nbe = np.bincount(u[cnt == 1].ravel(), minlength=F.max() + 1)
+        pinch = np.where(nbe > 2)[0]
+        drop = bmask.sum(1) >= 2
+        if len(pinch):
+            drop |= np.isin(F, pinch).any(1)
+        if not drop.any():
+            return F
+        F = F[~drop]
+
+
+def lv_ellipsoid(freq: int, seed: int, a: float = 2.0, b: float = 1.0, f_cut: float = 0.375, nflip: int = 4,
+                 jitter: float = 0.1, alpha_apex: float = 60.0, alpha_base: float = -60.0,
+                 lambda_a: float = 0.88) -> Mesh:
+    """Truncated prolate spheroid shell x^2/b^2 + y^2/b^2 + z^2/a^2 = 1 kept
+    for z >= a (1 - 2 f_cut) (the LV options -lv_a, -lv_b, -lv_f_cut), apex at
+    z = +a, outward-oriented triangles, the cut rim as the one boundary ring.
+
+    Mesh: the icosahedron refined twice by edge midpoints, nflip seeded edge
+    flips above the cut (valence 5/7 pairs), then a frequency-`freq` geodesic
+    subdivision, so the extraordinary vertices stay isolated; interior nodes get a seeded
+    tangential jitter of `jitter` x the node's shortest edge, pulled back to the
+    surface.  Fibres: the mid-wall helix of lv_geometry_unstructured.c:296-366
+    with the latitude sweep: e_n = unit grad F at the element centroid, e_l =
+    the projection of -e_z, e_c = e_n x e_l, alpha = (1 - z*) alpha_apex +
+    z* alpha_base with z* = (a - c_z) / (a - z_base); activation lambda_a on
+    every element (tapers off).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    V, F = _icosahedron()
+    V, F = _midpoint_refine(V, _orient_outward(V, F))
+    V, F = _midpoint_refine(V, _orient_outward(V, F))
+    z_base = a * (1.0 - 2.0 * f_cut)
+    F = _orient_outward(V, _flip_edges(V, _orient_outward(V, F), nflip, rng, z_base / a + 0.15))
+    V, F = _geodesic(V, F, freq)
+    F = _orient_outward(V, F)
+    V = V * np.array([b, b, a])
+    keep = V[:, 2] >= z_base
+    F = F[keep[F].all(1)]
+    F = _clean_cap(F)
+    used = np.unique(F)
+    remap = -np.ones(len(V), dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    V, F = V[used], remap[F]
+    # boundary ring, following the triangles' edge directions
+    he = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+    s = set(map(tuple, he))
+    bhe = [h for h in map(tuple, he) if (h[1], h[0]) not in s]
+    nxt = dict(bhe)
+    start = min(nxt)
+    ring = [start]
+    while nxt[ring[-1]] != start:
+        ring.append(nxt[ring[-1]])
+    if len(ring) != len(bhe):
+        raise RuntimeError("the cut boundary is not a single ring")
+    ring = np.array(ring, dtype=np.int32)
+    # tangential jitter of interior nodes, scaled by each node's shortest edge
+    e = np.sort(np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1)
+    elen = np.linalg.norm(V[e[:, 0]] - V[e[:, 1]], axis=1)
+    hmean = elen.mean()
+    hmin = np.full(len(V), np.inf)
+    np.minimum.at(hmin, e[:, 0], elen)
+    np.minimum.at(hmin, e[:, 1], elen)
+    interior = np.ones(len(V), bool)
+    interior[ring] = False
+    grad = V / np.array([b * b, b * b, a * a])
+    nrm = grad / np.linalg.norm(grad, axis=1)[:, None]
+    d = rng.uniform(-1.0, 1.0, size=V.shape) * (jitter * hmin)[:, None]
+    d -= (d * nrm).sum(1)[:, None] * nrm
+    W = V + np.where(interior[:, None], d, 0.0)
+    s_ = np.sqrt((W[:, 0] / b) ** 2 + (W[:, 1] / b) ** 2 + (W[:, 2] / a) ** 2)
+    V = np.where(interior[:, None], W / s_[:, None], V)
+    # fibres (mid-wall helix, latitude sweep) and activation
+    c = V[F].mean(1)
+    en = c / np.array([b * b, b * b, a * a])
+    en /= np.linalg.norm(en, axis=1)[:, None]
+    down = np.array([0.0, 0.0, -1.0])
+    el = down[None, :] - (en @ down)[:, None] * en
+    small = np.linalg.norm(el, axis=1) <= 1e-10
+    ex = np.array([1.0, 0.0, 0.0])
+    el[small] = ex - (en[small] @ ex)[:, None] * en[small]
+    el /= np.linalg.norm(el, axis=1)[:, None]
+    ec_ = np.cross(en, el)
+    zs = np.clip((a - c[:, 2]) / (a - z_base), 0.0, 1.0)
+    alpha = np.deg2rad((1.0 - zs) * alpha_apex + zs * alpha_base)
+    fib = np.cos(alpha)[:, None] * ec_ + np.sin(alpha)[:, None] * el
+    return Mesh(xyz0=V, tri=F.astype(np.int32), n_bnodes=np.array([ring.size], dtype=np.int32), bnodes=ring,
+                fib=fib, gamma_scale=np.full(len(F), 1.0 - lambda_a),
+                meta=dict(kind="lv", freq=freq, seed=seed, a=a, b=b, f_cut=f_cut, nflip=nflip, jitter=jitter,
+                          hmean=hmean))

@@ -20,3 +20,18 @@ def pytest_configure(config):
 def oracle_lib():
     from oracle.pyoracle import Oracle
     return Oracle()
+
+
+def golden_case(path):
+    """(workload, meta, arrays) of a golden fixture made by tests/golden/make_golden.py."""
+    import json
+    import numpy as np
+    from biofem import configs
+    d = np.load(path)
+    meta = json.loads(str(d["meta"]))
+    if meta.get("kind") == "lv":
+        keys = ("name", "freq", "index", "n_qp", "c33_iters", "pressure", "lambda_a", "nflip", "jitter")
+        return configs.LVWorkload(**{k: meta[k] for k in keys}), meta, d
+    keys = ("name", "nx", "ny", "n_qp", "c33_iters", "pressure", "z_sigma", "activation",
+            "lambda_a", "disp_rel", "index")
+    return configs.Workload(**{k: meta[k] for k in keys}), meta, d

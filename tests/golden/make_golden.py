@@ -35,6 +35,10 @@ def sha(a: np.ndarray) -> str:
 
 
 def workload_dict(w) -> dict:
+    if isinstance(w, configs.LVWorkload):
+        return dict(kind="lv", name=w.name, freq=w.freq, index=w.index, n_qp=w.n_qp, c33_iters=w.c33_iters,
+                    pressure=w.pressure, lambda_a=w.lambda_a, nflip=w.nflip, jitter=w.jitter,
+                    mu=configs.MU, bulk=configs.BULK, h0=configs.H0)
     return dict(name=w.name, nx=w.nx, ny=w.ny, n_qp=w.n_qp, c33_iters=w.c33_iters, pressure=w.pressure,
                 z_sigma=w.z_sigma, activation=w.activation, lambda_a=w.lambda_a, disp_rel=w.disp_rel,
                 index=w.index, mu=configs.MU, bulk=configs.BULK, h0=configs.H0)
@@ -81,10 +85,15 @@ CASES_FULL = [
     configs.small(12, 8, n_qp=5, c33_iters=1, index=12, pressure=1e-3),
     configs.small(10, 6, n_qp=2, c33_iters=4, activation="random", index=13),
     configs.C1,
+    # truncated ellipsoid caps: interior valence 5/7 and jagged-rim irregular patches
+    configs.LVWorkload("lv_f3", 3, index=40),
+    configs.LVWorkload("lv_f4_q5", 4, index=41, n_qp=5, c33_iters=2, pressure=5e-4),
 ]
 
 if __name__ == "__main__":
+    only = [a for a in sys.argv[1:] if not a.startswith("--")]
     for w in CASES_FULL:
-        make(w, full=True)
+        if not only or w.name in only:
+            make(w, full=True)
     if "--c2" in sys.argv:
         make(configs.C2, full=False)

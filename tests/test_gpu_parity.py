@@ -14,7 +14,7 @@ import json
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, golden_case
 from biofem import configs
 from biofem.configs import Workload
 
@@ -24,11 +24,7 @@ FULL = sorted(p for p in GOLDEN.glob("*.npz") if "R" in np.load(p))
 
 
 def load_case(path):
-    d = np.load(path)
-    meta = json.loads(str(d["meta"]))
-    keys = ("name", "nx", "ny", "n_qp", "c33_iters", "pressure", "z_sigma", "activation",
-            "lambda_a", "disp_rel", "index")
-    return Workload(**{k: meta[k] for k in keys}), meta, d
+    return golden_case(path)
 
 
 def shell_for(m, w):
@@ -70,6 +66,7 @@ def test_residual_is_deterministic():
                                 configs.small(10, 8, activation="random", index=44, n_qp=6, pressure=1e-4),
                                 configs.small(11, 8, activation="random", index=45, n_qp=6, basis=1),
                                 configs.small(12, 9, index=46, basis=1, tnormal=1, pressure=1e-3),
+                                configs.LVWorkload("lv_f4", 4, index=47),
                                 configs.C1],
                          ids=lambda w: w.name + ("_exact" if w.basis else "") + ("_tnormal" if w.tnormal else ""))
 def test_tangent_matches_oracle_directional_derivative(wl, oracle_lib):
@@ -78,7 +75,8 @@ def test_tangent_matches_oracle_directional_derivative(wl, oracle_lib):
     sh = shell_for(m, wl)
     x = wl.initial_x(m, sh.topology()["xyz0_full"])
     rng = np.random.default_rng(5)
-    x[: 3 * m.n_v] += 1e-3 * (wl.nx ** -1) * rng.standard_normal(3 * m.n_v)
+    h = 1.0 / wl.nx if hasattr(wl, "nx") else m.meta["hmean"]
+    x[: 3 * m.n_v] += 1e-3 * h * rng.standard_normal(3 * m.n_v)
     R, K = sh.form_jacobian(x)
     Rres = sh.form_function(x)
     assert np.array_equal(R, Rres)  # the tangent pass returns the same residual

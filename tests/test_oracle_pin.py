@@ -12,7 +12,7 @@ import json
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, golden_case
 from biofem import configs
 from biofem.configs import Workload
 
@@ -20,12 +20,7 @@ FULL = sorted(p for p in GOLDEN.glob("*.npz") if "meta" in np.load(p) and "R" in
 
 
 def load_case(path):
-    d = np.load(path)
-    meta = json.loads(str(d["meta"]))
-    keys = ("name", "nx", "ny", "n_qp", "c33_iters", "pressure", "z_sigma", "activation",
-            "lambda_a", "disp_rel", "index")
-    w = Workload(**{k: meta[k] for k in keys})
-    return w, meta, d
+    return golden_case(path)
 
 
 @pytest.mark.parametrize("path", FULL, ids=lambda p: p.stem)

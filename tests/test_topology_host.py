@@ -27,6 +27,22 @@ def test_host_topology_equals_oracle(nx, ny, oracle_lib):
     sh.close()
 
 
+@pytest.mark.parametrize("freq", [3, 5])
+def test_host_topology_equals_oracle_ellipsoid(freq, oracle_lib):
+    """Truncated ellipsoid caps: isolated interior vertices of valence 5 and 7
+    and a jagged cut rim (boundary valences 5, 6, 7)."""
+    w = configs.LVWorkload(f"lv_f{freq}", freq, index=50 + freq)
+    m = w.build_mesh()
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0)
+    to = o.topology()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    th = sh.topology()
+    assert th["ire"].sum() > 0
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        assert np.array_equal(th[k], getattr(to, k)), k
+    sh.close()
+
+
 def test_host_topology_matches_reference_checksum_C2():
     """C2 (98,304 triangles): the reference's O(N^2) Patch() output is stored
     as SHA-256 checksums in tests/golden/C2_flat_256x192.npz."""
