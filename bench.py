@@ -145,6 +145,23 @@ def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0):
     return n_elems * len(times) / sum(times), sum(times), n_elems
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest rank's time: every rank's timed region is reduced with MAX
+    (replicas: no data exchange inside the timed region)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_rank: int, seconds: float) -> float:
+    """Weak scaling: every rank processes its own copy of the workload, so the
+    job rate is all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 def newton_bench(reps=3):
     """One quasi-static load step (Newton + multigrid-preconditioned device
     GMRES to ||R|| <= 1e-10 ||R0||) on C1 and C2, FP64 and FP32-bulk tangents;
@@ -402,11 +419,7 @@ def run_ours(args):
         sh.sync(sp)
         clk = clocks.stop()
         ms_steps = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-        ms = sum(ms_steps) / args.steps
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(sum(ms_steps) / args.steps, dist, dev)
 
         # per-kernel durations (separate pass; the library records events between launches)
         sh.kernel_timing(True)
@@ -478,11 +491,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         sh.residual_jacobian_host_ptrs(hx.data_ptr(), hR.data_ptr(), hK.data_ptr())
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_t) / len(e2e_t)
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(sum(e2e_t) / len(e2e_t), dist, dev)
     # consistency: the host call returns the same R as the device call
     Rdev = dR.cpu().numpy()
     sh.residual_host_ptrs(hx.data_ptr(), hR.data_ptr())
@@ -501,7 +510,7 @@ def run_ours(args):
 
     info = sh.info
     ne = info.n_elmt
-    value = world * ne / (ms * 1e-3)
+    value = whole_job_rate(world, ne, ms * 1e-3)
     b_alg = algorithmic_bytes(info, topo, sh.nnzb)
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
@@ -538,7 +547,7 @@ def run_ours(args):
                              "peak_tflops": 1.25, "peak_source": "nominal GB300 FP64 (not measured)"},
         "kernels_ms": dict(zip(names, kms)),
         "residual_only": {"ms_per_step": sum(r_ms) / len(r_ms), "elems_per_s": ne / (sum(r_ms) / len(r_ms) * 1e-3)},
-        "e2e": {"value": world * ne / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 8 * sh.n_dof,
+        "e2e": {"value": whole_job_rate(world, ne, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 8 * sh.n_dof,
                 "d2h_bytes_per_step": 8 * sh.n_dof + 72 * sh.nnzb, "host_equals_device_R": same},
         "fp32_bulk": {"ms_per_step": f32_step, "elems_per_s": world * ne / (f32_step * 1e-3),
                       "speedup_vs_fp64": ms / f32_step,
