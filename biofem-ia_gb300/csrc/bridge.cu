@@ -636,9 +636,9 @@ int GetGpuLaunchCounts(const BiofemGpuMesh *m, int32_t *res, int32_t *jac)
 {
   if (!m) return fail(85, "null argument");
   if (res) *res = 4;   /* positions, element residual, node gather, scale */
-  /* FP64: positions, element tangent, node gather, block gather, scale;
-     FP32-bulk adds the FP64 element residual */
-  if (jac) *jac = m->prm.precision == BIOFEM_FP64 ? 5 : 6;
+  /* positions, element residual (FP64), element tangent, node gather,
+     block gather, scale */
+  if (jac) *jac = 6;
   return 0;
 }
 
@@ -679,12 +679,15 @@ int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_
   int rc = 0;
   tmark(m, st, 0);
   if (m->prm.precision == BIOFEM_FP64) {
+    /* R from the residual kernel, so that the Jacobian call returns exactly
+       the residual call's R */
     double *K = static_cast<double *>(d_K);
     if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
-    if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 2); }
-    if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 3); }
-    if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st); tmark(m, st, 4); }
-    if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, K, st); tmark(m, st, 5); }
+    if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
+    if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 3); }
+    if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
+    if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st); tmark(m, st, 5); }
+    if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, K, st); tmark(m, st, 6); }
   } else {
     /* FP32-bulk: residual in FP64, tangent (D, K_e, K) in FP32 */
     float *K = static_cast<float *>(d_K);

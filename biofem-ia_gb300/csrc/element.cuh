@@ -200,70 +200,173 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
   }
 }
 
+/* Mid-surface geometry of the element from y = (a1, a2, Aaa, Abb, Aab). */
+template <class T> struct ElemGeom {
+  V3<T> a1, a2, Aaa, Abb, Aab, n, gc1, gc2, a31, a32;
+};
+
+template <class T, class R>
+__host__ __device__ __forceinline__ ElemGeom<T> elem_geom(const T y[15], const EPar<R> &p)
+{
+  const R one = R(1);
+  ElemGeom<T> g;
+  g.a1 = {y[0], y[1], y[2]}; g.a2 = {y[3], y[4], y[5]};
+  g.Aaa = {y[6], y[7], y[8]}; g.Abb = {y[9], y[10], y[11]}; g.Aab = {y[12], y[13], y[14]};
+  const V3<T> cr = cross(g.a1, g.a2);
+  const T cn = dsqrt(dot(cr, cr));
+  const T icn = one / cn;
+  g.n = scl(icn, cr);
+  const V3<T> t1 = cross(g.a2, g.n);
+  g.gc1 = scl(one / dot(g.a1, t1), t1);
+  const V3<T> t2 = cross(g.n, g.a1);
+  g.gc2 = scl(one / dot(g.a2, t2), t2);
+  g.a31 = scl(icn, cross(g.Aaa, g.a2) + cross(g.a1, g.Aab));
+  g.a32 = scl(icn, cross(g.Aab, g.a2) + cross(g.a1, g.Abb));
+  if (p.tnormal) {   /* n_,alpha: drop the J_,alpha / J n part of the unnormalised derivative */
+    g.a31 = g.a31 - scl(dot(g.a31, g.n), g.n);
+    g.a32 = g.a32 - scl(dot(g.a32, g.n), g.n);
+  }
+  return g;
+}
+
+/* Metric (00 11 01 02 12 22) of the thickness point theta3 (ElemUpdateG). */
+template <class T, class R>
+__host__ __device__ __forceinline__ void qp_metric(const ElemGeom<T> &g, R th3, T gm[6])
+{
+  const V3<T> g1 = g.a1 + scl(th3, g.a31), g2 = g.a2 + scl(th3, g.a32);
+  gm[0] = dot(g1, g1); gm[1] = dot(g2, g2); gm[2] = dot(g1, g2);
+  gm[3] = dot(g1, g.n); gm[4] = dot(g2, g.n); gm[5] = dot(g.n, g.n);
+}
+
+template <class R>
+__host__ __device__ __forceinline__ QpRef<R> load_qpref(const R *ref, int stride, int q)
+{
+  QpRef<R> r;
+  const R *rq = ref + (size_t)kRefPerQp * q * stride;
+  r.gc00 = rq[0]; r.gc11 = rq[(size_t)1 * stride]; r.gc01 = rq[(size_t)2 * stride]; r.gc22 = rq[(size_t)3 * stride];
+  for (int k = 0; k < 3; k++) {
+    r.s[k] = rq[(size_t)(4 + k) * stride];
+    r.t[k] = rq[(size_t)(7 + k) * stride];
+    r.av[k] = rq[(size_t)(11 + k) * stride];
+    r.aw[k] = rq[(size_t)(14 + k) * stride];
+    r.ae[k] = rq[(size_t)(17 + k) * stride];
+  }
+  r.rho = rq[(size_t)10 * stride];
+  return r;
+}
+
+/* The 15 force components from the resultants (ElemUpdFint, Nᵀ applied by the caller). */
+template <class T, class R>
+__host__ __device__ __forceinline__ void elem_out(const ElemGeom<T> &g, T N0, T N1, T N2, T M0, T M1, T M2, R pref0,
+                                                  T f[15])
+{
+  const R two = R(2);
+  N0 = pref0 * N0; N1 = pref0 * N1; N2 = pref0 * N2;
+  M0 = pref0 * M0; M1 = pref0 * M1; M2 = pref0 * M2;
+  const T twoM2 = two * M2;
+  const V3<T> Q = scl(M0, g.Aaa) + scl(M1, g.Abb) + scl(twoM2, g.Aab);
+  const V3<T> f1 = scl(N0, g.a1) + scl(N2, g.a2) - scl(dot(g.gc1, Q), g.n);
+  const V3<T> f2 = scl(N1, g.a2) + scl(N2, g.a1) - scl(dot(g.gc2, Q), g.n);
+  f[0] = f1.x; f[1] = f1.y; f[2] = f1.z;
+  f[3] = f2.x; f[4] = f2.y; f[5] = f2.z;
+  f[6] = -(M0 * g.n.x); f[7] = -(M0 * g.n.y); f[8] = -(M0 * g.n.z);
+  f[9] = -(M1 * g.n.x); f[10] = -(M1 * g.n.y); f[11] = -(M1 * g.n.z);
+  f[12] = -(twoM2 * g.n.x); f[13] = -(twoM2 * g.n.y); f[14] = -(twoM2 * g.n.z);
+}
+
 /* f(y): the 15 force components of the element.
    ref points at the element's first SoA constant (type R); stride = ne. */
 template <class T, class R>
 __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R> &p, const R *ref, int stride,
                                                      T f[15], int &status)
 {
-  const R one = R(1), two = R(2);
-  const V3<T> a1 = {y[0], y[1], y[2]}, a2 = {y[3], y[4], y[5]};
-  const V3<T> Aaa = {y[6], y[7], y[8]}, Abb = {y[9], y[10], y[11]}, Aab = {y[12], y[13], y[14]};
-  const V3<T> cr = cross(a1, a2);
-  const T cn = dsqrt(dot(cr, cr));
-  const T icn = one / cn;
-  const V3<T> n = scl(icn, cr);
-  const V3<T> t1 = cross(a2, n);
-  const V3<T> gc1 = scl(one / dot(a1, t1), t1);
-  const V3<T> t2 = cross(n, a1);
-  const V3<T> gc2 = scl(one / dot(a2, t2), t2);
-  V3<T> a31 = scl(icn, cross(Aaa, a2) + cross(a1, Aab));
-  V3<T> a32 = scl(icn, cross(Aab, a2) + cross(a1, Abb));
-  if (p.tnormal) {   /* n_,alpha: drop the J_,alpha / J n part of the unnormalised derivative */
-    a31 = a31 - scl(dot(a31, n), n);
-    a32 = a32 - scl(dot(a32, n), n);
-  }
-
+  const ElemGeom<T> g = elem_geom<T, R>(y, p);
   const int nq = p.nq;
   const R gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];
   const R gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
   const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
   const R pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
-
   const T zero = T{R(0)};
   T N0 = zero, N1 = zero, N2 = zero, M0 = zero, M1 = zero, M2 = zero;
   for (int q = 0; q < nq; q++) {
-    QpRef<R> r;
-    const R *rq = ref + (size_t)kRefPerQp * q * stride;
-    r.gc00 = rq[0]; r.gc11 = rq[(size_t)1 * stride]; r.gc01 = rq[(size_t)2 * stride]; r.gc22 = rq[(size_t)3 * stride];
-    for (int k = 0; k < 3; k++) {
-      r.s[k] = rq[(size_t)(4 + k) * stride];
-      r.t[k] = rq[(size_t)(7 + k) * stride];
-      r.av[k] = rq[(size_t)(11 + k) * stride];
-      r.aw[k] = rq[(size_t)(14 + k) * stride];
-      r.ae[k] = rq[(size_t)(17 + k) * stride];
-    }
-    r.rho = rq[(size_t)10 * stride];
+    const QpRef<R> r = load_qpref(ref, stride, q);
     const R th3 = p.hhalf * p.theta[q];
-    const V3<T> g1 = a1 + scl(th3, a31), g2 = a2 + scl(th3, a32);
-    T gm[6] = {dot(g1, g1), dot(g2, g2), dot(g1, g2), dot(g1, n), dot(g2, n), dot(n, n)};
+    T gm[6];
+    qp_metric(g, th3, gm);
     T sv[3];
     qp_stress(gm, r, gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
     const R wq = p.w[q], wt = p.w[q] * th3;
     N0 = N0 + wq * sv[0]; N1 = N1 + wq * sv[1]; N2 = N2 + wq * sv[2];
     M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
   }
-  N0 = pref0 * N0; N1 = pref0 * N1; N2 = pref0 * N2;
-  M0 = pref0 * M0; M1 = pref0 * M1; M2 = pref0 * M2;
-  const T twoM2 = two * M2;
-  const V3<T> Q = scl(M0, Aaa) + scl(M1, Abb) + scl(twoM2, Aab);
-  const V3<T> f1 = scl(N0, a1) + scl(N2, a2) - scl(dot(gc1, Q), n);
-  const V3<T> f2 = scl(N1, a2) + scl(N2, a1) - scl(dot(gc2, Q), n);
-  f[0] = f1.x; f[1] = f1.y; f[2] = f1.z;
-  f[3] = f2.x; f[4] = f2.y; f[5] = f2.z;
-  f[6] = -(M0 * n.x); f[7] = -(M0 * n.y); f[8] = -(M0 * n.z);
-  f[9] = -(M1 * n.x); f[10] = -(M1 * n.y); f[11] = -(M1 * n.z);
-  f[12] = -(twoM2 * n.x); f[13] = -(twoM2 * n.y); f[14] = -(twoM2 * n.z);
+  elem_out(g, N0, N1, N2, M0, M1, M2, pref0, f);
+}
+
+/* Element forces and their derivative along y_lane, for a group of 16 lanes
+   sharing one element (lane l < 15 carries direction l of y).  The
+   constitutive update depends on y only through the 6 metric components of
+   each thickness point, so it is differentiated along those: job (q, k) =
+   derivative of the stress of point q along metric component k, one job per
+   lane per round; each lane then applies the chain rule with its own metric
+   derivative.  That is 6 nq constitutive evaluations per element instead of
+   16 nq.  The primal values are the plain R-precision evaluation.
+   jac: this group's scratch, kMaxQp * 21 values; the 16 lanes of the group
+   and the other group of the warp must all call this (it synchronises the
+   warp). */
+template <class R>
+__device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &p, const R *ref, int stride, int lane,
+                                                  R *jac, D1<R> f[15], int &status)
+{
+  typedef D1<R> T;
+  const int nq = p.nq;
+  const R gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];
+  const R gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
+  const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
+  const R pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
+  /* constitutive derivatives: jac[q*21 + 6*i + k] = d sv_i / d gm_k, jac[q*21 + 18 + i] = sv_i */
+  {
+    const ElemGeom<R> g0 = elem_geom<R, R>(y, p);
+    for (int job = lane; job < 6 * nq; job += 16) {
+      const int q = job / 6, k = job - 6 * q;
+      R gmv[6];
+      qp_metric(g0, p.hhalf * p.theta[q], gmv);
+      T gm[6];
+#pragma unroll
+      for (int c = 0; c < 6; c++) gm[c] = T{gmv[c], c == k ? R(1) : R(0)};
+      T sv[3];
+      qp_stress(gm, load_qpref(ref, stride, q), gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
+#pragma unroll
+      for (int i = 0; i < 3; i++) jac[q * 21 + 6 * i + k] = sv[i].d;
+      if (k == 0) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) jac[q * 21 + 18 + i] = sv[i].v;
+      }
+    }
+  }
+  __syncwarp();
+  T yd[15];
+#pragma unroll
+  for (int c = 0; c < 15; c++) yd[c] = T{y[c], c == lane ? R(1) : R(0)};
+  const ElemGeom<T> g = elem_geom<T, R>(yd, p);
+  const T zero = T{R(0), R(0)};
+  T N0 = zero, N1 = zero, N2 = zero, M0 = zero, M1 = zero, M2 = zero;
+  for (int q = 0; q < nq; q++) {
+    const R th3 = p.hhalf * p.theta[q];
+    T gm[6];
+    qp_metric(g, th3, gm);
+    T sv[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      R d = R(0);
+#pragma unroll
+      for (int c = 0; c < 6; c++) d += jac[q * 21 + 6 * i + c] * gm[c].d;
+      sv[i] = T{jac[q * 21 + 18 + i], d};
+    }
+    const R wq = p.w[q], wt = p.w[q] * th3;
+    N0 = N0 + wq * sv[0]; N1 = N1 + wq * sv[1]; N2 = N2 + wq * sv[2];
+    M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
+  }
+  elem_out(g, N0, N1, N2, M0, M1, M2, pref0, f);
 }
 
 } /* namespace biofem */

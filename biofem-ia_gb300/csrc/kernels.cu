@@ -238,6 +238,7 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   __shared__ double tabs[kNumTables * 80];
   __shared__ double Dsh[kTanElemsPerCta][15 * 16];   /* D[r][s] at r*16+s */
   __shared__ double Tsh[kTanElemsPerCta][15 * 48];   /* T[r3][c] : (D N) */
+  __shared__ double Jsh[kTanElemsPerCta][kMaxQp * 21]; /* constitutive derivatives per thickness point */
   for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
   __syncthreads();
   const int lane = threadIdx.x & 15;
@@ -250,12 +251,10 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   const double *tab = tabs + tabi * 80;
   double y[15];
   gather_y(m.pos, m.patch, ee, nen, tab, y);
-  D1d yd[15], fd[15];
-#pragma unroll
-  for (int k = 0; k < 15; k++) yd[k] = D1d{y[k], k == lane ? 1.0 : 0.0};
+  D1d fd[15];
   int st = 0;
   const EPar<double> ep = epar<double>(p);
-  elem_forces<D1d, double>(yd, ep, m.eref + ee, p.ne, fd, st);
+  elem_forces_split<double>(y, ep, m.eref + ee, p.ne, lane, Jsh[slot], fd, st);
   if (live) set_status(m.status, st);
   const size_t ne = p.ne;
   /* column `lane` of D = df/dy */
@@ -263,28 +262,7 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
 #pragma unroll
     for (int r = 0; r < 15; r++) Dsh[slot][r * 16 + lane] = fd[r].d;
   }
-  /* element force (primal part, identical in every lane) */
-  if (live) {
-    for (int idx = lane; idx < 3 * nen; idx += 16) {
-      const int a = idx / 3, d = idx - 3 * a;
-      double s = 0.0;
-#pragma unroll
-      for (int r = 0; r < 5; r++) s += tab[r * 16 + a] * fd[3 * r + d].v;
-      m.fb[(size_t)idx * ne + e] = s;
-    }
-    if (lane == 0 && p.pressure != 0.0) {
-      double X[3][3];
-      for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
-      const V3<double> d21 = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
-      const V3<double> d31 = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
-      const V3<double> ca = cross(d21, d31);
-      const double nrm = sqrt(ca.x * ca.x + ca.y * ca.y + ca.z * ca.z);
-      const double dA = 0.5 * nrm;
-      m.fp[e] = (ca.x / nrm) * p.pressure * dA / 3.;
-      m.fp[ne + e] = (ca.y / nrm) * p.pressure * dA / 3.;
-      m.fp[2 * ne + e] = (ca.z / nrm) * p.pressure * dA / 3.;
-    }
-  }
+  /* the element forces come from k_elem_residual, launched before this kernel */
   __syncwarp();
   /* T[(r,i)][(b,j)] = sum_s D[(r,i)][(s,j)] N[s][b] */
   const int ncol = 3 * nen;
@@ -349,6 +327,7 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
   __shared__ float tsum[kNumTables * 5];
   __shared__ float Dsh[kTanElemsPerCta][15 * 16];
   __shared__ float Tsh[kTanElemsPerCta][15 * 48];
+  __shared__ float JshF[kTanElemsPerCta][kMaxQp * 21];
   for (int i = threadIdx.x; i < kNumTables * 85; i += blockDim.x) {
     if (i < kNumTables * 80) tabs[i] = m.ntabF[i]; else tsum[i - kNumTables * 80] = m.ntabF[i];
   }
@@ -389,12 +368,10 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
       }
     }
   }
-  D1f yd[15], fd[15];
-#pragma unroll
-  for (int k = 0; k < 15; k++) yd[k] = D1f{y[k], k == lane ? 1.f : 0.f};
+  D1f fd[15];
   int st = 0;
   const EPar<float> ep = epar<float>(p);
-  elem_forces<D1f, float>(yd, ep, m.erefF + ee, p.ne, fd, st);
+  elem_forces_split<float>(y, ep, m.erefF + ee, p.ne, lane, JshF[slot], fd, st);
   if (live) set_status(m.status, st);
   if (lane < 15) {
 #pragma unroll
