@@ -37,8 +37,8 @@ for _p in (ROOT, ROOT / "biofem-ia_gb300"):
 
 METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_elem_tangent launch on
-# the 256x192 workload (ncu --set full; 61.6 MB read, 1,263 MB written)
-TANGENT_DRAM_BYTES_C2 = 61.6e6 + 1263e6
+# the 256x192 workload (ncu --set full; 62.5 MB read, 1,216 MB written)
+TANGENT_DRAM_BYTES_C2 = 62.5e6 + 1216e6
 UNIT = "elems/s"
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_ELEMS = 2048

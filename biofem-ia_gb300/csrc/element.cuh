@@ -62,11 +62,56 @@ template <class R> __host__ __device__ __forceinline__ D1<R> operator-(D1<R> a, 
 template <class R> __host__ __device__ __forceinline__ D1<R> operator-(R a, D1<R> b) { return {a - b.v, -b.d}; }
 template <class R> __host__ __device__ __forceinline__ D1<R> operator*(D1<R> a, R b) { return {a.v * b, a.d * b}; }
 template <class R> __host__ __device__ __forceinline__ D1<R> operator*(R a, D1<R> b) { return {a * b.v, a * b.d}; }
-template <class R> __host__ __device__ __forceinline__ D1<R> operator/(D1<R> a, D1<R> b) { R q = a.v / b.v; return {q, (a.d - q * b.d) / b.v}; }
-template <class R> __host__ __device__ __forceinline__ D1<R> operator/(R a, D1<R> b) { R q = a / b.v; return {q, -q * b.d / b.v}; }
-template <class R> __host__ __device__ __forceinline__ D1<R> operator/(D1<R> a, R b) { return {a.v / b, a.d / b}; }
-__host__ __device__ __forceinline__ D1d dsqrt(D1d a) { double r = sqrt(a.v); return {r, a.d / (2.0 * r)}; }
-__host__ __device__ __forceinline__ D1f dsqrt(D1f a) { float r = sqrtf(a.v); return {r, a.d / (2.0f * r)}; }
+/* Quotients take one reciprocal for value and derivative (the dual types are
+   used only by the tangent kernels, whose primal values feed derivatives
+   alone; the residual is evaluated separately in the plain type). */
+template <class R> __host__ __device__ __forceinline__ D1<R> operator/(D1<R> a, D1<R> b)
+{
+  const R r = R(1) / b.v, q = a.v * r;
+  return {q, (a.d - q * b.d) * r};
+}
+template <class R> __host__ __device__ __forceinline__ D1<R> operator/(R a, D1<R> b)
+{
+  const R r = R(1) / b.v, q = a * r;
+  return {q, -(q * b.d) * r};
+}
+template <class R> __host__ __device__ __forceinline__ D1<R> operator/(D1<R> a, R b) { const R r = R(1) / b; return {a.v * r, a.d * r}; }
+__host__ __device__ __forceinline__ D1d dsqrt(D1d a) { double r = sqrt(a.v); return {r, a.d * (0.5 / r)}; }
+__host__ __device__ __forceinline__ D1f dsqrt(D1f a) { float r = sqrtf(a.v); return {r, a.d * (0.5f / r)}; }
+/* K-direction dual number (the constitutive derivatives of the tangent
+   kernels carry 2 or 3 metric directions per lane). */
+template <class R, int K> struct DK { R v; R d[K]; };
+template <class R, int K> __host__ __device__ __forceinline__ R val(const DK<R, K> &a) { return a.v; }
+#define BIOFEM_DK_LOOP _Pragma("unroll") for (int i = 0; i < K; i++)
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator+(const DK<R, K> &a, const DK<R, K> &b)
+{ DK<R, K> c; c.v = a.v + b.v; BIOFEM_DK_LOOP c.d[i] = a.d[i] + b.d[i]; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator-(const DK<R, K> &a, const DK<R, K> &b)
+{ DK<R, K> c; c.v = a.v - b.v; BIOFEM_DK_LOOP c.d[i] = a.d[i] - b.d[i]; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator-(const DK<R, K> &a)
+{ DK<R, K> c; c.v = -a.v; BIOFEM_DK_LOOP c.d[i] = -a.d[i]; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator*(const DK<R, K> &a, const DK<R, K> &b)
+{ DK<R, K> c; c.v = a.v * b.v; BIOFEM_DK_LOOP c.d[i] = a.d[i] * b.v + a.v * b.d[i]; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator+(const DK<R, K> &a, R b)
+{ DK<R, K> c = a; c.v = a.v + b; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator+(R a, const DK<R, K> &b)
+{ DK<R, K> c = b; c.v = a + b.v; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator-(const DK<R, K> &a, R b)
+{ DK<R, K> c = a; c.v = a.v - b; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator-(R a, const DK<R, K> &b)
+{ DK<R, K> c; c.v = a - b.v; BIOFEM_DK_LOOP c.d[i] = -b.d[i]; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator*(const DK<R, K> &a, R b)
+{ DK<R, K> c; c.v = a.v * b; BIOFEM_DK_LOOP c.d[i] = a.d[i] * b; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator*(R a, const DK<R, K> &b)
+{ DK<R, K> c; c.v = a * b.v; BIOFEM_DK_LOOP c.d[i] = a * b.d[i]; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator/(const DK<R, K> &a, const DK<R, K> &b)
+{ DK<R, K> c; const R r = R(1) / b.v; c.v = a.v * r; BIOFEM_DK_LOOP c.d[i] = (a.d[i] - c.v * b.d[i]) * r; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator/(R a, const DK<R, K> &b)
+{ DK<R, K> c; const R r = R(1) / b.v; c.v = a * r; BIOFEM_DK_LOOP c.d[i] = -(c.v * b.d[i]) * r; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> operator/(const DK<R, K> &a, R b)
+{ DK<R, K> c; const R r = R(1) / b; c.v = a.v * r; BIOFEM_DK_LOOP c.d[i] = a.d[i] * r; return c; }
+template <class R, int K> __host__ __device__ __forceinline__ DK<R, K> dsqrt(const DK<R, K> &a)
+{ DK<R, K> c; c.v = sqrt(a.v); const R h = R(0.5) / c.v; BIOFEM_DK_LOOP c.d[i] = a.d[i] * h; return c; }
+#undef BIOFEM_DK_LOOP
 __host__ __device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
 __host__ __device__ __forceinline__ float dsqrt(float a) { return sqrtf(a); }
 __host__ __device__ __forceinline__ double dabs(double a) { return fabs(a); }
@@ -302,6 +347,39 @@ __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R
   elem_out(g, N0, N1, N2, M0, M1, M2, pref0, f);
 }
 
+/* Jobs (q, k0..k0+KD-1) of the split tangent: stress of thickness point q
+   with KD metric directions; jac layout as in elem_forces_split. */
+template <class R, int KD>
+__device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> &g0, const EPar<R> &p, const R *ref, int stride,
+                                                  int lane, R gam, R gamp, R c1, R *jac, int &status)
+{
+  typedef DK<R, KD> T;
+  constexpr int per_q = 6 / KD;
+  for (int job = lane; job < per_q * p.nq; job += 16) {
+    const int q = job / per_q, k0 = (job - per_q * q) * KD;
+    R gmv[6];
+    qp_metric(g0, p.hhalf * p.theta[q], gmv);
+    T gm[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+      gm[c].v = gmv[c];
+#pragma unroll
+      for (int i = 0; i < KD; i++) gm[c].d[i] = (c == k0 + i) ? R(1) : R(0);
+    }
+    T sv[3];
+    qp_stress(gm, load_qpref(ref, stride, q), gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+#pragma unroll
+      for (int t = 0; t < KD; t++) jac[q * 21 + 6 * i + k0 + t] = sv[i].d[t];
+    }
+    if (k0 == 0) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) jac[q * 21 + 18 + i] = sv[i].v;
+    }
+  }
+}
+
 /* Element forces and their derivative along y_lane, for a group of 16 lanes
    sharing one element (lane l < 15 carries direction l of y).  The
    constitutive update depends on y only through the 6 metric components of
@@ -323,24 +401,18 @@ __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &
   const R gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
   const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
   const R pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
-  /* constitutive derivatives: jac[q*21 + 6*i + k] = d sv_i / d gm_k, jac[q*21 + 18 + i] = sv_i */
+  /* constitutive derivatives: jac[q*21 + 6*i + k] = d sv_i / d gm_k, jac[q*21 + 18 + i] = sv_i;
+     FP64: KD metric directions per job so that the 6 nq / KD jobs fit one
+     round of 16 lanes (KD = 1 up to 2 thickness points, 2 up to 5, 3 for 6) */
   {
     const ElemGeom<R> g0 = elem_geom<R, R>(y, p);
-    for (int job = lane; job < 6 * nq; job += 16) {
-      const int q = job / 6, k = job - 6 * q;
-      R gmv[6];
-      qp_metric(g0, p.hhalf * p.theta[q], gmv);
-      T gm[6];
-#pragma unroll
-      for (int c = 0; c < 6; c++) gm[c] = T{gmv[c], c == k ? R(1) : R(0)};
-      T sv[3];
-      qp_stress(gm, load_qpref(ref, stride, q), gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
-#pragma unroll
-      for (int i = 0; i < 3; i++) jac[q * 21 + 6 * i + k] = sv[i].d;
-      if (k == 0) {
-#pragma unroll
-        for (int i = 0; i < 3; i++) jac[q * 21 + 18 + i] = sv[i].v;
-      }
+    if constexpr (sizeof(R) == 4) {
+      /* FP32: one direction per job (wider duals spill under the FP32 kernel's register cap) */
+      constitutive_jobs<R, 1>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
+    } else {
+      if (nq <= 2) constitutive_jobs<R, 1>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      else if (nq <= 5) constitutive_jobs<R, 2>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      else constitutive_jobs<R, 3>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
     }
   }
   __syncwarp();
