@@ -190,6 +190,41 @@ def newton_bench(reps=3):
     return out
 
 
+def dynamics_bench(steps=10):
+    """The implicit time loop (main.c:420-573): per step the element activation
+    gamma_e(t) (full sin^2 beat over the run, GammaOfTimeDelayed ramp 1, with a
+    wavefront delay on C4), a Newton solve with the Newmark inertial and damping
+    term in R and K (FDynamic), then xAccVel.  Wall time per step through the
+    public calls (host x in and out), FP64 and FP32-bulk tangents."""
+    from biofem import configs
+    from biofem.dynamics import Activation, Dynamics, time_loop
+    from biofem.gpu import GpuShell
+    out = {}
+    for w, dt in ((configs.C2, 1e-3), (configs.C4, 5e-3)):
+        m = w.build_mesh()
+        act = Activation(0.1, ramp_type=1)
+        delay = None
+        if "lv" in w.name:   # activation wavefront from the apex: delay proportional to height
+            z = m.xyz0[m.tri].mean(axis=1)[:, 2]
+            delay = 0.3 * steps * dt * (z - z.min()) / max(z.max() - z.min(), 1e-30)
+        for prec, tag in ((0, "fp64"), (1, "fp32_bulk")):
+            sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=prec)
+            x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+            dyn = Dynamics(dt=dt, rho=1.0, newmark_gamma=0.5, dampfactor=5.0, damping=1)
+            time_loop(sh, m, x0, dyn, act, 2, delay=delay, rtol=1e-10, max_newton=30)   # warm-up
+            t0 = time.perf_counter()
+            x, rec = time_loop(sh, m, x0, dyn, act, steps, delay=delay, rtol=1e-10, max_newton=30)
+            wall = time.perf_counter() - t0
+            out[f"{w.name}_{tag}"] = {
+                "ms_per_time_step": wall / steps * 1e3, "steps": steps, "dt": dt,
+                "newton_its_mean": float(np.mean([r.stats.get("newton_its", 0) for r in rec])),
+                "gmres_its_total": int(sum(r.stats.get("gmres_its_total", 0) for r in rec)),
+                "all_converged": all(r.converged for r in rec),
+                "max_displacement": float(np.abs((x - x0)[: 3 * m.n_v]).max())}
+            sh.close()
+    return out
+
+
 def case_bench(w, steps=5, warmup=2):
     """One large workload: R+K time of the FP64 and FP32-bulk forms (device
     pointers, L2 flushed between steps), a warm Newton load step with each,
@@ -510,6 +545,7 @@ def run_ours(args):
     c3 = case_bench(_cfg.C3) if not args.no_c3 else None
     c4 = case_bench(_cfg.C4) if not args.no_c3 else None
     serving = serve_bench(n_req=args.serve_requests) if not args.no_solve else None
+    dynamics = dynamics_bench() if not args.no_solve else None
 
     info = sh.info
     ne = info.n_elmt
@@ -569,6 +605,8 @@ def run_ours(args):
         line["newton_load_step"] = newton
     if serving:
         line["serving"] = serving
+    if dynamics:
+        line["dynamics"] = dynamics
     if c3:
         line["C3"] = c3
     if c4:

@@ -67,6 +67,11 @@ class NewtonOptions(ctypes.Structure):
                 ("line_search", ctypes.c_int32), ("preconditioner", ctypes.c_int32), ("forcing", ctypes.c_int32)]
 
 
+class DynParams(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("rho", ctypes.c_double), ("newmark_gamma", ctypes.c_double),
+                ("dampfactor", ctypes.c_double), ("timeinteg", ctypes.c_int32), ("damping", ctypes.c_int32)]
+
+
 class NewtonStats(ctypes.Structure):
     _fields_ = [("newton_its", ctypes.c_int32), ("gmres_its_total", ctypes.c_int32), ("gmres_its_last", ctypes.c_int32),
                 ("residual_evals", ctypes.c_int32), ("jacobian_evals", ctypes.c_int32), ("converged", ctypes.c_int32),
@@ -89,7 +94,9 @@ EXPORTS = ["InitGpuWorkspace", "DestroyGpuWorkspace", "PrepareGpuMesh", "Destroy
            "GetGpuBasisTables", "BiofemGpuLastError", "EnableGpuKernelTiming", "GetGpuKernelTimes",
            "GetGpuGhostMap", "RunGpuResidualNoAlloc", "BiofemNewtonDefaults", "RunGpuNewtonSolve",
            "RunGpuNewtonSolveDevice", "PrepareGpuMeshOnStream", "ServeCreate", "ServeSubmit", "ServeWait",
-           "ServeStatsGet", "ServeDestroy", "BiofemServeEstimateBytes", "GetGpuBasisTablesKind"]
+           "ServeStatsGet", "ServeDestroy", "BiofemServeEstimateBytes", "GetGpuBasisTablesKind",
+           "SetGpuDynamics", "SetGpuDynamicState", "GetGpuDynamicState", "RunGpuDynamicUpdate",
+           "SetGpuElementGamma"]
 
 
 def load_library(path: Path | str | None = None) -> ctypes.CDLL:
@@ -128,6 +135,11 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
     lib.EnableGpuKernelTiming.argtypes = [vp, ctypes.c_int]
     lib.GetGpuKernelTimes.argtypes = [vp, vp, ctypes.c_int32, vp]
     lib.GetGpuBasisTablesKind.argtypes = [ctypes.c_int32, vp]
+    lib.SetGpuDynamics.argtypes = [vp, ctypes.POINTER(DynParams)]
+    lib.SetGpuDynamicState.argtypes = [vp, vp, vp, vp, vp]
+    lib.GetGpuDynamicState.argtypes = [vp, vp, vp, vp, vp]
+    lib.RunGpuDynamicUpdate.argtypes = [vp, vp]
+    lib.SetGpuElementGamma.argtypes = [vp, vp]
     lib.ServeCreate.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(vp)]
     lib.ServeSubmit.argtypes = [vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(NewtonOptions),
                                 vp, ctypes.POINTER(ctypes.c_int64)]
@@ -274,6 +286,33 @@ class GpuShell:
         _check(self.lib, self.lib.RunGpuNewtonSolveDevice(self.handle, ctypes.c_void_p(d_x), ctypes.byref(o),
                                                           ctypes.byref(st), ctypes.c_void_p(stream or None)))
         return st.as_dict()
+
+    # ---- dynamics (FDynamic / xAccVel) and time-dependent activation ----
+    def set_dynamics(self, dt=None, rho=0.0, newmark_gamma=0.5, dampfactor=0.0, timeinteg=0, damping=0):
+        """SetGpuDynamics; dt=None switches the dynamic term off."""
+        if dt is None:
+            _check(self.lib, self.lib.SetGpuDynamics(self.handle, None))
+            return
+        d = DynParams(dt, rho, newmark_gamma, dampfactor, timeinteg, damping)
+        _check(self.lib, self.lib.SetGpuDynamics(self.handle, ctypes.byref(d)))
+
+    def set_dynamic_state(self, xn=None, xnm1=None, xd=None, xdd=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (xn, xnm1, xd, xdd)]
+        _check(self.lib, self.lib.SetGpuDynamicState(self.handle, *[None if a is None else _ptr(a) for a in arrs]))
+
+    def dynamic_state(self):
+        out = [np.empty(self.n_dof) for _ in range(4)]
+        _check(self.lib, self.lib.GetGpuDynamicState(self.handle, *[_ptr(a) for a in out]))
+        return dict(zip(("xn", "xnm1", "xd", "xdd"), out))
+
+    def dynamic_update(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _check(self.lib, self.lib.RunGpuDynamicUpdate(self.handle, _ptr(x)))
+
+    def set_element_gamma(self, gamma_e):
+        g = np.ascontiguousarray(gamma_e, dtype=np.float64)
+        assert g.size == self.info.n_elmt
+        _check(self.lib, self.lib.SetGpuElementGamma(self.handle, _ptr(g)))
 
     # ---- device-resident calls (raw CUDA pointers as ints) ----
     def residual_device(self, d_x: int, d_R: int, stream: int = 0):

@@ -39,6 +39,10 @@ struct KParams {
   double theta[kMaxQp], w[kMaxQp];
   double pressure;
   double gamma;
+  /* dynamic term (FDynamic, main.c:1157-1290): lumped corner mass rho h0 A0 / 3,
+     optional damping c M, Newmark (0) or central (1) differences */
+  int dyn, dyn_central, dyn_damp;
+  double dyn_rhoh0, dyn_dt, dyn_dampf, dyn_M1, dyn_M2, dyn_M3, dyn_C1, dyn_C2, dyn_C3, dyn_U2, dyn_U3;
   /* FP32 copies for the FP32-bulk kernels (filled on the host) */
   float muf, Kf, hhalff, pres6f;
   float thetaf[kMaxQp], wf[kMaxQp];
@@ -74,6 +78,10 @@ struct DevMesh {
   double *ke;                /* 9*total blocks element matrices (FP64 handles) */
   float *keF;                /* 9*total blocks element matrices (FP32-bulk handles) */
   int *status;               /* device error flag */
+  double *dA0;               /* n_elmt + 2 n_ghosts flat reference areas of every triangle (AreaNormal at Init) */
+  int *dptr, *didx;          /* per node, the triangles with that corner (ghost and bridging ones included), in triangle order */
+  double *xn, *xnm1, *xd, *xdd;   /* 3*nt dynamic state (previous positions, velocity, acceleration) */
+  double *dyn_diag;          /* nt: d Fdyn / d x on the diagonal of each free row */
   unsigned long long *fmax;  /* max |Fext| as ordered bits */
 };
 
@@ -89,6 +97,8 @@ int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);
 int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream);
 int launch_scale_f32(const DevMesh &m, const KParams &p, double *R, float *K, void *stream);
 int launch_to_float(const double *a, float *b, long long n, void *stream);
+int launch_dyn_diag(const DevMesh &m, const KParams &p, void *stream);
+int launch_dyn_update(const DevMesh &m, const KParams &p, const double *x, void *stream);
 int upload_tables(double *d_ntab);
 
 /* device Newton / GMRES (solver.cu) */

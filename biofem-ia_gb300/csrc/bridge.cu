@@ -157,6 +157,7 @@ struct BiofemGpuMesh_ {
   double *d_x = nullptr, *d_R = nullptr;   /* staging for host-array calls */
   void *d_K = nullptr;                      /* K values: double (FP64) or float (FP32-bulk) */
   SolverWork *solver = nullptr;             /* Newton/GMRES work, created on first solve */
+  double *d_fib = nullptr, *d_gam = nullptr;   /* fibres; per-element activation of SetGpuElementGamma */
   AmgHier *amg = nullptr;                   /* multigrid hierarchy, created on first multigrid solve */
   std::vector<unsigned char> rowkind;       /* host copy: 0 free, 1 clamped, 2 ghost */
   cudaStream_t st = nullptr;                /* stream of the host-array calls and of setup/teardown */
@@ -221,6 +222,18 @@ static void free_mesh(BiofemGpuMesh *m)
 }
 
 /* Host-side build of every map; no CUDA calls (usable without a GPU). */
+/* Flat reference area of triangle t (real, ghost or bridging), the
+   expression of AreaNormal (io.c:1646-1669) on the reference coordinates. */
+static double tri_area0(const HostTopo &T, int t)
+{
+  const double *X = T.xyz0_full.data();
+  const int a = T.tri_all[3 * (size_t)t], b = T.tri_all[3 * (size_t)t + 1], c = T.tri_all[3 * (size_t)t + 2];
+  const double d21[3] = {X[3 * b] - X[3 * a], X[3 * b + 1] - X[3 * a + 1], X[3 * b + 2] - X[3 * a + 2]};
+  const double d31[3] = {X[3 * c] - X[3 * a], X[3 * c + 1] - X[3 * a + 1], X[3 * c + 2] - X[3 * a + 2]};
+  const double cx = d21[1] * d31[2] - d31[1] * d21[2], cy = -d21[0] * d31[2] + d31[0] * d21[2], cz = d21[0] * d31[1] - d31[0] * d21[1];
+  return 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+}
+
 static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const BiofemParams &prm,
                            std::vector<int> &einfo, std::vector<int> &ecorner, std::vector<long long> &kofs, std::vector<unsigned char> &rowkind,
                            std::vector<int> &rptr, std::vector<int> &ridx, std::vector<int> &pptr, std::vector<int> &pidx,
@@ -287,14 +300,13 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
       }
     }
   }
-  /* pressure gather lists: element corners */
+  /* corner lists (pressure load, dynamic term): elements having the node
+     as a corner, in element order */
   pptr.assign(nt + 1, 0);
-  if (prm.pressure != 0.0) {
-    for (int e = 0; e < ne; e++) for (int k = 0; k < 3; k++) pptr[T.tri_all[3 * (size_t)e + k] + 1]++;
-  }
+  for (int e = 0; e < ne; e++) for (int k = 0; k < 3; k++) pptr[T.tri_all[3 * (size_t)e + k] + 1]++;
   for (int i = 0; i < nt; i++) pptr[i + 1] += pptr[i];
   pidx.assign(pptr[nt], 0);
-  if (prm.pressure != 0.0) {
+  {
     std::vector<int> fill(pptr.begin(), pptr.end() - 1);
     for (int e = 0; e < ne; e++) for (int k = 0; k < 3; k++) pidx[fill[T.tri_all[3 * (size_t)e + k]]++] = e;
   }
@@ -378,16 +390,9 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
       for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) colpos[m->colind[k]] = -1;
     }
   }
-  /* dA0 on the host too (GetGpuTopology); same expression as AreaNormal */
+  /* dA0 on the host too (GetGpuTopology) */
   m->dA0.assign(ne, 0.0);
-  for (int e = 0; e < ne; e++) {
-    const double *X = T.xyz0_full.data();
-    const int a = T.tri_all[3 * (size_t)e], b = T.tri_all[3 * (size_t)e + 1], c = T.tri_all[3 * (size_t)e + 2];
-    const double d21[3] = {X[3 * b] - X[3 * a], X[3 * b + 1] - X[3 * a + 1], X[3 * b + 2] - X[3 * a + 2]};
-    const double d31[3] = {X[3 * c] - X[3 * a], X[3 * c + 1] - X[3 * a + 1], X[3 * c + 2] - X[3 * a + 2]};
-    const double cx = d21[1] * d31[2] - d31[1] * d21[2], cy = -d21[0] * d31[2] + d31[0] * d21[2], cz = d21[0] * d31[1] - d31[0] * d21[1];
-    m->dA0[e] = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
-  }
+  for (int e = 0; e < ne; e++) m->dA0[e] = tri_area0(T, e);
   return 0;
 }
 
@@ -555,6 +560,7 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   }
   dm.eref = d_eref;
   dm.erefF = d_erefF;
+  m->d_fib = d_fib;
   CUDA_TRY(cudaMemsetAsync(dm.status, 0, sizeof(int), m->st));
   CUDA_TRY(cudaMemsetAsync(dm.fp, 0, 3 * sizeof(double) * (size_t)ne, m->st));
   /* reference positions (ghosts included) -> one-time reference geometry */
@@ -846,6 +852,111 @@ int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *op
   int rc = RunGpuNewtonSolveDevice(m, dx, &o, stats, m->st);
   if (rc) return rc;
   CUDA_TRY(cudaMemcpyAsync(x, dx, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
+  CUDA_TRY(cudaStreamSynchronize(m->st));
+  return 0;
+}
+
+/* ---------------- dynamic term and time-dependent activation ---------------- */
+int SetGpuDynamics(BiofemGpuMesh *m, const BiofemDynParams *d)
+{
+  if (!m) return fail(85, "null argument");
+  if (!m->dm.patch) return fail(58, "host-only handle");
+  KParams &kp = m->kp;
+  if (!d) { kp.dyn = 0; return 0; }
+  if (!(d->dt > 0.0) || d->rho < 0.0 || (d->timeinteg != 0 && d->timeinteg != 1))
+    return fail(62, "dynamic parameters out of range");
+  const size_t n = 3 * (size_t)kp.nt;
+  if (!m->dm.xn) {
+    /* lumped mass over every triangle (FDynamic's serial loop runs over
+       n_elmt + 2 n_ghosts): flat reference areas and, per node, its corner
+       triangles in triangle order */
+    const HostTopo &T = m->topo;
+    const int ntri = T.n_elmt + 2 * T.n_ghosts, nt = kp.nt;
+    std::vector<double> area(ntri);
+    for (int t = 0; t < ntri; t++) area[t] = tri_area0(T, t);
+    std::vector<int> dptr(nt + 1, 0), didx(3 * (size_t)ntri);
+    for (int t = 0; t < ntri; t++) for (int k = 0; k < 3; k++) dptr[T.tri_all[3 * (size_t)t + k] + 1]++;
+    for (int i = 0; i < nt; i++) dptr[i + 1] += dptr[i];
+    std::vector<int> fill(dptr.begin(), dptr.end() - 1);
+    for (int t = 0; t < ntri; t++) for (int k = 0; k < 3; k++) didx[fill[T.tri_all[3 * (size_t)t + k]]++] = t;
+    int rc;
+    if ((rc = dalloc(m, &m->dm.xn, n)) || (rc = dalloc(m, &m->dm.xnm1, n)) || (rc = dalloc(m, &m->dm.xd, n)) ||
+        (rc = dalloc(m, &m->dm.xdd, n)) || (rc = dalloc(m, &m->dm.dyn_diag, (size_t)nt)) ||
+        (rc = dupload(m, &m->dm.dA0, area)) || (rc = dupload(m, &m->dm.dptr, dptr)) || (rc = dupload(m, &m->dm.didx, didx)))
+      return rc;
+    CUDA_TRY(cudaStreamSynchronize(m->st));   /* the host vectors above go out of scope */
+  }
+  /* Init (main.c:1515-1540): xn = xnm1 = x = the reference coordinates, xd = xdd = 0 */
+  CUDA_TRY(cudaMemcpyAsync(m->dm.xn, m->dm.X, n * sizeof(double), cudaMemcpyDeviceToDevice, m->st));
+  CUDA_TRY(cudaMemcpyAsync(m->dm.xnm1, m->dm.X, n * sizeof(double), cudaMemcpyDeviceToDevice, m->st));
+  CUDA_TRY(cudaMemsetAsync(m->dm.xd, 0, n * sizeof(double), m->st));
+  CUDA_TRY(cudaMemsetAsync(m->dm.xdd, 0, n * sizeof(double), m->st));
+  /* the constants of FDynamic (main.c:1171-1176) and xAccVel (main.c:1383-1385) */
+  const double dt = d->dt, G = d->newmark_gamma, B = 0.25 * (G + 0.5) * (G + 0.5);
+  kp.dyn = 1; kp.dyn_central = d->timeinteg; kp.dyn_damp = d->damping != 0;
+  kp.dyn_rhoh0 = d->rho * m->prm.h0; kp.dyn_dt = dt; kp.dyn_dampf = d->dampfactor;
+  kp.dyn_M1 = 1. / (B * std::pow(dt, 2)); kp.dyn_M2 = 1. / (B * dt); kp.dyn_M3 = (1. / (2 * B)) - 1.;
+  kp.dyn_C1 = G / (B * dt); kp.dyn_C2 = (G / B) - 1; kp.dyn_C3 = dt * (G / (2. * B) - 1);
+  kp.dyn_U2 = (1. - G) * dt; kp.dyn_U3 = G * dt;
+  int rc = launch_dyn_diag(m->dm, kp, m->st);
+  if (rc) return fail(76, std::string("dynamic diagonal launch: ") + cudaGetErrorString((cudaError_t)rc));
+  CUDA_TRY(cudaStreamSynchronize(m->st));
+  return 0;
+}
+
+int SetGpuDynamicState(BiofemGpuMesh *m, const double *xn, const double *xnm1, const double *xd, const double *xdd)
+{
+  if (!m) return fail(85, "null argument");
+  if (!m->dm.xn) return fail(58, "dynamics not enabled (SetGpuDynamics)");
+  const size_t bytes = 3 * sizeof(double) * (size_t)m->kp.nt;
+  const double *src[4] = {xn, xnm1, xd, xdd};
+  double *dst[4] = {m->dm.xn, m->dm.xnm1, m->dm.xd, m->dm.xdd};
+  for (int k = 0; k < 4; k++)
+    if (src[k]) CUDA_TRY(cudaMemcpyAsync(dst[k], src[k], bytes, cudaMemcpyHostToDevice, m->st));
+  CUDA_TRY(cudaStreamSynchronize(m->st));
+  return 0;
+}
+
+int GetGpuDynamicState(BiofemGpuMesh *m, double *xn, double *xnm1, double *xd, double *xdd)
+{
+  if (!m) return fail(85, "null argument");
+  if (!m->dm.xn) return fail(58, "dynamics not enabled (SetGpuDynamics)");
+  const size_t bytes = 3 * sizeof(double) * (size_t)m->kp.nt;
+  double *dst[4] = {xn, xnm1, xd, xdd};
+  const double *src[4] = {m->dm.xn, m->dm.xnm1, m->dm.xd, m->dm.xdd};
+  for (int k = 0; k < 4; k++)
+    if (dst[k]) CUDA_TRY(cudaMemcpyAsync(dst[k], src[k], bytes, cudaMemcpyDeviceToHost, m->st));
+  CUDA_TRY(cudaStreamSynchronize(m->st));
+  return 0;
+}
+
+int RunGpuDynamicUpdate(BiofemGpuMesh *m, const double *x)
+{
+  if (!m || !x) return fail(85, "null argument");
+  if (!m->dm.xn) return fail(58, "dynamics not enabled (SetGpuDynamics)");
+  const size_t n = 3 * (size_t)m->kp.nt;
+  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
+  int rc = launch_dyn_update(m->dm, m->kp, m->d_x, m->st);
+  if (rc) return fail(76, std::string("dynamic update launch: ") + cudaGetErrorString((cudaError_t)rc));
+  CUDA_TRY(cudaStreamSynchronize(m->st));
+  return 0;
+}
+
+int SetGpuElementGamma(BiofemGpuMesh *m, const double *gamma_e)
+{
+  if (!m || !gamma_e) return fail(85, "null argument");
+  if (!m->dm.patch) return fail(58, "host-only handle");
+  const int ne = m->kp.ne;
+  if (!m->d_gam) { int rc = dalloc(m, &m->d_gam, (size_t)ne); if (rc) return rc; }
+  CUDA_TRY(cudaMemcpyAsync(m->d_gam, gamma_e, sizeof(double) * ne, cudaMemcpyHostToDevice, m->st));
+  /* reference constants with gamma_e in place of gamma * gamma_scale */
+  KParams kp = m->kp;
+  kp.gamma = 1.0;
+  int rc = launch_positions(m->dm, kp, m->dm.X, m->st);
+  if (!rc) rc = launch_ref_prep(m->dm, kp, m->d_fib, m->d_gam, const_cast<double *>(m->dm.eref), m->st);
+  const size_t nref = (size_t)(kRefPerQp * kp.nq + kRefPerElem) * ne;
+  if (!rc && m->dm.erefF) rc = launch_to_float(m->dm.eref, const_cast<float *>(m->dm.erefF), (long long)nref, m->st);
+  if (rc) return fail(76, std::string("activation update launch: ") + cudaGetErrorString((cudaError_t)rc));
   CUDA_TRY(cudaStreamSynchronize(m->st));
   return 0;
 }

@@ -450,6 +450,7 @@ __global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K)
       comp = (tt - s) - yv;
       s = tt;
     }
+    if (p.dyn && m.colind[k] == row && (w == 0 || w == 4 || w == 8)) s += (float)m.dyn_diag[row];
   }
   K[t] = s;
 }
@@ -481,15 +482,39 @@ __global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x
       const size_t base = (size_t)m.ridx[c];   /* 3*slot*ne + e */
       fi[0] += m.fb[base]; fi[1] += m.fb[base + ne]; fi[2] += m.fb[base + 2 * ne];
     }
-    for (int c = m.pptr[i]; c < m.pptr[i + 1]; c++) {
-      const size_t e = (size_t)m.pidx[c];
-      fe[0] += m.fp[e]; fe[1] += m.fp[ne + e]; fe[2] += m.fp[2 * ne + e];
-    }
+    if (p.pressure != 0.0)
+      for (int c = m.pptr[i]; c < m.pptr[i + 1]; c++) {
+        const size_t e = (size_t)m.pidx[c];
+        fe[0] += m.fp[e]; fe[1] += m.fp[ne + e]; fe[2] += m.fp[2 * ne + e];
+      }
     const int kind = m.rowkind[i];
+    /* FDynamic (main.c:1293-1360, the serial path): triangle-order sum of the
+       node's inertial (and damping) force over every triangle with this
+       corner, ghost and bridging triangles included */
+    double fd[3] = {0.0, 0.0, 0.0};
+    if (p.dyn && kind == 0) {
+      for (int c = m.dptr[i]; c < m.dptr[i + 1]; c++) {
+        const double M = p.dyn_rhoh0 * m.dA0[m.didx[c]] / 3;
+        const double C = p.dyn_damp ? p.dyn_dampf * M : 0.0;
+        for (int d = 0; d < 3; d++) {
+          const size_t o = 3 * (size_t)i + d;
+          double f;
+          if (!p.dyn_central) {
+            const double facc = M * (p.dyn_M1 * m.xn[o] + p.dyn_M2 * m.xd[o] + p.dyn_M3 * m.xdd[o]);
+            const double fvel = C * (p.dyn_C1 * m.xn[o] + p.dyn_C2 * m.xd[o] + p.dyn_C3 * m.xdd[o]);
+            f = M * p.dyn_M1 * x[o] + C * p.dyn_C1 * x[o] - facc - fvel;
+          } else {
+            f = M * (x[o] - 2 * m.xn[o] + m.xnm1[o]) / (p.dyn_dt * p.dyn_dt) + C * (x[o] - m.xn[o]) / p.dyn_dt;
+          }
+          fd[d] += f;
+        }
+      }
+    }
     for (int d = 0; d < 3; d++) {
       double r;
       if (kind == 2) r = 0.0;
       else if (kind == 1) r = x[3 * (size_t)i + d] - m.X[3 * (size_t)i + d];
+      else if (p.dyn) r = (-1.0 * fe[d] + fi[d]) + 1. * fd[d];
       else r = -1.0 * fe[d] + fi[d];
       R[3 * (size_t)i + d] = r;
       const unsigned long long b = abs_bits(fe[d]);
@@ -522,6 +547,7 @@ __global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
       if (id >= 0) s += m.ke[(size_t)id * 9 + w];
       else s -= m.ke[(size_t)(-(id + 1)) * 9 + w];
     }
+    if (p.dyn && m.colind[k] == row && (w == 0 || w == 4 || w == 8)) s += m.dyn_diag[row];
   }
   K[t] = s;
 }
@@ -597,6 +623,49 @@ __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, 
 int launch_to_float(const double *a, float *b, long long n, void *stream)
 {
   k_to_float<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(a, b, n);
+  return (int)cudaGetLastError();
+}
+
+/* d Fdyn / d x: per free node, the triangle-order sum over its corner
+   triangles of M M1 + C C1 (Newmark) or M / dt^2 + C / dt (central) */
+__global__ void k_dyn_diag(DevMesh m, KParams p)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.nt) return;
+  double s = 0.0;
+  if (m.rowkind[i] == 0) {
+    for (int c = m.dptr[i]; c < m.dptr[i + 1]; c++) {
+      const double M = p.dyn_rhoh0 * m.dA0[m.didx[c]] / 3;
+      const double C = p.dyn_damp ? p.dyn_dampf * M : 0.0;
+      s += p.dyn_central ? M / (p.dyn_dt * p.dyn_dt) + C / p.dyn_dt : M * p.dyn_M1 + C * p.dyn_C1;
+    }
+  }
+  m.dyn_diag[i] = s;
+}
+
+/* xAccVel (main.c:1367-1412, the serial path over n_v + n_ghosts nodes),
+   then xnm1 <- xn, xn <- x (main.c:571-572) */
+__global__ void k_dyn_update(DevMesh m, KParams p, const double *__restrict__ x)
+{
+  const size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (j >= 3 * (size_t)p.nt) return;
+  const double xddn = m.xdd[j];
+  const double a = p.dyn_M1 * (x[j] - m.xn[j]) - p.dyn_M2 * m.xd[j] - p.dyn_M3 * m.xdd[j];
+  m.xdd[j] = a;
+  m.xd[j] = m.xd[j] + p.dyn_U2 * xddn + p.dyn_U3 * a;
+  m.xnm1[j] = m.xn[j];
+  m.xn[j] = x[j];
+}
+
+int launch_dyn_diag(const DevMesh &m, const KParams &p, void *stream)
+{
+  k_dyn_diag<<<blocks_for(p.nt, 256), 256, 0, (cudaStream_t)stream>>>(m, p);
+  return (int)cudaGetLastError();
+}
+
+int launch_dyn_update(const DevMesh &m, const KParams &p, const double *x, void *stream)
+{
+  k_dyn_update<<<blocks_for(3LL * p.nt, 256), 256, 0, (cudaStream_t)stream>>>(m, p, x);
   return (int)cudaGetLastError();
 }
 

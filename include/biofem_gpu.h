@@ -189,6 +189,31 @@ int RunGpuNewtonSolve(BiofemGpuMesh *m, double *x, const BiofemNewtonOptions *op
 int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOptions *opt, BiofemNewtonStats *stats,
                             void *stream);
 
+/* Dynamic term and time stepping (main.c:420-567, FDynamic main.c:1157-1290,
+   Mass/Damp material.c:100-139, xAccVel main.c:1367-1412).  With dynamics
+   on, R = (Fint - Fext) + Fdyn and K gains d Fdyn / dx on the diagonal:
+   per element and corner M = rho h0 A0 / 3 (A0 the flat reference area),
+   C = dampfactor M when damping, and with beta = (gamma_nm + 1/2)^2 / 4
+     Newmark (timeinteg 0): Fd = M M1 x + C C1 x - M (M1 xn + M2 xd + M3 xdd)
+                                  - C (C1 xn + C2 xd + C3 xdd),
+     central (timeinteg 1): Fd = M (x - 2 xn + xnm1) / dt^2 + C (x - xn) / dt.
+   SetGpuDynamics(m, NULL) switches the term off; the state (3*(n_v+n_ghosts)
+   each) starts at zero and is set or read with the state calls (NULL entries
+   are skipped).  RunGpuDynamicUpdate(m, x) ends a step from the converged x:
+   acceleration and velocity updates on the real nodes, then xnm1 <- xn,
+   xn <- x.  SetGpuElementGamma(m, g) recomputes the per-element activation
+   constants with g[e] in place of gamma * gamma_scale[e] (the value of
+   GammaOfTimeDelayed times gamma_scale, active_strain.c:1156-1212). */
+typedef struct {
+  double  dt, rho, newmark_gamma, dampfactor;
+  int32_t timeinteg, damping;
+} BiofemDynParams;
+int SetGpuDynamics(BiofemGpuMesh *m, const BiofemDynParams *params);
+int SetGpuDynamicState(BiofemGpuMesh *m, const double *xn, const double *xnm1, const double *xd, const double *xdd);
+int GetGpuDynamicState(BiofemGpuMesh *m, double *xn, double *xnm1, double *xd, double *xdd);
+int RunGpuDynamicUpdate(BiofemGpuMesh *m, const double *x);
+int SetGpuElementGamma(BiofemGpuMesh *m, const double *gamma_e);
+
 /* Serving loop for load-step requests (new; the reference runs each case as
    a separate batch job, bin/biofem:352-456).  Continuous batching: requests
    are admitted first-fit in arrival order whenever one of max_slots slots is

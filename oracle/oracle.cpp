@@ -655,10 +655,22 @@ static int elem_forces(const Mesh &m, const Params &P, int ec, const RefElem &R,
 }
 
 /* ---------------- whole-residual restatement ---------------- */
+/* Time integration state of FDynamic / xAccVel (main.c:1157-1412).
+   Newmark's Beta is tied to Gama, Beta = (Gama + 1/2)^2 / 4 (main.c:1171). */
+struct Dyn {
+  bool on = false;
+  int central = 0, damp = 0;
+  double dt = 0, rhoh0 = 0, dampf = 0;
+  double M1 = 0, M2 = 0, M3 = 0, C1 = 0, C2 = 0, C3 = 0, U2 = 0, U3 = 0;
+  std::vector<double> dA0;                 /* flat reference area, n_elmt + 2 n_ghosts triangles */
+  std::vector<double> xn, xnm1, xd, xdd;   /* 3 (n_v + n_ghosts) */
+};
+
 struct Body {
   Mesh m;
   Params P;
   std::vector<RefElem> ref;
+  Dyn D;
   bool ready = false;
 };
 
@@ -742,8 +754,35 @@ static int residual(const Body &B, const T *x, T *R, T *Fint_out = nullptr, T *F
       }
     }
   }
-  /* R = -1*Fext + Fint (+ Fdyn = 0), main.c:844-845 */
-  for (int i = 0; i < ndof; i++) R[i] = (-1. * Fext[i] + Fint[i]) + 1. * T(0.0);
+  /* FDynamic, main.c:1157-1360 (serial path): every triangle, ghosts and
+     bridging triangles included, adds M (M1 x - ...) per corner, M = rho h0 dA0 / 3
+     (Mass, material.c:100-119) and C = dampfactor M (Damp, material.c:122-137). */
+  std::vector<T> Fdyn(ndof, T(0.0));
+  if (B.D.on) {
+    const Dyn &D = B.D;
+    const T *xc[3] = {xb.data(), yb.data(), zb.data()};
+    for (int ec = 0; ec < m.n_elmt + 2 * m.n_ghosts; ec++) {
+      const double M = D.rhoh0 * D.dA0[ec] / 3;
+      const double C = D.damp ? D.dampf * M : 0.0;
+      const int c[3] = {m.nv1[ec], m.nv2[ec], m.nv3[ec]};
+      for (int k = 0; k < 3; k++)
+        for (int d = 0; d < 3; d++) {
+          const int o = 3 * c[k] + d;
+          const T xv = xc[d][c[k]];
+          T f;
+          if (!D.central) {
+            const double facc = M * (D.M1 * D.xn[o] + D.M2 * D.xd[o] + D.M3 * D.xdd[o]);
+            const double fvel = C * (D.C1 * D.xn[o] + D.C2 * D.xd[o] + D.C3 * D.xdd[o]);
+            f = M * D.M1 * xv + C * D.C1 * xv - facc - fvel;
+          } else {
+            f = M * (xv - 2 * D.xn[o] + D.xnm1[o]) / (D.dt * D.dt) + C * (xv - D.xn[o]) / D.dt;
+          }
+          Fdyn[o] = Fdyn[o] + f;
+        }
+    }
+  }
+  /* R = -1*Fext + Fint + 1*Fdyn, main.c:844-845 */
+  for (int i = 0; i < ndof; i++) R[i] = (-1. * Fext[i] + Fint[i]) + 1. * Fdyn[i];
   /* EdgeDirectionalFix(0, d), external.c:1706-1741: R := x_bp - x_bp0 */
   if (B.P.clamp && m.n_edge > 0) {
     for (int nbc = 0; nbc < m.n_bnodes[0]; nbc++) {
@@ -878,6 +917,98 @@ int oracle_setup_given_topology(int n_v, int n_elmt, const int *tri_all, const d
 }
 
 int oracle_set_threads(int n) { g_threads = n > 0 ? n : 1; return 0; }
+
+/* Switch the dynamic term on (dt > 0) or off (dt <= 0): the -dt, -rho,
+   -newmark_gamma, -dampfactor, -timeinteg, -damping options of main.c.
+   The state starts at xn = xnm1 = the reference coordinates, xd = xdd = 0. */
+int oracle_set_dynamics(double dt, double rho, double newmark_gamma, double dampfactor, int timeinteg, int damping)
+{
+  if (!g_body || !g_body->ready) return 58;
+  Body &B = *g_body;
+  const Mesh &m = B.m;
+  Dyn &D = B.D;
+  if (!(dt > 0.0)) { D = Dyn(); return 0; }
+  if (timeinteg != 0 && timeinteg != 1) return 66;
+  const double G = newmark_gamma, Be = 0.25 * (G + 0.5) * (G + 0.5);
+  D.on = true; D.central = timeinteg; D.damp = damping != 0;
+  D.dt = dt; D.rhoh0 = rho * B.P.h0; D.dampf = dampfactor;
+  /* FDynamic's constants (main.c:1175-1176) and xAccVel's velocity update
+     weights (main.c:1383-1385) */
+  D.M1 = 1. / (Be * pow(dt, 2)); D.M2 = 1. / (Be * dt); D.M3 = (1. / (2 * Be)) - 1.;
+  D.C1 = G / (Be * dt); D.C2 = (G / Be) - 1; D.C3 = dt * (G / (2. * Be) - 1);
+  D.U2 = (1. - G) * dt; D.U3 = G * dt;
+  const int ntri = m.n_elmt + 2 * m.n_ghosts, ntot = m.n_v + m.n_ghosts;
+  D.dA0.assign(ntri, 0.0);
+  for (int ec = 0; ec < ntri; ec++) {
+    double dA; V3<double> n;
+    area_normal(m, m.x0.data(), m.y0.data(), m.z0.data(), ec, dA, n);
+    D.dA0[ec] = dA;
+  }
+  D.xn.assign(3 * (size_t)ntot, 0.0);
+  for (int v = 0; v < ntot; v++) { D.xn[3 * v] = m.x0[v]; D.xn[3 * v + 1] = m.y0[v]; D.xn[3 * v + 2] = m.z0[v]; }
+  D.xnm1 = D.xn;
+  D.xd.assign(3 * (size_t)ntot, 0.0);
+  D.xdd.assign(3 * (size_t)ntot, 0.0);
+  return 0;
+}
+
+/* Any of the four may be null (left unchanged); each has 3 (n_v + n_ghosts) entries. */
+int oracle_set_dynamic_state(const double *xn, const double *xnm1, const double *xd, const double *xdd)
+{
+  if (!g_body || !g_body->ready || !g_body->D.on) return 58;
+  Dyn &D = g_body->D;
+  const size_t n = D.xn.size();
+  if (xn) std::copy(xn, xn + n, D.xn.begin());
+  if (xnm1) std::copy(xnm1, xnm1 + n, D.xnm1.begin());
+  if (xd) std::copy(xd, xd + n, D.xd.begin());
+  if (xdd) std::copy(xdd, xdd + n, D.xdd.begin());
+  return 0;
+}
+
+int oracle_get_dynamic_state(double *xn, double *xnm1, double *xd, double *xdd)
+{
+  if (!g_body || !g_body->ready || !g_body->D.on) return 58;
+  const Dyn &D = g_body->D;
+  std::copy(D.xn.begin(), D.xn.end(), xn);
+  std::copy(D.xnm1.begin(), D.xnm1.end(), xnm1);
+  std::copy(D.xd.begin(), D.xd.end(), xd);
+  std::copy(D.xdd.begin(), D.xdd.end(), xdd);
+  return 0;
+}
+
+/* xAccVel (main.c:1367-1412, serial path over n_v + n_ghosts nodes), then
+   xnm1 <- xn, xn <- x (main.c:571-572). */
+int oracle_dynamic_update(const double *x)
+{
+  if (!g_body || !g_body->ready || !g_body->D.on) return 58;
+  Dyn &D = g_body->D;
+  const size_t n = D.xn.size();
+  for (size_t j = 0; j < n; j++) {
+    const double xddn = D.xdd[j];
+    D.xdd[j] = D.M1 * (x[j] - D.xn[j]) - D.M2 * D.xd[j] - D.M3 * D.xdd[j];
+    D.xd[j] = D.xd[j] + D.U2 * xddn + D.U3 * D.xdd[j];
+  }
+  D.xnm1 = D.xn;
+  std::copy(x, x + n, D.xn.begin());
+  return 0;
+}
+
+/* Per-element activation gamma_e (ElemActDefGrad, active_strain.c:1207-1212:
+   GammaOfTimeDelayed(delay_e) * gamma_scale_e), taken as given: the body's
+   scalar gamma becomes 1 and gamma_scale the caller's values; the reference
+   geometry per element is rebuilt. */
+int oracle_set_element_gamma(const double *gamma_e)
+{
+  if (!g_body || !g_body->ready) return 58;
+  Body &B = *g_body;
+  B.P.gamma = 1.0;
+  B.m.gscale.assign(gamma_e, gamma_e + B.m.n_elmt);
+  for (int ec = 0; ec < B.m.n_elmt; ec++) {
+    int rc = ref_elem(B.m, B.P, ec, B.ref[ec]);
+    if (rc) return rc;
+  }
+  return 0;
+}
 
 int oracle_sizes(int *n_ghosts, int *n_dof)
 {

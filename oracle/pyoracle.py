@@ -95,6 +95,48 @@ class _Base:
 class Oracle(_Base):
     prefix = "oracle"
 
+    # ---- dynamic term (FDynamic / xAccVel) and per-element activation ----
+    def set_dynamics(self, dt=None, rho=0.0, newmark_gamma=0.5, dampfactor=0.0, timeinteg=0, damping=0):
+        f = self.lib.oracle_set_dynamics
+        f.argtypes = [_c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_int]
+        rc = f(0.0 if dt is None else float(dt), rho, newmark_gamma, dampfactor, int(timeinteg), int(damping))
+        if rc:
+            raise RuntimeError(f"oracle_set_dynamics failed with code {rc}")
+
+    def set_dynamic_state(self, xn=None, xnm1=None, xd=None, xdd=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (xn, xnm1, xd, xdd)]
+        f = self.lib.oracle_set_dynamic_state
+        f.argtypes = [_vp] * 4
+        rc = f(*[None if a is None else _p(a) for a in arrs])
+        if rc:
+            raise RuntimeError(f"oracle_set_dynamic_state failed with code {rc}")
+
+    def dynamic_state(self):
+        out = [np.zeros(self.n_dof) for _ in range(4)]
+        f = self.lib.oracle_get_dynamic_state
+        f.argtypes = [_vp] * 4
+        rc = f(*[_p(a) for a in out])
+        if rc:
+            raise RuntimeError(f"oracle_get_dynamic_state failed with code {rc}")
+        return dict(zip(("xn", "xnm1", "xd", "xdd"), out))
+
+    def dynamic_update(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        f = self.lib.oracle_dynamic_update
+        f.argtypes = [_vp]
+        rc = f(_p(x))
+        if rc:
+            raise RuntimeError(f"oracle_dynamic_update failed with code {rc}")
+
+    def set_element_gamma(self, gamma_e):
+        g = np.ascontiguousarray(gamma_e, dtype=np.float64)
+        assert g.size == self.n_elmt
+        f = self.lib.oracle_set_element_gamma
+        f.argtypes = [_vp]
+        rc = f(_p(g))
+        if rc:
+            raise RuntimeError(f"oracle_set_element_gamma failed with code {rc}")
+
     def __init__(self, build: bool = True):
         from . import build_oracle  # type: ignore
         path = build_oracle.build() if build else build_oracle.LIB
@@ -230,11 +272,14 @@ class Oracle(_Base):
         J = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows_i), np.concatenate(cols_j))), shape=(n, n))
         return J, len(colors)
 
-    def newton(self, x0: np.ndarray, topo, rtol: float = 1e-10, max_it: int = 30, verbose: bool = False):
+    def newton(self, x0: np.ndarray, topo, rtol: float = 1e-10, max_it: int = 30, verbose: bool = False,
+               jacobian_its: int | None = None):
         """Newton load step on the oracle residual with its exact sparse
         Jacobian (ghost rows/columns replaced by identity) and a direct solve;
         backtracking on ||R|| as the GPU solver does.  The converged state
-        depends only on R."""
+        depends only on R.  ``jacobian_its`` = k rebuilds the Jacobian on the
+        first k iterations only and then keeps its factorisation (a chord
+        iteration: cheaper, linearly convergent, same root)."""
         import scipy.sparse as sp
         import scipy.sparse.linalg as spla
         x = np.array(x0, dtype=np.float64)
@@ -246,11 +291,13 @@ class Oracle(_Base):
             rn = np.linalg.norm(R)
             if rn <= rtol * r0:
                 break
-            J, _ = self.sparse_jacobian(x, topo)
-            J = J.tolil()
-            for i in range(nreal, self.n_dof):
-                J[i, i] = 1.0
-            dx = spla.spsolve(J.tocsc(), -R)
+            if jacobian_its is None or it < jacobian_its:
+                J, _ = self.sparse_jacobian(x, topo)
+                J = J.tolil()
+                for i in range(nreal, self.n_dof):
+                    J[i, i] = 1.0
+                lu = spla.splu(J.tocsc())
+            dx = lu.solve(-R)
             dx[nreal:] = 0.0
             alpha = 1.0
             for _ in range(12):
