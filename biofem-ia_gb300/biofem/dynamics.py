@@ -95,13 +95,18 @@ class StepRecord:
 
 
 def time_loop(shell: GpuShell, mesh, x0: np.ndarray, dyn: Dynamics, act: Activation, tisteps: int,
-              tistart: int = 0, delay=None, on_step=None, **newton):
-    """Run ``tisteps`` implicit steps from x0 on a prepared GpuShell.
+              tistart: int = 0, delay=None, on_step=None, pre_update=None, reset_state: bool = True, **newton):
+    """Run ``tisteps`` implicit steps (ti = tistart .. tistart + tisteps - 1) from
+    x0 on a prepared GpuShell.
 
-    ``on_step(ti, x, record)`` is called after every step (for output).
-    Returns (x, [StepRecord]).
+    ``pre_update(ti, x)`` is called with the step's solution before xAccVel,
+    ``on_step(ti, x, record)`` after it (for output).  ``reset_state`` = False
+    keeps the dynamic state already on the shell (a restart).  The ramps'
+    default period is ``tisteps * dt`` as in the reference, where tisteps is
+    the run's step count.  Returns (x, [StepRecord]).
     """
-    dyn.apply(shell)
+    if reset_state:
+        dyn.apply(shell)
     x = np.array(x0, dtype=np.float64, copy=True)
     records = []
     for ti in range(tistart, tistart + tisteps):
@@ -113,6 +118,8 @@ def time_loop(shell: GpuShell, mesh, x0: np.ndarray, dyn: Dynamics, act: Activat
         except BiofemError as e:
             x_new, st, ok = x, dict(getattr(e, "stats", {}) or {}, error=str(e)), False
         x = x_new
+        if pre_update is not None:
+            pre_update(ti, x)
         shell.dynamic_update(x)
         rec = StepRecord(ti, float(np.mean(g)), ok, st)
         records.append(rec)

@@ -31,6 +31,8 @@ BIOFEM_PC_AMG = 0
 BIOFEM_PC_BJACOBI = 1
 BIOFEM_FP64 = 0
 BIOFEM_FP32_BULK = 1
+BIOFEM_CKPT_VERTEX_ORDER = 0
+BIOFEM_CKPT_VEC = 1
 
 _i32p = ctypes.POINTER(ctypes.c_int32)
 _f64p = ctypes.POINTER(ctypes.c_double)
@@ -72,6 +74,14 @@ class DynParams(ctypes.Structure):
                 ("dampfactor", ctypes.c_double), ("timeinteg", ctypes.c_int32), ("damping", ctypes.c_int32)]
 
 
+class SurfaceFields(ctypes.Structure):
+    _fields_ = [("n_v", ctypes.c_int32), ("n_elmt", ctypes.c_int32), ("tri", ctypes.c_void_p),
+                ("x", ctypes.c_void_p), ("X", ctypes.c_void_p), ("mass", ctypes.c_void_p),
+                ("Fint", ctypes.c_void_p), ("Fext", ctypes.c_void_p), ("Fdyn", ctypes.c_void_p),
+                ("xd", ctypes.c_void_p), ("dA0", ctypes.c_void_p), ("gamma_e", ctypes.c_void_p),
+                ("fib", ctypes.c_void_p)]
+
+
 class NewtonStats(ctypes.Structure):
     _fields_ = [("newton_its", ctypes.c_int32), ("gmres_its_total", ctypes.c_int32), ("gmres_its_last", ctypes.c_int32),
                 ("residual_evals", ctypes.c_int32), ("jacobian_evals", ctypes.c_int32), ("converged", ctypes.c_int32),
@@ -96,7 +106,8 @@ EXPORTS = ["InitGpuWorkspace", "DestroyGpuWorkspace", "PrepareGpuMesh", "Destroy
            "RunGpuNewtonSolveDevice", "PrepareGpuMeshOnStream", "ServeCreate", "ServeSubmit", "ServeWait",
            "ServeStatsGet", "ServeDestroy", "BiofemServeEstimateBytes", "GetGpuBasisTablesKind",
            "SetGpuDynamics", "SetGpuDynamicState", "GetGpuDynamicState", "RunGpuDynamicUpdate",
-           "SetGpuElementGamma"]
+           "SetGpuElementGamma", "RunGpuResidualParts", "RunGpuElementThickness", "BiofemLocationOut",
+           "BiofemLocationIn", "BiofemWriteSurfaceVTK", "BiofemWriteShell3dVTK"]
 
 
 def load_library(path: Path | str | None = None) -> ctypes.CDLL:
@@ -140,6 +151,13 @@ def load_library(path: Path | str | None = None) -> ctypes.CDLL:
     lib.GetGpuDynamicState.argtypes = [vp, vp, vp, vp, vp]
     lib.RunGpuDynamicUpdate.argtypes = [vp, vp]
     lib.SetGpuElementGamma.argtypes = [vp, vp]
+    lib.RunGpuResidualParts.argtypes = [vp, vp, vp, vp, vp, vp]
+    lib.RunGpuElementThickness.argtypes = [vp, vp, vp]
+    i32, i64, cp = ctypes.c_int32, ctypes.c_int64, ctypes.c_char_p
+    lib.BiofemLocationOut.argtypes = [cp, i32, i32, i64, vp, vp, vp, vp, i32]
+    lib.BiofemLocationIn.argtypes = [cp, i32, i32, i64, vp, vp, vp, vp]
+    lib.BiofemWriteSurfaceVTK.argtypes = [cp, i32, i32, ctypes.POINTER(SurfaceFields)]
+    lib.BiofemWriteShell3dVTK.argtypes = [cp, i32, i32, i32, i32, vp, vp, vp]
     lib.ServeCreate.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(vp)]
     lib.ServeSubmit.argtypes = [vp, ctypes.POINTER(MeshDesc), ctypes.POINTER(Params), ctypes.POINTER(NewtonOptions),
                                 vp, ctypes.POINTER(ctypes.c_int64)]
@@ -313,6 +331,20 @@ class GpuShell:
         g = np.ascontiguousarray(gamma_e, dtype=np.float64)
         assert g.size == self.info.n_elmt
         _check(self.lib, self.lib.SetGpuElementGamma(self.handle, _ptr(g)))
+
+    # ---- output quantities ----
+    def residual_parts(self, x):
+        """RunGpuResidualParts: (R, Fint, Fext, Fdyn), the forces unscaled."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = [np.empty(self.n_dof) for _ in range(4)]
+        _check(self.lib, self.lib.RunGpuResidualParts(self.handle, _ptr(x), *[_ptr(a) for a in out]))
+        return tuple(out)
+
+    def element_thickness(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        th = np.empty(self.info.n_elmt)
+        _check(self.lib, self.lib.RunGpuElementThickness(self.handle, _ptr(x), _ptr(th)))
+        return th
 
     # ---- device-resident calls (raw CUDA pointers as ints) ----
     def residual_device(self, d_x: int, d_R: int, stream: int = 0):

@@ -90,7 +90,9 @@ int launch_ref_prep(const DevMesh &m, const KParams &p, const double *fib, const
 int launch_positions(const DevMesh &m, const KParams &p, const double *x, void *stream);
 int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream);
 int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream);
-int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream);
+int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream,
+                       double *parts = nullptr);
+int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double *th, void *stream);
 int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream);
 int launch_scale(const DevMesh &m, const KParams &p, double *R, double *K, void *stream);
 int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);

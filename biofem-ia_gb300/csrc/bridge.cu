@@ -170,6 +170,8 @@ static std::mutex g_meshes_mu;
 namespace biofem {
 /* accessors for the no-allocation residual (noalloc.cu) */
 int noalloc_fail(int code, const std::string &msg) { return fail(code, msg); }
+/* the calling thread's last error for the host-only modules (formats.cpp) */
+int host_fail(int code, const std::string &msg) { return fail(code, msg); }
 const DevMesh *mesh_devview(const BiofemGpuMesh *m, const KParams **kp)
 {
   if (!m || !m->dm.patch) return nullptr;
@@ -770,6 +772,51 @@ int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K
   if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
   CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, m->st));
   return BiofemGpuSync(m, m->st);
+}
+
+int RunGpuResidualParts(BiofemGpuMesh *m, const double *x, double *R, double *Fint, double *Fext, double *Fdyn)
+{
+  if (!m || !x) return fail(85, "null argument");
+  if (!m->dm.patch) return fail(58, "host-only handle");
+  const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
+  cudaStream_t st = m->st;
+  double *parts = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **)&parts, 3 * n * sizeof(double), st));
+  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  int rc = launch_positions(m->dm, m->kp, m->d_x, st);
+  if (!rc) rc = launch_elem_residual(m->dm, m->kp, st);
+  if (!rc) rc = launch_node_gather(m->dm, m->kp, m->d_x, m->d_R, st, parts);
+  if (!rc) rc = launch_scale(m->dm, m->kp, m->d_R, nullptr, st);
+  if (rc) {
+    cudaFreeAsync(parts, st);
+    return fail(76, std::string("residual launch: ") + cudaGetErrorString((cudaError_t)rc));
+  }
+  double *out[4] = {R, Fint, Fext, Fdyn};
+  const double *src[4] = {m->d_R, parts, parts + n, parts + 2 * n};
+  for (int k = 0; k < 4; k++)
+    if (out[k]) CUDA_TRY(cudaMemcpyAsync(out[k], src[k], n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaFreeAsync(parts, st));
+  return BiofemGpuSync(m, st);
+}
+
+int RunGpuElementThickness(BiofemGpuMesh *m, const double *x, double *thickness)
+{
+  if (!m || !x || !thickness) return fail(85, "null argument");
+  if (!m->dm.patch) return fail(58, "host-only handle");
+  const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts), ne = (size_t)m->kp.ne;
+  cudaStream_t st = m->st;
+  double *d_th = nullptr;
+  CUDA_TRY(cudaMallocAsync((void **)&d_th, ne * sizeof(double), st));
+  CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  int rc = launch_positions(m->dm, m->kp, m->d_x, st);
+  if (!rc) rc = launch_elem_thickness(m->dm, m->kp, m->prm.h0, d_th, st);
+  if (rc) {
+    cudaFreeAsync(d_th, st);
+    return fail(76, std::string("thickness launch: ") + cudaGetErrorString((cudaError_t)rc));
+  }
+  CUDA_TRY(cudaMemcpyAsync(thickness, d_th, ne * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaFreeAsync(d_th, st));
+  return BiofemGpuSync(m, st);
 }
 
 int FormFunctionFEMGpu(void *snes, const double *x, double *R, void *ctx)

@@ -20,7 +20,7 @@ LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libbiofem_gpu.so"
 OBJ_DIR = LIB_DIR / "obj"
 CUDA_SOURCES = ["kernels.cu", "bridge.cu", "noalloc.cu", "solver.cu", "amg.cu"]
-CXX_SOURCES = ["topology.cpp", "serve.cpp", "amg_setup.cpp"]
+CXX_SOURCES = ["topology.cpp", "serve.cpp", "amg_setup.cpp", "formats.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-pthread"]

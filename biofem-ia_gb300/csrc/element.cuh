@@ -177,7 +177,7 @@ __host__ __device__ __forceinline__ T qform(const T &c00, const T &c11, const T 
 template <class T, class R>
 __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 12 22 */, const QpRef<R> &r,
                                                    R gam, R gamp, R c1, R mu, R K,
-                                                   int iters, T sv[3], int &status)
+                                                   int iters, T sv[3], int &status, T *c33_out = nullptr)
 {
   const R one = R(1), two = R(2), half = R(0.5), quarter = R(0.25);
   const T &g00 = gm[0], &g11 = gm[1], &g01 = gm[2], &g02 = gm[3], &g12 = gm[4], &g22 = gm[5];
@@ -243,6 +243,7 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
       c00 = g11 * id2; c11 = g00 * id2; c01 = -g01 * id2; c22 = one / C33;
     }
   }
+  if (c33_out) *c33_out = C33;
 }
 
 /* Mid-surface geometry of the element from y = (a1, a2, Aaa, Abb, Aab). */
@@ -345,6 +346,30 @@ __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R
     M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
   }
   elem_out(g, N0, N1, N2, M0, M1, M2, pref0, f);
+}
+
+/* UpdateElementThickness (active_strain.c:2198-2224): h0 sqrt(C33) with C33
+   the mean over the thickness points of C33 after the sub-iterations (1 when
+   that mean is not positive). */
+template <class R>
+__host__ __device__ __forceinline__ R elem_thickness(const R y[15], const EPar<R> &p, const R *ref, int stride, R h0,
+                                                     int &status)
+{
+  const ElemGeom<R> g = elem_geom<R, R>(y, p);
+  const int nq = p.nq;
+  const R gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];
+  const R gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
+  const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
+  R sum = R(0);
+  for (int q = 0; q < nq; q++) {
+    const QpRef<R> r = load_qpref(ref, stride, q);
+    R gm[6], sv[3], c33 = R(1);
+    qp_metric(g, p.hhalf * p.theta[q], gm);
+    qp_stress(gm, r, gam, gamp, c1, p.mu, p.K, p.iters, sv, status, &c33);
+    sum += c33;
+  }
+  const R C33 = nq > 0 ? sum / (R)nq : R(1);
+  return h0 * (C33 > R(0) ? sqrt(C33) : R(1));
 }
 
 /* Jobs (q, k0..k0+KD-1) of the split tangent: stress of thickness point q

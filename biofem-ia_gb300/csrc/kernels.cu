@@ -471,7 +471,8 @@ __device__ __forceinline__ unsigned long long abs_bits(double v)
   return (unsigned long long)__double_as_longlong(fabs(v));
 }
 
-__global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x, double *__restrict__ R)
+__global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x, double *__restrict__ R,
+                              double *__restrict__ parts)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long lmax = 0ull;
@@ -492,7 +493,7 @@ __global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x
        node's inertial (and damping) force over every triangle with this
        corner, ghost and bridging triangles included */
     double fd[3] = {0.0, 0.0, 0.0};
-    if (p.dyn && kind == 0) {
+    if (p.dyn && (kind == 0 || (parts && i < p.nv))) {
       for (int c = m.dptr[i]; c < m.dptr[i + 1]; c++) {
         const double M = p.dyn_rhoh0 * m.dA0[m.didx[c]] / 3;
         const double C = p.dyn_damp ? p.dyn_dampf * M : 0.0;
@@ -517,6 +518,13 @@ __global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x
       else if (p.dyn) r = (-1.0 * fe[d] + fi[d]) + 1. * fd[d];
       else r = -1.0 * fe[d] + fi[d];
       R[3 * (size_t)i + d] = r;
+      if (parts) {   /* unscaled Fint, Fext, Fdyn of the real nodes (ghost entries 0) */
+        const size_t n3 = 3 * (size_t)p.nt, o = 3 * (size_t)i + d;
+        const bool real = i < p.nv;
+        parts[o] = real ? fi[d] : 0.0;
+        parts[n3 + o] = real ? fe[d] : 0.0;
+        parts[2 * n3 + o] = real ? fd[d] : 0.0;
+      }
       const unsigned long long b = abs_bits(fe[d]);
       lmax = b > lmax ? b : lmax;
     }
@@ -626,6 +634,32 @@ int launch_to_float(const double *a, float *b, long long n, void *stream)
   return (int)cudaGetLastError();
 }
 
+/* UpdateElementThickness (active_strain.c:2198-2224): one thread per element,
+   the residual kernel's geometry and stress with C33 of every thickness point
+   kept; thickness = h0 sqrt(mean C33). */
+__global__ void __launch_bounds__(128) k_elem_thickness(DevMesh m, KParams p, double h0, double *__restrict__ th)
+{
+  __shared__ double tabs[kNumTables * 80];
+  for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ne) return;
+  const int info = m.einfo[e];
+  const int nen = info & 0xff, tabi = info >> 8;
+  double y[15];
+  gather_y(m.pos, m.patch, e, nen, tabs + tabi * 80, y);
+  int st = 0;
+  const EPar<double> ep = epar<double>(p);
+  th[e] = elem_thickness<double>(y, ep, m.eref + e, p.ne, h0, st);
+  set_status(m.status, st);
+}
+
+int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double *th, void *stream)
+{
+  k_elem_thickness<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p, h0, th);
+  return (int)cudaGetLastError();
+}
+
 /* d Fdyn / d x: per free node, the triangle-order sum over its corner
    triangles of M M1 + C C1 (Newmark) or M / dt^2 + C / dt (central) */
 __global__ void k_dyn_diag(DevMesh m, KParams p)
@@ -669,10 +703,10 @@ int launch_dyn_update(const DevMesh &m, const KParams &p, const double *x, void 
   return (int)cudaGetLastError();
 }
 
-int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream)
+int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream, double *parts)
 {
   cudaMemsetAsync(m.fmax, 0, sizeof(unsigned long long), (cudaStream_t)stream);
-  k_node_gather<<<blocks_for(p.nt, 256), 256, 0, (cudaStream_t)stream>>>(m, p, x, R);
+  k_node_gather<<<blocks_for(p.nt, 256), 256, 0, (cudaStream_t)stream>>>(m, p, x, R, parts);
   return (int)cudaGetLastError();
 }
 

@@ -197,11 +197,14 @@ int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOpt
      Newmark (timeinteg 0): Fd = M M1 x + C C1 x - M (M1 xn + M2 xd + M3 xdd)
                                   - C (C1 xn + C2 xd + C3 xdd),
      central (timeinteg 1): Fd = M (x - 2 xn + xnm1) / dt^2 + C (x - xn) / dt.
-   SetGpuDynamics(m, NULL) switches the term off; the state (3*(n_v+n_ghosts)
-   each) starts at zero and is set or read with the state calls (NULL entries
-   are skipped).  RunGpuDynamicUpdate(m, x) ends a step from the converged x:
-   acceleration and velocity updates on the real nodes, then xnm1 <- xn,
-   xn <- x.  SetGpuElementGamma(m, g) recomputes the per-element activation
+   The corner sum runs over every triangle, ghost and bridging triangles
+   included (the serial FDynamic loop, main.c:1293).  SetGpuDynamics(m, NULL)
+   switches the term off; each SetGpuDynamics call restarts the state
+   (3*(n_v+n_ghosts) each) at xn = xnm1 = the reference coordinates and
+   xd = xdd = 0 (Init, main.c:1515-1540); the state calls set or read it (NULL
+   entries are skipped).  RunGpuDynamicUpdate(m, x) ends a step from the
+   converged x: xAccVel's acceleration and velocity updates (main.c:1367-1412),
+   then xnm1 <- xn, xn <- x.  SetGpuElementGamma(m, g) recomputes the per-element activation
    constants with g[e] in place of gamma * gamma_scale[e] (the value of
    GammaOfTimeDelayed times gamma_scale, active_strain.c:1156-1212). */
 typedef struct {
@@ -213,6 +216,53 @@ int SetGpuDynamicState(BiofemGpuMesh *m, const double *xn, const double *xnm1, c
 int GetGpuDynamicState(BiofemGpuMesh *m, double *xn, double *xnm1, double *xd, double *xdd);
 int RunGpuDynamicUpdate(BiofemGpuMesh *m, const double *x);
 int SetGpuElementGamma(BiofemGpuMesh *m, const double *gamma_e);
+
+/* Output quantities of a state x (host arrays, 3*(n_v+n_ghosts) each): the
+   unscaled node forces Fint, Fext and Fdyn of FormFunctionFEM
+   (main.c:829-845; Fdyn zero while the dynamic term is off) and the residual
+   R; any output pointer may be NULL. */
+int RunGpuResidualParts(BiofemGpuMesh *m, const double *x, double *R, double *Fint, double *Fext, double *Fdyn);
+/* Wall thickness per element of a state x (UpdateElementThickness,
+   active_strain.c:2198-2224): h0 sqrt(mean over the thickness points of C33
+   after the sub-iterations); n_elmt values. */
+int RunGpuElementThickness(BiofemGpuMesh *m, const double *x, double *thickness);
+
+/* On-disk formats (host only; formats.cpp).
+   Checkpoints: LocationOut / LocationIn (io.c:1272-1376, 1513-1640) write and
+   read "<dir>/<tag><ibi>_<ti>.dat" for tag x, xn, xd, xdd, each n_dof =
+   3*(n_v+n_ghosts) doubles in original-vertex order, big-endian:
+   BIOFEM_CKPT_VERTEX_ORDER the values alone (the DMPlex path, any process
+   count), BIOFEM_CKPT_VEC a PETSc VecView record (int32 classid 1211214, int32
+   length, values; the serial path).  BiofemLocationIn accepts both (and a
+   VecView record with 64-bit header integers), choosing by the file size. */
+#define BIOFEM_CKPT_VERTEX_ORDER 0
+#define BIOFEM_CKPT_VEC 1
+int BiofemLocationOut(const char *dir, int32_t ti, int32_t ibi, int64_t n_dof, const double *x, const double *xn,
+                      const double *xd, const double *xdd, int32_t layout);
+int BiofemLocationIn(const char *dir, int32_t ti, int32_t ibi, int64_t n_dof, double *x, double *xn, double *xd,
+                     double *xdd);
+/* "<dir>/surface<ibi>_<ti>.vtk" (Output, io.c:540-964, with muscle
+   activation on and no contact): points x, triangles, point data contact (0),
+   m, IE (0), disp = x - X, Fint, Fext, Fdyn, Fcnt (0), u = xd, Res = Fint -
+   Fext + Fdyn; cell data nfib (when fib is given, the LV loader's field), dA
+   (flat area on x), dA0 (given, or the flat area on X), gamma.  Node arrays
+   hold the n_v real nodes; NULL force / velocity / mass arrays print zeros. */
+typedef struct {
+  int32_t n_v, n_elmt;
+  const int32_t *tri;      /* 3 n_elmt corners */
+  const double *x, *X;     /* 3 n_v current and reference positions */
+  const double *mass;      /* n_v lumped mass (Init, main.c:1465-1470) */
+  const double *Fint, *Fext, *Fdyn, *xd;   /* 3 n_v each */
+  const double *dA0;       /* n_elmt */
+  const double *gamma_e;   /* n_elmt activation of the step (required) */
+  const double *fib;       /* 3 n_elmt fibre directions */
+} BiofemSurfaceFields;
+int BiofemWriteSurfaceVTK(const char *dir, int32_t ti, int32_t ibi, const BiofemSurfaceFields *fields);
+/* "<dir>/shell3d<ibi>_<ti>.vtk" (Write3DShellVTK, io.c:983-1064): one layer of
+   wedges, each surface node offset by half its node-averaged thickness along
+   its area-weighted normal. */
+int BiofemWriteShell3dVTK(const char *dir, int32_t ti, int32_t ibi, int32_t n_v, int32_t n_elmt, const int32_t *tri,
+                          const double *x, const double *thickness_e);
 
 /* Serving loop for load-step requests (new; the reference runs each case as
    a separate batch job, bin/biofem:352-456).  Continuous batching: requests

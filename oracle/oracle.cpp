@@ -712,7 +712,8 @@ static int g_threads = 1;
 /* FormFunctionFEM at np = 1, main.c:757-1032 (see oracle/ref_driver.c for the
    load and BC choices).  x and R have 3 (n_v + n_ghosts) entries. */
 template <class T>
-static int residual(const Body &B, const T *x, T *R, T *Fint_out = nullptr, T *Fext_out = nullptr)
+static int residual(const Body &B, const T *x, T *R, T *Fint_out = nullptr, T *Fext_out = nullptr,
+                    T *Fdyn_out = nullptr)
 {
   const Mesh &m = B.m;
   const int ntot = m.n_v + m.n_ghosts, ndof = 3 * ntot;
@@ -801,6 +802,7 @@ static int residual(const Body &B, const T *x, T *R, T *Fint_out = nullptr, T *F
   for (int i = 0; i < ndof; i++) R[i] = R[i] * scale;
   if (Fint_out) for (int i = 0; i < ndof; i++) Fint_out[i] = Fint[i];
   if (Fext_out) for (int i = 0; i < ndof; i++) Fext_out[i] = Fext[i];
+  if (Fdyn_out) for (int i = 0; i < ndof; i++) Fdyn_out[i] = Fdyn[i];
   return 0;
 }
 
@@ -1037,6 +1039,13 @@ int oracle_residual(const double *x, double *R, double *Fint, double *Fext)
 {
   if (!g_body || !g_body->ready) return 58;
   return residual<double>(*g_body, x, R, Fint, Fext);
+}
+
+/* R and the unscaled Fint, Fext, Fdyn of main.c:829-845 */
+int oracle_residual_parts(const double *x, double *R, double *Fint, double *Fext, double *Fdyn)
+{
+  if (!g_body || !g_body->ready) return 58;
+  return residual<double>(*g_body, x, R, Fint, Fext, Fdyn);
 }
 
 /* Directional derivative J v of the residual (exact, forward mode). */

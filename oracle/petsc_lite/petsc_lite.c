@@ -4,6 +4,9 @@
  */
 #include "petscsys.h"
 
+#include <fcntl.h>
+#include <unistd.h>
+
 static int lite_verbose_(void) { return getenv("PETSC_LITE_VERBOSE") != NULL; }
 
 PetscErrorCode PetscLiteError_(PetscErrorCode code, const char *file, int line, const char *fmt, ...)
@@ -223,16 +226,88 @@ PetscErrorCode VecGetOwnershipRange(Vec v, PetscInt *lo, PetscInt *hi) { *lo = 0
 #define LITE_UNSUPPORTED(name) \
   return PetscLiteError_(PETSC_ERR_SUP, __FILE__, __LINE__, "%s is not part of petsc-lite", name)
 
-PetscErrorCode VecView(Vec v, PetscViewer w) { (void)v; (void)w; LITE_UNSUPPORTED("VecView"); }
-PetscErrorCode VecLoad(Vec v, PetscViewer w) { (void)v; (void)w; LITE_UNSUPPORTED("VecLoad"); }
-PetscErrorCode PetscViewerBinaryOpen(MPI_Comm c, const char name[], PetscFileMode m, PetscViewer *w)
-{ (void)c; (void)name; (void)m; (void)w; LITE_UNSUPPORTED("PetscViewerBinaryOpen"); }
-PetscErrorCode PetscViewerDestroy(PetscViewer *w) { (void)w; return 0; }
-PetscErrorCode PetscViewerBinaryGetDescriptor(PetscViewer w, int *fd) { (void)w; (void)fd; LITE_UNSUPPORTED("PetscViewerBinaryGetDescriptor"); }
+/* Binary viewer: PETSc's documented file layout, every item big-endian
+   (PetscBinaryWrite / PetscBinaryRead); VecView writes the record
+   VEC_FILE_CLASSID (1211214), the length, the values, with 32-bit PetscInt.
+   No ".info" side file is written. */
+struct PetscLiteOpaque_ { int fd; };
+#define LITE_VEC_FILE_CLASSID 1211214
+
+static void lite_swap_(unsigned char *b, size_t size, size_t n)
+{
+  for (size_t i = 0; i < n; i++) {
+    unsigned char *e = b + i * size;
+    for (size_t k = 0; k < size / 2; k++) { unsigned char t = e[k]; e[k] = e[size - 1 - k]; e[size - 1 - k] = t; }
+  }
+}
+
+static int lite_little_endian_(void) { const unsigned one = 1; return *(const unsigned char *)&one == 1; }
+
 PetscErrorCode PetscBinaryWrite(int fd, const void *p, PetscInt n, PetscDataType t)
-{ (void)fd; (void)p; (void)n; (void)t; LITE_UNSUPPORTED("PetscBinaryWrite"); }
+{
+  const size_t size = t == PETSC_INT ? sizeof(PetscInt) : sizeof(PetscReal);
+  unsigned char *b = (unsigned char *)malloc(size * (size_t)(n > 0 ? n : 1));
+  memcpy(b, p, size * (size_t)n);
+  if (lite_little_endian_()) lite_swap_(b, size, (size_t)n);
+  const ssize_t w = write(fd, b, size * (size_t)n);
+  free(b);
+  if (w != (ssize_t)(size * (size_t)n)) return PetscLiteError_(PETSC_ERR_FILE_WRITE, __FILE__, __LINE__, "short write");
+  return 0;
+}
+
 PetscErrorCode PetscBinaryRead(int fd, void *p, PetscInt n, PetscInt *count, PetscDataType t)
-{ (void)fd; (void)p; (void)n; (void)count; (void)t; LITE_UNSUPPORTED("PetscBinaryRead"); }
+{
+  const size_t size = t == PETSC_INT ? sizeof(PetscInt) : sizeof(PetscReal);
+  size_t got = 0;
+  while (got < size * (size_t)n) {
+    const ssize_t r = read(fd, (unsigned char *)p + got, size * (size_t)n - got);
+    if (r <= 0) break;
+    got += (size_t)r;
+  }
+  if (lite_little_endian_()) lite_swap_((unsigned char *)p, size, got / size);
+  if (count) *count = (PetscInt)(got / size);
+  else if (got != size * (size_t)n) return PetscLiteError_(PETSC_ERR_FILE_READ, __FILE__, __LINE__, "short read");
+  return 0;
+}
+
+PetscErrorCode PetscViewerBinaryOpen(MPI_Comm c, const char name[], PetscFileMode m, PetscViewer *w)
+{
+  (void)c;
+  const int fd = m == FILE_MODE_READ ? open(name, O_RDONLY) : open(name, O_WRONLY | O_CREAT | O_TRUNC, 0666);
+  if (fd < 0) return PetscLiteError_(PETSC_ERR_FILE_OPEN, __FILE__, __LINE__, "cannot open %s", name);
+  *w = (PetscViewer)malloc(sizeof(**w));
+  (*w)->fd = fd;
+  return 0;
+}
+
+PetscErrorCode PetscViewerDestroy(PetscViewer *w)
+{
+  if (w && *w) { close((*w)->fd); free(*w); *w = NULL; }
+  return 0;
+}
+
+PetscErrorCode PetscViewerBinaryGetDescriptor(PetscViewer w, int *fd)
+{
+  if (!w) return PetscLiteError_(PETSC_ERR_ARG_NULL, __FILE__, __LINE__, "null viewer");
+  *fd = w->fd;
+  return 0;
+}
+
+PetscErrorCode VecView(Vec v, PetscViewer w)
+{
+  PetscInt head[2] = {LITE_VEC_FILE_CLASSID, v->n};
+  PetscCall(PetscBinaryWrite(w->fd, head, 2, PETSC_INT));
+  return PetscBinaryWrite(w->fd, v->a, v->n, PETSC_REAL);
+}
+
+PetscErrorCode VecLoad(Vec v, PetscViewer w)
+{
+  PetscInt head[2];
+  PetscCall(PetscBinaryRead(w->fd, head, 2, NULL, PETSC_INT));
+  if (head[0] != LITE_VEC_FILE_CLASSID || head[1] != v->n)
+    return PetscLiteError_(PETSC_ERR_FILE_UNEXPECTED, __FILE__, __LINE__, "not a Vec record of length %d", (int)v->n);
+  return PetscBinaryRead(w->fd, v->a, v->n, NULL, PETSC_REAL);
+}
 PetscErrorCode PetscRealView(PetscInt n, const PetscReal v[], PetscViewer w) { (void)n; (void)v; (void)w; LITE_UNSUPPORTED("PetscRealView"); }
 
 PetscErrorCode MatCreate(MPI_Comm c, Mat *m) { (void)c; (void)m; LITE_UNSUPPORTED("MatCreate"); }

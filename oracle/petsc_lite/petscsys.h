@@ -57,6 +57,9 @@ typedef void *PetscOptions;
 #define PETSC_ERR_ARG_WRONG       62
 #define PETSC_ERR_ARG_OUTOFRANGE  63
 #define PETSC_ERR_FILE_OPEN       65
+#define PETSC_ERR_FILE_READ       66
+#define PETSC_ERR_FILE_WRITE      67
+#define PETSC_ERR_FILE_UNEXPECTED 79
 #define PETSC_ERR_FP              72
 #define PETSC_ERR_LIB             76
 #define PETSC_ERR_PLIB            77

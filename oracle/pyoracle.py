@@ -95,6 +95,17 @@ class _Base:
 class Oracle(_Base):
     prefix = "oracle"
 
+    def residual_parts(self, x):
+        """(R, Fint, Fext, Fdyn), the forces unscaled."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = [np.zeros(self.n_dof) for _ in range(4)]
+        f = self.lib.oracle_residual_parts
+        f.argtypes = [_vp] * 5
+        rc = f(_p(x), *[_p(a) for a in out])
+        if rc:
+            raise RuntimeError(f"oracle_residual_parts failed with code {rc}")
+        return tuple(out)
+
     # ---- dynamic term (FDynamic / xAccVel) and per-element activation ----
     def set_dynamics(self, dt=None, rho=0.0, newmark_gamma=0.5, dampfactor=0.0, timeinteg=0, damping=0):
         f = self.lib.oracle_set_dynamics
@@ -360,3 +371,39 @@ class RefOracle(_Base):
         if rc:
             raise RuntimeError(rc)
         return S, C33, g
+
+    # ---- the reference's own on-disk writers and readers (io.c) ----
+    def location_out(self, out_dir, ti: int, x, xn, xd, xdd, ibi: int = 0, dmplex: bool = True):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, xn, xd, xdd)]
+        f = self.lib.ref_location_out
+        f.argtypes = [ctypes.c_char_p, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int]
+        rc = f(str(out_dir).encode(), ti, ibi, *[_p(a) for a in arrs], int(dmplex))
+        if rc:
+            raise RuntimeError(f"ref_location_out failed with code {rc}")
+
+    def location_in(self, out_dir, ti: int, ibi: int = 0, dmplex: bool = True):
+        out = [np.zeros(self.n_dof) for _ in range(4)]
+        f = self.lib.ref_location_in
+        f.argtypes = [ctypes.c_char_p, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int]
+        rc = f(str(out_dir).encode(), ti, ibi, *[_p(a) for a in out], int(dmplex))
+        if rc:
+            raise RuntimeError(f"ref_location_in failed with code {rc}")
+        return dict(zip(("x", "xn", "xd", "xdd"), out))
+
+    def output_vtk(self, out_dir, ti: int, x, Fdyn, xd, rho: float, lv: bool = False, ibi: int = 0):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, Fdyn, xd)]
+        f = self.lib.ref_output_vtk
+        f.argtypes = [ctypes.c_char_p, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_int]
+        rc = f(str(out_dir).encode(), ti, ibi, *[_p(a) for a in arrs], float(rho), int(lv))
+        if rc:
+            raise RuntimeError(f"ref_output_vtk failed with code {rc}")
+
+    def thickness(self, x, out_dir=None, ti: int = 0, ibi: int = 0):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        th = np.zeros(self.n_elmt)
+        f = self.lib.ref_thickness
+        f.argtypes = [ctypes.c_char_p, _c_int, _c_int, _vp, _vp]
+        rc = f(None if out_dir is None else str(out_dir).encode(), ti, ibi, _p(x), _p(th))
+        if rc:
+            raise RuntimeError(f"ref_thickness failed with code {rc}")
+        return th

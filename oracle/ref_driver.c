@@ -313,3 +313,93 @@ int ref_elem_state(int ec, double *S, double *C33, double *geom24)
   for (int k = 0; k < 8; k++) { geom24[3 * k] = vs[k]->x; geom24[3 * k + 1] = vs[k]->y; geom24[3 * k + 2] = vs[k]->z; }
   return 0;
 }
+
+/* ---- on-disk formats: the reference's own writers and readers ---- */
+extern PetscErrorCode LocationOut(FE *fem, PetscInt ti, PetscInt ibi, const char *out_dir);
+extern PetscErrorCode LocationIn(FE *fem, PetscInt ti, PetscInt ibi, const char *out_dir);
+extern PetscErrorCode Output(FE *fem, PetscInt ti, PetscInt ibi, const char *out_dir);
+extern PetscErrorCode Write3DShellVTK(FE *fem, PetscInt ti, PetscInt ibi, const char *out_dir);
+extern PetscErrorCode UpdateElementThickness(FE *fem);
+
+/* LocationOut (io.c:1272) of the given state.  dmplex = 1 keeps the driver's
+   DMPlex context (raw ibm-order files), 0 takes the serial VecView path. */
+int ref_location_out(const char *dir, int ti_out, int ibi, const double *x, const double *xn, const double *xd,
+                     const double *xdd, int dmplex)
+{
+  if (!g_ready) return PETSC_ERR_ORDER;
+  FE *fem = &g_fem;
+  const PetscInt ndof = dof * (g_ibm.n_v + g_ibm.n_ghosts);
+  Vec v[4] = {fem->x, fem->xn, fem->xd, fem->xdd};
+  const double *src[4] = {x, xn, xd, xdd};
+  for (int k = 0; k < 4; k++) for (PetscInt i = 0; i < ndof; i++) v[k]->a[i] = src[k][i];
+  const PetscBool init = fem->geom_ctx.initialized;
+  fem->geom_ctx.initialized = dmplex ? PETSC_TRUE : PETSC_FALSE;
+  PetscErrorCode rc = LocationOut(fem, ti_out, ibi, dir);
+  fem->geom_ctx.initialized = init;
+  return rc;
+}
+
+/* LocationIn (io.c:1513) into x, xn, xd, xdd (each 3 (n_v + n_ghosts)). */
+int ref_location_in(const char *dir, int ti_in, int ibi, double *x, double *xn, double *xd, double *xdd, int dmplex)
+{
+  if (!g_ready) return PETSC_ERR_ORDER;
+  FE *fem = &g_fem;
+  const PetscInt ndof = dof * (g_ibm.n_v + g_ibm.n_ghosts);
+  const PetscBool init = fem->geom_ctx.initialized;
+  fem->geom_ctx.initialized = dmplex ? PETSC_TRUE : PETSC_FALSE;
+  PetscErrorCode rc = LocationIn(fem, ti_in, ibi, dir);
+  fem->geom_ctx.initialized = init;
+  if (rc) return rc;
+  Vec v[4] = {fem->x, fem->xn, fem->xd, fem->xdd};
+  double *dst[4] = {x, xn, xd, xdd};
+  for (int k = 0; k < 4; k++) for (PetscInt i = 0; i < ndof; i++) dst[k][i] = v[k]->a[i];
+  return 0;
+}
+
+/* Output (io.c:540) after a residual evaluation at x.  The driver has no
+   FDynamic: Fdyn and the velocity xd are the caller's.  The nodal mass is
+   Init's (main.c:1465-1470) for density rho_in; IE is zeroed as FormFunctionFEM
+   does (main.c:831); lv sets lv_geom_process (the nfib cell field). */
+int ref_output_vtk(const char *dir, int ti_out, int ibi, const double *x, const double *Fdyn, const double *xd,
+                   double rho_in, int lv)
+{
+  if (!g_ready) return PETSC_ERR_ORDER;
+  FE *fem = &g_fem;
+  IBMNodes *ibm = &g_ibm;
+  const PetscInt ndof = dof * (ibm->n_v + ibm->n_ghosts);
+  double *R = (double *)malloc(sizeof(double) * (size_t)ndof);
+  int rc = ref_residual(x, R, NULL, NULL);
+  free(R);
+  if (rc) return rc;
+  for (PetscInt i = 0; i < ndof; i++) { fem->Fdyn->a[i] = Fdyn[i]; fem->xd->a[i] = xd[i]; }
+  rho = rho_in;
+  for (PetscInt v = 0; v < ibm->n_v; v++) ibm->m[v] = 0.;
+  for (PetscInt ec = 0; ec < ibm->n_elmt; ec++) {
+    const PetscReal mass = 1. / 3. * rho * ibm->dA0[ec] * h0;
+    ibm->m[ibm->nv1[ec]] += mass; ibm->m[ibm->nv2[ec]] += mass; ibm->m[ibm->nv3[ec]] += mass;
+  }
+  for (PetscInt v = 0; v < ibm->n_v; v++) fem->IE[v] = 0.;
+  const PetscInt lv_was = lv_geom_process;
+  lv_geom_process = lv;
+  rc = Output(fem, ti_out, ibi, dir);
+  lv_geom_process = lv_was;
+  return rc;
+}
+
+/* UpdateElementThickness (active_strain.c:2198) after a residual evaluation at
+   x, then Write3DShellVTK (io.c:983) when dir is not NULL. */
+int ref_thickness(const char *dir, int ti_out, int ibi, const double *x, double *thickness)
+{
+  if (!g_ready) return PETSC_ERR_ORDER;
+  FE *fem = &g_fem;
+  IBMNodes *ibm = &g_ibm;
+  const PetscInt ndof = dof * (ibm->n_v + ibm->n_ghosts);
+  double *R = (double *)malloc(sizeof(double) * (size_t)ndof);
+  int rc = ref_residual(x, R, NULL, NULL);
+  free(R);
+  if (rc) return rc;
+  PetscCall(UpdateElementThickness(fem));
+  for (PetscInt ec = 0; ec < ibm->n_elmt; ec++) thickness[ec] = ibm->thickness[ec];
+  if (dir) PetscCall(Write3DShellVTK(fem, ti_out, ibi, dir));
+  return 0;
+}
