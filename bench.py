@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true", help="skip the Newton and serving measurements")
     ap.add_argument("--no-c3", action="store_true", help="skip the C3 (1024x768) and C4 (ellipsoid) measurements")
-    ap.add_argument("--serve-requests", type=int, default=128)
+    ap.add_argument("--serve-requests", type=int, default=512)
     return ap.parse_args()
 
 
@@ -290,7 +290,7 @@ def case_bench(w, steps=5, warmup=2):
     return out
 
 
-def serve_bench(n_req=128, slots=16, budget=40 << 30, load=0.8):
+def serve_bench(n_req=512, slots=16, budget=40 << 30, load=0.8):
     """Load-step serving stream (C5): flat sheets with nx log-uniform in
     [16, 256], ny = round(0.75 nx), seeded smooth imperfection, lambda_a,
     fibre angle and pressure per request; 5 Newton iterations at most, each to

@@ -173,11 +173,17 @@ __host__ __device__ __forceinline__ T qform(const T &c00, const T &c11, const T 
 }
 
 /* Stress of one thickness point after the C33 sub-iterations:
-   returns S^11, S^22, S^12 in sv[0..2]; status bit 1 on a vanishing CC3333. */
+   returns S^11, S^22, S^12 in sv[0..2]; status bit 1 on a vanishing CC3333.
+   Every sub-iteration ends with the C33 update (ModElemC33); the stress is
+   taken before the last one, so final_update = false skips that update
+   (CC3333 and its check included) when only the stress is wanted and another
+   kernel of the same call performs the check.  c33_out receives C33 after
+   the last update. */
 template <class T, class R>
 __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 12 22 */, const QpRef<R> &r,
                                                    R gam, R gamp, R c1, R mu, R K,
-                                                   int iters, T sv[3], int &status, T *c33_out = nullptr)
+                                                   int iters, T sv[3], int &status, T *c33_out = nullptr,
+                                                   bool final_update = true)
 {
   const R one = R(1), two = R(2), half = R(0.5), quarter = R(0.25);
   const T &g00 = gm[0], &g11 = gm[1], &g01 = gm[2], &g02 = gm[3], &g12 = gm[4], &g22 = gm[5];
@@ -212,6 +218,7 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
       sv[2] = mu * (r.gc01 + c1 * r.s[0] * r.s[1])
             + half_a * (two * c01 + gamp * r.s[1] * u0 - gam * r.s[0] * u1 - gg * r.s[0] * r.s[1] * tau);
     }
+    if (!final_update && it == iters - 1) break;
     /* CC3333 */
     const T qvv = qform(c00, c11, c01, c22, r.av, r.av);
     const T qww = qform(c00, c11, c01, c22, r.aw, r.aw);
@@ -238,9 +245,13 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
     }
     C33 = Ct;
     if (it + 1 < iters) {
-      /* C_inv = INV([[gm00 gm01 0][gm01 gm11 0][0 0 C33]]) */
-      const T id2 = one / (g00 * g11 - g01 * g01);
-      c00 = g11 * id2; c11 = g00 * id2; c01 = -g01 * id2; c22 = one / C33;
+      /* C_inv = INV([[gm00 gm01 0][gm01 gm11 0][0 0 C33]]): the in-plane block
+         is the same in every later sub-iteration */
+      if (it == 0) {
+        const T id2 = one / (g00 * g11 - g01 * g01);
+        c00 = g11 * id2; c11 = g00 * id2; c01 = -g01 * id2;
+      }
+      c22 = one / C33;
     }
   }
   if (c33_out) *c33_out = C33;
@@ -372,14 +383,24 @@ __host__ __device__ __forceinline__ R elem_thickness(const R y[15], const EPar<R
   return h0 * (C33 > R(0) ? sqrt(C33) : R(1));
 }
 
+/* Metric components the stress is differentiated along: 00 11 01 02 12.  The
+   sixth, g33 = n.n, is 1 for every y (d(n.n) = 2 n.dn = 0), so its column of
+   the constitutive derivative is never used; with the tangential thickness
+   metric g_alpha.n = (a_alpha + th a3,alpha).n is 0 for every y as well, which
+   leaves 00 11 01. */
+template <class R>
+__host__ __device__ __forceinline__ int metric_dirs(const EPar<R> &p) { return p.tnormal ? 3 : 5; }
+
 /* Jobs (q, k0..k0+KD-1) of the split tangent: stress of thickness point q
-   with KD metric directions; jac layout as in elem_forces_split. */
+   with KD metric directions (the last job of a point may carry unused
+   directions); jac layout as in elem_forces_split. */
 template <class R, int KD>
 __device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> &g0, const EPar<R> &p, const R *ref, int stride,
                                                   int lane, R gam, R gamp, R c1, R *jac, int &status)
 {
   typedef DK<R, KD> T;
-  constexpr int per_q = 6 / KD;
+  const int ndirs = metric_dirs(p);
+  const int per_q = (ndirs + KD - 1) / KD;
   for (int job = lane; job < per_q * p.nq; job += 16) {
     const int q = job / per_q, k0 = (job - per_q * q) * KD;
     R gmv[6];
@@ -389,14 +410,16 @@ __device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> &g0, const E
     for (int c = 0; c < 6; c++) {
       gm[c].v = gmv[c];
 #pragma unroll
-      for (int i = 0; i < KD; i++) gm[c].d[i] = (c == k0 + i) ? R(1) : R(0);
+      for (int i = 0; i < KD; i++) gm[c].d[i] = (c == k0 + i && c < ndirs) ? R(1) : R(0);
     }
     T sv[3];
-    qp_stress(gm, load_qpref(ref, stride, q), gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
+    /* the stress only: the residual kernel of the same call checks the last CC3333 */
+    qp_stress(gm, load_qpref(ref, stride, q), gam, gamp, c1, p.mu, p.K, p.iters, sv, status, (T *)nullptr, false);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
 #pragma unroll
-      for (int t = 0; t < KD; t++) jac[q * 21 + 6 * i + k0 + t] = sv[i].d[t];
+      for (int t = 0; t < KD; t++)
+        if (k0 + t < ndirs) jac[q * 21 + 6 * i + k0 + t] = sv[i].d[t];
     }
     if (k0 == 0) {
 #pragma unroll
@@ -411,8 +434,8 @@ __device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> &g0, const E
    each thickness point, so it is differentiated along those: job (q, k) =
    derivative of the stress of point q along metric component k, one job per
    lane per round; each lane then applies the chain rule with its own metric
-   derivative.  That is 6 nq constitutive evaluations per element instead of
-   16 nq.  The primal values are the plain R-precision evaluation.
+   derivative.  That is 5 nq (3 nq with the tangential thickness metric)
+   constitutive derivative directions per element instead of 16 nq.  The primal values are the plain R-precision evaluation.
    jac: this group's scratch, kMaxQp * 21 values; the 16 lanes of the group
    and the other group of the warp must all call this (it synchronises the
    warp). */
@@ -426,21 +449,23 @@ __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &
   const R gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
   const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
   const R pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
-  /* constitutive derivatives: jac[q*21 + 6*i + k] = d sv_i / d gm_k, jac[q*21 + 18 + i] = sv_i;
-     FP64: KD metric directions per job so that the 6 nq / KD jobs fit one
-     round of 16 lanes (KD = 1 up to 2 thickness points, 2 up to 5, 3 for 6) */
+  /* constitutive derivatives: jac[q*21 + 6*i + k] = d sv_i / d gm_k (k < ndirs),
+     jac[q*21 + 18 + i] = sv_i; FP64: KD metric directions per job, the fewest
+     for which the ceil(ndirs / KD) nq jobs fit one round of 16 lanes */
   {
     const ElemGeom<R> g0 = elem_geom<R, R>(y, p);
     if constexpr (sizeof(R) == 4) {
       /* FP32: one direction per job (wider duals spill under the FP32 kernel's register cap) */
       constitutive_jobs<R, 1>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
     } else {
-      if (nq <= 2) constitutive_jobs<R, 1>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
-      else if (nq <= 5) constitutive_jobs<R, 2>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      const int ndirs = metric_dirs(p);
+      if (ndirs * nq <= 16) constitutive_jobs<R, 1>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      else if (((ndirs + 1) / 2) * nq <= 16) constitutive_jobs<R, 2>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
       else constitutive_jobs<R, 3>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
     }
   }
   __syncwarp();
+  const int ndirs = metric_dirs(p);
   T yd[15];
 #pragma unroll
   for (int c = 0; c < 15; c++) yd[c] = T{y[c], c == lane ? R(1) : R(0)};
@@ -456,7 +481,8 @@ __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &
     for (int i = 0; i < 3; i++) {
       R d = R(0);
 #pragma unroll
-      for (int c = 0; c < 6; c++) d += jac[q * 21 + 6 * i + c] * gm[c].d;
+      for (int c = 0; c < 5; c++)
+        if (c < ndirs) d += jac[q * 21 + 6 * i + c] * gm[c].d;
       sv[i] = T{jac[q * 21 + 18 + i], d};
     }
     const R wq = p.w[q], wt = p.w[q] * th3;

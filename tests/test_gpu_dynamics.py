@@ -129,3 +129,50 @@ def test_time_loop_matches_oracle(precision, oracle_lib):
     for k in ("xd", "xdd"):
         assert np.linalg.norm(sg[k][:nr] - so[k][:nr]) <= 1e-5 * np.linalg.norm(so[k][:nr]), k
     sh.close()
+
+
+def test_dynamic_term_full_size_C2():
+    """C2 (98,304 triangles): Fdyn is the lumped-mass Newmark form of an
+    independent numpy statement (every triangle, ghosts included), and the
+    tangent grows by exactly its diagonal on the free rows."""
+    from biofem.gpu import GpuShell
+    w = configs.C2
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    topo = sh.topology()
+    x = w.initial_x(m, topo["xyz0_full"])
+    rng = np.random.default_rng(85)
+    st = dict(xn=x + 1e-4 * rng.standard_normal(x.size), xd=rng.standard_normal(x.size),
+              xdd=rng.standard_normal(x.size))
+    _, K0 = sh.form_jacobian(x)
+    dt, rho, G, c = 1e-3, 1.1, 0.55, 4.0
+    sh.set_dynamics(dt, rho, G, c, 0, 1)
+    sh.set_dynamic_state(**st)
+    R, Fi, Fe, Fd = sh.residual_parts(x)
+    X = topo["xyz0_full"]
+    tri = topo["gtri"]
+    A = 0.5 * np.linalg.norm(np.cross(X[tri[:, 1]] - X[tri[:, 0]], X[tri[:, 2]] - X[tri[:, 0]]), axis=1)
+    mass = np.zeros(X.shape[0])
+    for k in range(3):
+        np.add.at(mass, tri[:, k], rho * configs.H0 * A / 3)
+    M = np.repeat(mass, 3)
+    B = 0.25 * (G + 0.5) ** 2
+    M1, M2, M3 = 1 / (B * dt * dt), 1 / (B * dt), 1 / (2 * B) - 1
+    C1, C2, C3 = G / (B * dt), G / B - 1, dt * (G / (2 * B) - 1)
+    fd = M * (M1 * (x - st["xn"]) - M2 * st["xd"] - M3 * st["xdd"]) \
+        + c * M * (C1 * (x - st["xn"]) - C2 * st["xd"] - C3 * st["xdd"])
+    nr = 3 * m.n_v
+    np.testing.assert_allclose(Fd[:nr], fd[:nr], rtol=1e-9, atol=1e-12 * np.abs(fd[:nr]).max())
+    _, K1 = sh.form_jacobian(x)
+    v = rng.standard_normal(sh.n_dof)
+    d = sh.to_scipy(K1) @ v - sh.to_scipy(K0) @ v
+    kinds = np.zeros(sh.n_dof, bool)
+    kinds[:nr] = True
+    clamped = np.zeros(sh.n_dof, bool)
+    for nb in m.bnodes[: m.n_bnodes[0]]:
+        clamped[3 * nb: 3 * nb + 3] = True
+    free = kinds & ~clamped
+    expect = M * (M1 + c * C1) * v   # R is unscaled here: no pressure on C2 beyond 1e-4 (max|Fext| < 1)
+    np.testing.assert_allclose(d[free], expect[free], rtol=1e-9, atol=1e-9 * np.abs(expect[free]).max())
+    assert not d[~free].any()
+    sh.close()
