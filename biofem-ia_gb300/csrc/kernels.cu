@@ -550,7 +550,21 @@ __global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
   if (kind != 0) {
     s = (m.colind[k] == row && (w == 0 || w == 4 || w == 8)) ? 1.0 : 0.0;
   } else {
-    for (long long c = m.cptr[k]; c < m.cptr[k + 1]; c++) {
+    long long c = m.cptr[k];
+    const long long cend = m.cptr[k + 1];
+    /* four gathered loads in flight per step; the sum keeps the list order
+       (s - v and s + (-v) round alike) */
+    for (; c + 4 <= cend; c += 4) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int id = m.cidx[c + u];
+        v[u] = id >= 0 ? m.ke[(size_t)id * 9 + w] : -m.ke[(size_t)(-(id + 1)) * 9 + w];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) s += v[u];
+    }
+    for (; c < cend; c++) {
       const int id = m.cidx[c];
       if (id >= 0) s += m.ke[(size_t)id * 9 + w];
       else s -= m.ke[(size_t)(-(id + 1)) * 9 + w];
