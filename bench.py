@@ -37,8 +37,8 @@ for _p in (ROOT, ROOT / "biofem-ia_gb300"):
 
 METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_elem_tangent launch on
-# the 256x192 workload (ncu --set full; 62.5 MB read, 1,216 MB written)
-TANGENT_DRAM_BYTES_C2 = 62.5e6 + 1216e6
+# the 256x192 workload (ncu --set full; 62.8 MB read, 1,064 MB written)
+TANGENT_DRAM_BYTES_C2 = 62.756e6 + 1063.924e6
 UNIT = "elems/s"
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_ELEMS = 2048
@@ -300,7 +300,10 @@ def serve_bench(n_req=512, slots=16, budget=40 << 30, load=0.8):
     at `load` x capacity."""
     from biofem import configs
     from biofem.gpu import GpuShell, Serve, BIOFEM_FP64, BIOFEM_FP32_BULK
-    newton = dict(max_newton=5, rtol=1e-10, forcing=1)
+    # at most 300 GMRES iterations per Newton step: a request whose sheet carries
+    # no pre-tension (lambda_a near 1) has a near-singular tangent, and one such
+    # request ran 20,000 iterations for 7 s, the makespan's whole tail
+    newton = dict(max_newton=5, rtol=1e-10, forcing=1, gmres_max_it=300)
     reqs = []
     for i in range(n_req):
         w = configs.serve_request(i)
@@ -355,8 +358,8 @@ def serve_bench(n_req=512, slots=16, budget=40 << 30, load=0.8):
     return {
         "requests": n_req, "slots": slots, "hbm_budget_gb": budget / 2**30,
         "mesh_sizes_nx": [q[0].nx for q in reqs],
-        "newton": "at most 5 iterations to ||R|| <= 1e-10 ||R0||, multigrid-preconditioned device GMRES, "
-                  "Eisenstat-Walker forcing terms (both arms)",
+        "newton": "at most 5 iterations to ||R|| <= 1e-10 ||R0||, multigrid-preconditioned device GMRES "
+                  "(at most 300 iterations per step), Eisenstat-Walker forcing terms (both arms)",
         "sequential_fp64_load_steps_per_s": n_req / seq_s,
         "served_fp32_bulk_capacity_load_steps_per_s": cap32,
         "served_fp64_capacity_load_steps_per_s": n_req / span64,
