@@ -39,6 +39,8 @@ METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP6
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_elem_tangent launch on
 # the 256x192 workload (ncu --set full; 62.8 MB read, 1,064 MB written)
 TANGENT_DRAM_BYTES_C2 = 62.756e6 + 1063.924e6
+# sm__pipe_fp64_cycles_active (of peak sustained active) of the same capture
+FP64_PIPE_ACTIVE_C2 = 0.901
 UNIT = "elems/s"
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_ELEMS = 2048
@@ -193,8 +195,9 @@ def newton_bench(reps=3):
 def dynamics_bench(steps=10):
     """The implicit time loop (main.c:420-573): per step the element activation
     gamma_e(t) (full sin^2 beat over the run, GammaOfTimeDelayed ramp 1, with a
-    wavefront delay on C4), a Newton solve with the Newmark inertial and damping
-    term in R and K (FDynamic), then xAccVel.  Wall time per step through the
+    wavefront delay on C4), a Newton solve (Eisenstat-Walker linear tolerances)
+    with the Newmark inertial and damping term in R and K (FDynamic), then
+    xAccVel.  Wall time per step through the
     public calls (host x in and out), FP64 and FP32-bulk tangents."""
     from biofem import configs
     from biofem.dynamics import Activation, Dynamics, time_loop
@@ -211,9 +214,9 @@ def dynamics_bench(steps=10):
             sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=prec)
             x0 = w.initial_x(m, sh.topology()["xyz0_full"])
             dyn = Dynamics(dt=dt, rho=1.0, newmark_gamma=0.5, dampfactor=5.0, damping=1)
-            time_loop(sh, m, x0, dyn, act, 2, delay=delay, rtol=1e-10, max_newton=30)   # warm-up
+            time_loop(sh, m, x0, dyn, act, 2, delay=delay, rtol=1e-10, max_newton=30, forcing=1)   # warm-up
             t0 = time.perf_counter()
-            x, rec = time_loop(sh, m, x0, dyn, act, steps, delay=delay, rtol=1e-10, max_newton=30)
+            x, rec = time_loop(sh, m, x0, dyn, act, steps, delay=delay, rtol=1e-10, max_newton=30, forcing=1)
             wall = time.perf_counter() - t0
             out[f"{w.name}_{tag}"] = {
                 "ms_per_time_step": wall / steps * 1e3, "steps": steps, "dt": dt,
@@ -589,7 +592,11 @@ def run_ours(args):
         "compute_roofline": {"kernel": "k_elem_tangent", "bound": "fp64", "kernel_ms": k_tan,
                              "canonical_flops_per_step": f_alg,
                              "achieved_tflops_canonical": f_alg / (k_tan * 1e-3) / 1e12,
-                             "peak_tflops": 1.25, "peak_source": "nominal GB300 FP64 (not measured)"},
+                             "peak_tflops": 1.25, "peak_source": "nominal GB300 FP64 (not measured)",
+                             "fp64_pipe_active_frac": FP64_PIPE_ACTIVE_C2,
+                             "note": "the canonical count leaves out geometry, the C33 sub-iterations and their "
+                                     "derivatives; fp64_pipe_active_frac is sm__pipe_fp64_cycles_active of one "
+                                     "k_elem_tangent launch on C2 (ncu --set full)"},
         "kernels_ms": dict(zip(names, kms)),
         "residual_only": {"ms_per_step": sum(r_ms) / len(r_ms), "elems_per_s": ne / (sum(r_ms) / len(r_ms) * 1e-3)},
         "e2e": {"value": whole_job_rate(world, ne, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 8 * sh.n_dof,
