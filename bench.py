@@ -195,9 +195,8 @@ def newton_bench(reps=3):
 def dynamics_bench(steps=10):
     """The implicit time loop (main.c:420-573): per step the element activation
     gamma_e(t) (full sin^2 beat over the run, GammaOfTimeDelayed ramp 1, with a
-    wavefront delay on C4), a Newton solve (Eisenstat-Walker linear tolerances)
-    with the Newmark inertial and damping term in R and K (FDynamic), then
-    xAccVel.  Wall time per step through the
+    wavefront delay on C4), a Newton solve with the Newmark inertial and damping
+    term in R and K (FDynamic), then xAccVel.  Wall time per step through the
     public calls (host x in and out), FP64 and FP32-bulk tangents."""
     from biofem import configs
     from biofem.dynamics import Activation, Dynamics, time_loop
@@ -214,9 +213,9 @@ def dynamics_bench(steps=10):
             sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=prec)
             x0 = w.initial_x(m, sh.topology()["xyz0_full"])
             dyn = Dynamics(dt=dt, rho=1.0, newmark_gamma=0.5, dampfactor=5.0, damping=1)
-            time_loop(sh, m, x0, dyn, act, 2, delay=delay, rtol=1e-10, max_newton=30, forcing=1)   # warm-up
+            time_loop(sh, m, x0, dyn, act, 2, delay=delay, rtol=1e-10, max_newton=30)   # warm-up
             t0 = time.perf_counter()
-            x, rec = time_loop(sh, m, x0, dyn, act, steps, delay=delay, rtol=1e-10, max_newton=30, forcing=1)
+            x, rec = time_loop(sh, m, x0, dyn, act, steps, delay=delay, rtol=1e-10, max_newton=30)
             wall = time.perf_counter() - t0
             out[f"{w.name}_{tag}"] = {
                 "ms_per_time_step": wall / steps * 1e3, "steps": steps, "dt": dt,
