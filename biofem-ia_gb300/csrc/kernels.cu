@@ -66,6 +66,23 @@ __device__ __forceinline__ void gather_y(const double *pos, const int *patch, in
   }
 }
 
+/* gather_y for a group of 16 lanes sharing one element: lane l < 15 sums
+   component l (row l / 3, coordinate l % 3) in gather_y's order, then the
+   group exchanges the 15 sums, so every lane ends with gather_y's y at one
+   fifteenth of the FP64 work. */
+__device__ __forceinline__ void gather_y_group(const double *pos, const int *patch, int e, int nen, const double *tab,
+                                               int lane, double y[15])
+{
+  double s = 0.0;
+  if (lane < 15) {
+    const int r = lane / 3, d = lane - 3 * r;
+    const int *pe = patch + 16 * (size_t)e;
+    for (int i = 0; i < nen; i++) s += tab[r * 16 + i] * __ldg(pos + 4 * (size_t)__ldg(pe + i) + d);
+  }
+#pragma unroll
+  for (int c = 0; c < 15; c++) y[c] = __shfl_sync(0xffffffffu, s, c, 16);
+}
+
 /* ---------------- positions / ghosts ---------------- */
 __global__ void k_positions(int nv, int ng, const double *__restrict__ x, const int *__restrict__ ghost3,
                             double *__restrict__ pos)
@@ -250,7 +267,7 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   const int nen = info & 0xff, tabi = info >> 8;
   const double *tab = tabs + tabi * 80;
   double y[15];
-  gather_y(m.pos, m.patch, ee, nen, tab, y);
+  gather_y_group(m.pos, m.patch, ee, nen, tab, lane, y);
   D1d fd[15];
   int st = 0;
   const EPar<double> ep = epar<double>(p);
