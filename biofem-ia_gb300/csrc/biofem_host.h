@@ -94,10 +94,9 @@ int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, doub
                        double *parts = nullptr);
 int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double *th, void *stream);
 int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream);
-int launch_scale(const DevMesh &m, const KParams &p, double *R, double *K, void *stream);
+int launch_scale(const DevMesh &m, const KParams &p, double *R, void *stream);
 int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);
 int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream);
-int launch_scale_f32(const DevMesh &m, const KParams &p, double *R, float *K, void *stream);
 int launch_to_float(const double *a, float *b, long long n, void *stream);
 int launch_dyn_diag(const DevMesh &m, const KParams &p, void *stream);
 int launch_dyn_update(const DevMesh &m, const KParams &p, const double *x, void *stream);

@@ -673,7 +673,7 @@ int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void 
   if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
   if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
   if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 3); }
-  if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, nullptr, st); tmark(m, st, 4); }
+  if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 4); }
   if (rc) return fail(76, std::string("residual launch: ") + cudaGetErrorString((cudaError_t)rc));
   timer_collect(m);
   return 0;
@@ -695,7 +695,7 @@ int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_
     if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 3); }
     if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
     if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st); tmark(m, st, 5); }
-    if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, K, st); tmark(m, st, 6); }
+    if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   } else {
     /* FP32-bulk: residual in FP64, tangent (D, K_e, K) in FP32 */
     float *K = static_cast<float *>(d_K);
@@ -704,7 +704,7 @@ int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_
     if (!rc) { rc = launch_elem_tangent_f32(m->dm, m->kp, st); tmark(m, st, 3); }
     if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
     if (!rc) { rc = launch_block_gather_f32(m->dm, m->kp, K, st); tmark(m, st, 5); }
-    if (!rc) { rc = launch_scale_f32(m->dm, m->kp, d_R, K, st); tmark(m, st, 6); }
+    if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   }
   if (rc) return fail(76, std::string("jacobian launch: ") + cudaGetErrorString((cudaError_t)rc));
   timer_collect(m);
@@ -766,11 +766,20 @@ int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K
   if (!m || !x || !K) return fail(85, "null argument");
   const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
   const size_t kbytes = 9 * (size_t)m->nnzb * (m->prm.precision == BIOFEM_FP64 ? sizeof(double) : sizeof(float));
+  /* A page-locked, device-mapped K buffer (cudaHostAlloc / cudaMallocHost /
+     cudaHostRegister) is written by the block gather itself, each value once,
+     so the copy-out overlaps the assembly instead of following it. */
+  void *dK = m->d_K;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, K) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer)
+    dK = a.devicePointer;
+  else
+    cudaGetLastError();
   CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
-  int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, m->d_K, m->st);
+  int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, dK, m->st);
   if (rc) return rc;
   if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
-  CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, m->st));
+  if (dK == m->d_K) CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, m->st));
   return BiofemGpuSync(m, m->st);
 }
 
@@ -786,7 +795,7 @@ int RunGpuResidualParts(BiofemGpuMesh *m, const double *x, double *R, double *Fi
   int rc = launch_positions(m->dm, m->kp, m->d_x, st);
   if (!rc) rc = launch_elem_residual(m->dm, m->kp, st);
   if (!rc) rc = launch_node_gather(m->dm, m->kp, m->d_x, m->d_R, st, parts);
-  if (!rc) rc = launch_scale(m->dm, m->kp, m->d_R, nullptr, st);
+  if (!rc) rc = launch_scale(m->dm, m->kp, m->d_R, st);
   if (rc) {
     cudaFreeAsync(parts, st);
     return fail(76, std::string("residual launch: ") + cudaGetErrorString((cudaError_t)rc));

@@ -17,7 +17,8 @@
  *                    clamp rows R = x - X, ghost rows 0 (main.c:844-1016)
  *   k_block_gather   one thread per tangent value: sum of the element-matrix
  *                    entries mapped to that 3x3 block, in element order
- *   k_scale          R, K *= 1 / max(|Fext|_inf, 1) (main.c:1020-1026)
+ *   k_scale          R *= 1 / max(|Fext|_inf, 1) (main.c:1020-1026); the block
+ *                    gathers apply the same factor to K as they write it
  *
  * Assembly is deterministic: every sum runs in a fixed order given by the
  * precomputed element-to-node / element-to-block maps, independent of the
@@ -469,17 +470,14 @@ __global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K)
     }
     if (p.dyn && m.colind[k] == row && (w == 0 || w == 4 || w == 8)) s += (float)m.dyn_diag[row];
   }
-  K[t] = s;
-}
-
-__global__ void k_scale_f32(DevMesh m, KParams p, double *__restrict__ R, float *__restrict__ K)
-{
+  /* R and K scale by 1/max(|Fext|_inf, 1) (main.c:1020-1026; k_node_gather
+     found the max); ghost rows stay identity */
   const double fmax = __longlong_as_double((long long)*m.fmax);
-  if (!(fmax > 1.0)) return;
-  const double sc = 1.0 / fmax;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < 3LL * p.nt) R[t] = R[t] * sc;
-  if (t < 9 * m.nnzb && m.rowkind[m.blkrow[t / 9]] != 2) K[t] = (float)(K[t] * sc);
+  if (fmax > 1.0 && kind != 2) {
+    const double sc = 1.0 / fmax;
+    s = (float)(s * sc);
+  }
+  K[t] = s;
 }
 
 /* ---------------- node gather (residual assembly) ---------------- */
@@ -588,21 +586,24 @@ __global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
     }
     if (p.dyn && m.colind[k] == row && (w == 0 || w == 4 || w == 8)) s += m.dyn_diag[row];
   }
+  /* the scale 1/max(|Fext|_inf, 1) of R and K (main.c:1020-1026; k_node_gather
+     found the max), applied as the value is written; ghost rows stay identity */
+  const double fmax = __longlong_as_double((long long)*m.fmax);
+  if (fmax > 1.0 && kind != 2) {
+    const double sc = 1.0 / fmax;
+    s = s * sc;
+  }
   K[t] = s;
 }
 
 /* ---------------- scaling ---------------- */
-__global__ void k_scale(DevMesh m, KParams p, double *__restrict__ R, double *__restrict__ K)
+__global__ void k_scale(DevMesh m, KParams p, double *__restrict__ R)
 {
   const double fmax = __longlong_as_double((long long)*m.fmax);
   if (!(fmax > 1.0)) return;
   const double sc = 1.0 / fmax;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long nR = 3LL * p.nt;
-  if (t < nR) R[t] = R[t] * sc;
-  if (K && t < 9 * m.nnzb) {
-    if (m.rowkind[m.blkrow[t / 9]] != 2) K[t] = K[t] * sc;
-  }
+  if (t < 3LL * p.nt) R[t] = R[t] * sc;
 }
 
 /* ---------------- launchers ---------------- */
@@ -642,14 +643,6 @@ int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *
 {
   if (m.nnzb == 0) return 0;
   k_block_gather_f32<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K);
-  return (int)cudaGetLastError();
-}
-
-int launch_scale_f32(const DevMesh &m, const KParams &p, double *R, float *K, void *stream)
-{
-  long long n = 3LL * p.nt;
-  if (9 * m.nnzb > n) n = 9 * m.nnzb;
-  k_scale_f32<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(m, p, R, K);
   return (int)cudaGetLastError();
 }
 
@@ -748,11 +741,9 @@ int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *str
   return (int)cudaGetLastError();
 }
 
-int launch_scale(const DevMesh &m, const KParams &p, double *R, double *K, void *stream)
+int launch_scale(const DevMesh &m, const KParams &p, double *R, void *stream)
 {
-  long long n = 3LL * p.nt;
-  if (K && 9 * m.nnzb > n) n = 9 * m.nnzb;
-  k_scale<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(m, p, R, K);
+  k_scale<<<blocks_for(3LL * p.nt, 256), 256, 0, (cudaStream_t)stream>>>(m, p, R);
   return (int)cudaGetLastError();
 }
 

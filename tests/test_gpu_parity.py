@@ -144,3 +144,25 @@ def test_kinematic_checks_C1():
     R2 = sh.form_function(X + d)
     assert R2[3 * bn[0]] == pytest.approx(1e-3, rel=0, abs=1e-18)
     sh.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32_bulk"])
+def test_host_call_into_pinned_buffers(precision):
+    """RunGpuResidualJacobian with page-locked host buffers: the block gather
+    writes K straight into the mapped buffer; R and K equal the pageable-buffer
+    call bitwise."""
+    import torch
+    from biofem.gpu import GpuShell
+    w = configs.small(10, 8, activation="random", index=48, pressure=300.0)   # max|Fext| > 1: R and K scaled
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=precision)
+    x = w.initial_x(m, sh.topology()["xyz0_full"])
+    R, K = sh.form_jacobian(x)
+    hx = torch.tensor(x).pin_memory()
+    hR = torch.empty(sh.n_dof, dtype=torch.float64).pin_memory()
+    kdt = torch.float64 if precision == 0 else torch.float32
+    hK = torch.full((9 * sh.nnzb,), float("nan"), dtype=kdt).pin_memory()
+    sh.residual_jacobian_host_ptrs(hx.data_ptr(), hR.data_ptr(), hK.data_ptr())
+    np.testing.assert_array_equal(hR.numpy(), R)
+    np.testing.assert_array_equal(hK.numpy().reshape(K.shape), K)
+    sh.close()
