@@ -82,13 +82,14 @@ struct DevMesh {
   int *dptr, *didx;          /* per node, the triangles with that corner (ghost and bridging ones included), in triangle order */
   double *xn, *xnm1, *xd, *xdd;   /* 3*nt dynamic state (previous positions, velocity, acceleration) */
   double *dyn_diag;          /* nt: d Fdyn / d x on the diagonal of each free row */
+  double *gmq;               /* FP64 handles: 6 nq x ne thickness-point metrics, k_elem_residual -> k_elem_tangent */
   unsigned long long *fmax;  /* max |Fext| as ordered bits */
 };
 
 /* kernel launchers (kernels.cu); return cudaError_t as int */
 int launch_ref_prep(const DevMesh &m, const KParams &p, const double *fib, const double *gscale, double *eref_out, void *stream);
 int launch_positions(const DevMesh &m, const KParams &p, const double *x, void *stream);
-int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream);
+int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream, bool store_metric = false);
 int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream);
 int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream,
                        double *parts = nullptr);

@@ -552,7 +552,8 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   float *d_erefF = nullptr;
   if (params->precision == BIOFEM_FP64) {
     double *dK = nullptr;
-    if ((rc = dalloc(m, &dm.ke, 9 * keblocks)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb))) { free_mesh(m); return rc; }
+    if ((rc = dalloc(m, &dm.ke, 9 * keblocks)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb)) ||
+        (rc = dalloc(m, &dm.gmq, 6 * (size_t)kp.nq * ne))) { free_mesh(m); return rc; }
     m->d_K = dK;
   } else {
     float *dK = nullptr;
@@ -691,7 +692,7 @@ int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_
        the residual call's R */
     double *K = static_cast<double *>(d_K);
     if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
-    if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
+    if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st, true); tmark(m, st, 2); }
     if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 3); }
     if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
     if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st); tmark(m, st, 5); }

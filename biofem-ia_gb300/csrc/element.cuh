@@ -335,7 +335,7 @@ __host__ __device__ __forceinline__ void elem_out(const ElemGeom<T> &g, T N0, T 
    ref points at the element's first SoA constant (type R); stride = ne. */
 template <class T, class R>
 __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R> &p, const R *ref, int stride,
-                                                     T f[15], int &status)
+                                                     T f[15], int &status, R *gm_out = nullptr)
 {
   const ElemGeom<T> g = elem_geom<T, R>(y, p);
   const int nq = p.nq;
@@ -350,6 +350,8 @@ __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R
     const R th3 = p.hhalf * p.theta[q];
     T gm[6];
     qp_metric(g, th3, gm);
+    if (gm_out)   /* the metric of every thickness point, SoA over elements, for the tangent */
+      for (int c = 0; c < 6; c++) gm_out[(size_t)(6 * q + c) * stride] = val(gm[c]);
     T sv[3];
     qp_stress(gm, r, gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
     const R wq = p.w[q], wt = p.w[q] * th3;
@@ -395,8 +397,8 @@ __host__ __device__ __forceinline__ int metric_dirs(const EPar<R> &p) { return p
    with KD metric directions (the last job of a point may carry unused
    directions); jac layout as in elem_forces_split. */
 template <class R, int KD>
-__device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> &g0, const EPar<R> &p, const R *ref, int stride,
-                                                  int lane, R gam, R gamp, R c1, R *jac, int &status)
+__device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> *g0, const R *gmq, const EPar<R> &p, const R *ref,
+                                                  int stride, int lane, R gam, R gamp, R c1, R *jac, int &status)
 {
   typedef DK<R, KD> T;
   const int ndirs = metric_dirs(p);
@@ -404,7 +406,12 @@ __device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> &g0, const E
   for (int job = lane; job < per_q * p.nq; job += 16) {
     const int q = job / per_q, k0 = (job - per_q * q) * KD;
     R gmv[6];
-    qp_metric(g0, p.hhalf * p.theta[q], gmv);
+    if (gmq) {
+#pragma unroll
+      for (int c = 0; c < 6; c++) gmv[c] = gmq[(size_t)(6 * q + c) * stride];
+    } else {
+      qp_metric(*g0, p.hhalf * p.theta[q], gmv);
+    }
     T gm[6];
 #pragma unroll
     for (int c = 0; c < 6; c++) {
@@ -441,7 +448,7 @@ __device__ __forceinline__ void constitutive_jobs(const ElemGeom<R> &g0, const E
    warp). */
 template <class R>
 __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &p, const R *ref, int stride, int lane,
-                                                  R *jac, D1<R> f[15], int &status)
+                                                  R *jac, D1<R> f[15], int &status, const R *gmq = nullptr)
 {
   typedef D1<R> T;
   const int nq = p.nq;
@@ -453,15 +460,18 @@ __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &
      jac[q*21 + 18 + i] = sv_i; FP64: KD metric directions per job, the fewest
      for which the ceil(ndirs / KD) nq jobs fit one round of 16 lanes */
   {
-    const ElemGeom<R> g0 = elem_geom<R, R>(y, p);
+    /* the primal metric of each thickness point: stored by the residual
+       kernel of the same call (gmq), or from the element geometry here */
+    ElemGeom<R> g0;
+    if (!gmq) g0 = elem_geom<R, R>(y, p);
     if constexpr (sizeof(R) == 4) {
       /* FP32: one direction per job (wider duals spill under the FP32 kernel's register cap) */
-      constitutive_jobs<R, 1>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      constitutive_jobs<R, 1>(&g0, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
     } else {
       const int ndirs = metric_dirs(p);
-      if (ndirs * nq <= 16) constitutive_jobs<R, 1>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
-      else if (((ndirs + 1) / 2) * nq <= 16) constitutive_jobs<R, 2>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
-      else constitutive_jobs<R, 3>(g0, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      if (ndirs * nq <= 16) constitutive_jobs<R, 1>(&g0, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      else if (((ndirs + 1) / 2) * nq <= 16) constitutive_jobs<R, 2>(&g0, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
+      else constitutive_jobs<R, 3>(&g0, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
     }
   }
   __syncwarp();

@@ -203,7 +203,7 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
 }
 
 /* ---------------- residual element kernel ---------------- */
-__global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p)
+__global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, double *__restrict__ gm_out)
 {
   __shared__ double tabs[kNumTables * 80];
   for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p)
   double f[15];
   int st = 0;
   const EPar<double> ep = epar<double>(p);
-  elem_forces<double, double>(y, ep, m.eref + e, p.ne, f, st);
+  elem_forces<double, double>(y, ep, m.eref + e, p.ne, f, st, gm_out ? gm_out + e : nullptr);
   set_status(m.status, st);
   /* Fb_a = sum_r N[r][a] f_r, stored slot-major: fb[(3a+d)*ne + e] */
   const size_t ne = p.ne;
@@ -272,7 +272,8 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   D1d fd[15];
   int st = 0;
   const EPar<double> ep = epar<double>(p);
-  elem_forces_split<double>(y, ep, m.eref + ee, p.ne, lane, Jsh[slot], fd, st);
+  /* the thickness-point metrics come from k_elem_residual, launched before this kernel */
+  elem_forces_split<double>(y, ep, m.eref + ee, p.ne, lane, Jsh[slot], fd, st, m.gmq + ee);
   if (live) set_status(m.status, st);
   const size_t ne = p.ne;
   /* column `lane` of D = df/dy */
@@ -453,6 +454,7 @@ __global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K)
   if (t >= 9 * m.nnzb) return;
   const long long k = t / 9;
   const int w = (int)(t - 9 * k);
+  const double fmax = __longlong_as_double((long long)*m.fmax);   /* read early: its latency hides under the sum */
   const int row = m.blkrow[k];
   const int kind = m.rowkind[row];
   float s = 0.f;
@@ -472,7 +474,6 @@ __global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K)
   }
   /* R and K scale by 1/max(|Fext|_inf, 1) (main.c:1020-1026; k_node_gather
      found the max); ghost rows stay identity */
-  const double fmax = __longlong_as_double((long long)*m.fmax);
   if (fmax > 1.0 && kind != 2) {
     const double sc = 1.0 / fmax;
     s = (float)(s * sc);
@@ -559,6 +560,7 @@ __global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
   if (t >= 9 * m.nnzb) return;
   const long long k = t / 9;
   const int w = (int)(t - 9 * k);
+  const double fmax = __longlong_as_double((long long)*m.fmax);   /* read early: its latency hides under the sum */
   const int row = m.blkrow[k];
   const int kind = m.rowkind[row];
   double s = 0.0;
@@ -588,7 +590,6 @@ __global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
   }
   /* the scale 1/max(|Fext|_inf, 1) of R and K (main.c:1020-1026; k_node_gather
      found the max), applied as the value is written; ghost rows stay identity */
-  const double fmax = __longlong_as_double((long long)*m.fmax);
   if (fmax > 1.0 && kind != 2) {
     const double sc = 1.0 / fmax;
     s = s * sc;
@@ -621,9 +622,9 @@ int launch_positions(const DevMesh &m, const KParams &p, const double *x, void *
   return (int)cudaGetLastError();
 }
 
-int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream)
+int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream, bool store_metric)
 {
-  k_elem_residual<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p);
+  k_elem_residual<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p, store_metric ? m.gmq : nullptr);
   return (int)cudaGetLastError();
 }
 
