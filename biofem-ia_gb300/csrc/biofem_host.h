@@ -70,6 +70,7 @@ struct DevMesh {
   const int *rowptr, *colind, *blkrow;   /* BSR pattern; block -> row */
   const long long *cptr;     /* nnzb+1 */
   const int *cidx;           /* contribution: Ke block id, negative = subtract (-(id+1)) */
+  const int *gperm;          /* nnzb: the gathers' block order (each row's blocks by decreasing count) */
   long long nnzb;
   /* work arrays */
   double *pos;               /* 4*nt padded positions */
@@ -94,10 +95,10 @@ int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream);
 int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream,
                        double *parts = nullptr);
 int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double *th, void *stream);
-int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream);
+int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream, bool k_on_host = false);
 int launch_scale(const DevMesh &m, const KParams &p, double *R, void *stream);
 int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);
-int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream);
+int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream, bool k_on_host = false);
 int launch_to_float(const double *a, float *b, long long n, void *stream);
 int launch_dyn_diag(const DevMesh &m, const KParams &p, void *stream);
 int launch_dyn_update(const DevMesh &m, const KParams &p, const double *x, void *stream);

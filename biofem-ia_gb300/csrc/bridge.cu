@@ -535,7 +535,19 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
 #define UP(field, vec) do { rc = dupload(m, const_cast<std::remove_const<std::remove_pointer<decltype(dm.field)>::type>::type **>(&dm.field), vec); if (rc) { free_mesh(m); return rc; } } while (0)
   UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3); UP(kofs, kofs);
   UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(pptr, pptr); UP(pidx, pidx);
-  UP(rowptr, m->rowptr); UP(colind, m->colind); UP(blkrow, blkrow); UP(cptr, cptr); UP(cidx, cidx);
+  /* block order of the gathers: within each row, blocks by decreasing
+     contribution count, so the threads of a warp run loops of nearly one
+     length (in row order a warp's blocks range from the diagonal, with the
+     most contributions, to the far ones; the loop's FP64 adds occupy the
+     pipe for every lane of the warp); writes stay inside the row */
+  std::vector<int> gperm((size_t)m->nnzb);
+  for (int i = 0; i < nt; i++) {
+    const int k0 = m->rowptr[i], k1 = m->rowptr[i + 1];
+    for (int k = k0; k < k1; k++) gperm[k] = k;
+    std::stable_sort(gperm.begin() + k0, gperm.begin() + k1,
+                     [&](int a, int b) { return cptr[a + 1] - cptr[a] > cptr[b + 1] - cptr[b]; });
+  }
+  UP(rowptr, m->rowptr); UP(colind, m->colind); UP(blkrow, blkrow); UP(cptr, cptr); UP(cidx, cidx); UP(gperm, gperm);
 #undef UP
   dm.nnzb = m->nnzb;
   double *d_fib = nullptr, *d_gsc = nullptr, *d_eref = nullptr;
@@ -680,7 +692,15 @@ int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void 
   return 0;
 }
 
+static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream, bool k_on_host);
+
 int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream)
+{
+  return residual_jacobian(m, d_x, d_R, d_K, stream, false);
+}
+
+/* k_on_host: d_K is the device view of a mapped page-locked host buffer */
+static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream, bool k_on_host)
 {
   if (!m || !d_x || !d_R || !d_K) return fail(85, "null argument");
   if (!m->dm.patch) return fail(58, "host-only handle");
@@ -695,7 +715,7 @@ int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_
     if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st, true); tmark(m, st, 2); }
     if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 3); }
     if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
-    if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st); tmark(m, st, 5); }
+    if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st, k_on_host); tmark(m, st, 5); }
     if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   } else {
     /* FP32-bulk: residual in FP64, tangent (D, K_e, K) in FP32 */
@@ -704,7 +724,7 @@ int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_
     if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
     if (!rc) { rc = launch_elem_tangent_f32(m->dm, m->kp, st); tmark(m, st, 3); }
     if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
-    if (!rc) { rc = launch_block_gather_f32(m->dm, m->kp, K, st); tmark(m, st, 5); }
+    if (!rc) { rc = launch_block_gather_f32(m->dm, m->kp, K, st, k_on_host); tmark(m, st, 5); }
     if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   }
   if (rc) return fail(76, std::string("jacobian launch: ") + cudaGetErrorString((cudaError_t)rc));
@@ -777,7 +797,7 @@ int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K
   else
     cudaGetLastError();
   CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
-  int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, dK, m->st);
+  int rc = residual_jacobian(m, m->d_x, m->d_R, dK, m->st, dK != m->d_K);
   if (rc) return rc;
   if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
   if (dK == m->d_K) CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, m->st));

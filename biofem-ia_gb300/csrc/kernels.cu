@@ -448,12 +448,13 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
 }
 
 /* FP32 block gather with compensated (Kahan) summation in element order. */
-__global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K)
+__global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K, const int *__restrict__ perm)
 {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 9 * m.nnzb) return;
-  const long long k = t / 9;
-  const int w = (int)(t - 9 * k);
+  const long long kk = t / 9;
+  const int w = (int)(t - 9 * kk);
+  const long long k = perm ? perm[kk] : kk;
   const double fmax = __longlong_as_double((long long)*m.fmax);   /* read early: its latency hides under the sum */
   const int row = m.blkrow[k];
   const int kind = m.rowkind[row];
@@ -478,7 +479,7 @@ __global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K)
     const double sc = 1.0 / fmax;
     s = (float)(s * sc);
   }
-  K[t] = s;
+  K[9 * k + w] = s;
 }
 
 /* ---------------- node gather (residual assembly) ---------------- */
@@ -554,12 +555,13 @@ __global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x
 }
 
 /* ---------------- block gather (tangent assembly) ---------------- */
-__global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
+__global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K, const int *__restrict__ perm)
 {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 9 * m.nnzb) return;
-  const long long k = t / 9;
-  const int w = (int)(t - 9 * k);
+  const long long kk = t / 9;
+  const int w = (int)(t - 9 * kk);
+  const long long k = perm ? perm[kk] : kk;   /* blocks of one row by decreasing contribution count */
   const double fmax = __longlong_as_double((long long)*m.fmax);   /* read early: its latency hides under the sum */
   const int row = m.blkrow[k];
   const int kind = m.rowkind[row];
@@ -594,7 +596,7 @@ __global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K)
     const double sc = 1.0 / fmax;
     s = s * sc;
   }
-  K[t] = s;
+  K[9 * k + w] = s;
 }
 
 /* ---------------- scaling ---------------- */
@@ -640,10 +642,10 @@ int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream)
   return (int)cudaGetLastError();
 }
 
-int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream)
+int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream, bool k_on_host)
 {
   if (m.nnzb == 0) return 0;
-  k_block_gather_f32<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K);
+  k_block_gather_f32<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K, k_on_host ? nullptr : m.gperm);
   return (int)cudaGetLastError();
 }
 
@@ -735,10 +737,12 @@ int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, doub
   return (int)cudaGetLastError();
 }
 
-int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream)
+int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream, bool k_on_host)
 {
   if (m.nnzb == 0) return 0;
-  k_block_gather<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K);
+  /* K in HBM: each row's blocks by decreasing contribution count; K in mapped
+     host memory: plain block order, so the stores stream out in address order */
+  k_block_gather<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K, k_on_host ? nullptr : m.gperm);
   return (int)cudaGetLastError();
 }
 
