@@ -573,20 +573,25 @@ __global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K, con
     const long long cend = m.cptr[k + 1];
     /* four gathered loads in flight per step; the sum keeps the list order
        (s - v and s + (-v) round alike) */
+    /* the sign of a chain-rule contribution is flipped on the integer pipe
+       (the FP64 pipe, which bounds this kernel, then sees one add each) */
     for (; c + 4 <= cend; c += 4) {
       double v[4];
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         const int id = m.cidx[c + u];
-        v[u] = id >= 0 ? m.ke[(size_t)id * 9 + w] : -m.ke[(size_t)(-(id + 1)) * 9 + w];
+        const long long neg = (long long)(id < 0) << 63;
+        const long long bits = __double_as_longlong(m.ke[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]);
+        v[u] = __longlong_as_double(bits ^ neg);
       }
 #pragma unroll
       for (int u = 0; u < 4; u++) s += v[u];
     }
     for (; c < cend; c++) {
       const int id = m.cidx[c];
-      if (id >= 0) s += m.ke[(size_t)id * 9 + w];
-      else s -= m.ke[(size_t)(-(id + 1)) * 9 + w];
+      const long long neg = (long long)(id < 0) << 63;
+      const long long bits = __double_as_longlong(m.ke[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]);
+      s += __longlong_as_double(bits ^ neg);
     }
     if (p.dyn && m.colind[k] == row && (w == 0 || w == 4 || w == 8)) s += m.dyn_diag[row];
   }
