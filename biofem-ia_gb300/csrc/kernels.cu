@@ -465,7 +465,8 @@ __global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K, 
     float comp = 0.f;
     for (long long c = m.cptr[k]; c < m.cptr[k + 1]; c++) {
       const int id = m.cidx[c];
-      const float v = id >= 0 ? m.keF[(size_t)id * 9 + w] : -m.keF[(size_t)(-(id + 1)) * 9 + w];
+      const int neg = (int)((unsigned)(id < 0) << 31);   /* sign flip of a chain-rule contribution, integer pipe */
+      const float v = __int_as_float(__float_as_int(m.keF[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]) ^ neg);
       const float yv = v - comp;
       const float tt = s + yv;
       comp = (tt - s) - yv;
