@@ -37,10 +37,10 @@ for _p in (ROOT, ROOT / "biofem-ia_gb300"):
 
 METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_elem_tangent launch on
-# the 256x192 workload (ncu --set full; 62.8 MB read, 1,064 MB written)
-TANGENT_DRAM_BYTES_C2 = 62.756e6 + 1063.924e6
+# the 256x192 workload (ncu --set full; 76.4 MB read, 1,055 MB written)
+TANGENT_DRAM_BYTES_C2 = 76.383e6 + 1054.585e6
 # sm__pipe_fp64_cycles_active (of peak sustained active) of the same capture
-FP64_PIPE_ACTIVE_C2 = 0.901
+FP64_PIPE_ACTIVE_C2 = 0.888
 UNIT = "elems/s"
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_ELEMS = 2048
