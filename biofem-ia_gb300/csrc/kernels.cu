@@ -463,7 +463,26 @@ __global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K, 
     s = (m.colind[k] == row && (w == 0 || w == 4 || w == 8)) ? 1.f : 0.f;
   } else {
     float comp = 0.f;
-    for (long long c = m.cptr[k]; c < m.cptr[k + 1]; c++) {
+    long long c = m.cptr[k];
+    const long long cend = m.cptr[k + 1];
+    /* four gathered loads in flight per step; the compensated sum keeps the list order */
+    for (; c + 4 <= cend; c += 4) {
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int id = m.cidx[c + u];
+        const int neg = (int)((unsigned)(id < 0) << 31);
+        v[u] = __int_as_float(__float_as_int(m.keF[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]) ^ neg);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const float yv = v[u] - comp;
+        const float tt = s + yv;
+        comp = (tt - s) - yv;
+        s = tt;
+      }
+    }
+    for (; c < cend; c++) {
       const int id = m.cidx[c];
       const int neg = (int)((unsigned)(id < 0) << 31);   /* sign flip of a chain-rule contribution, integer pipe */
       const float v = __int_as_float(__float_as_int(m.keF[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]) ^ neg);
