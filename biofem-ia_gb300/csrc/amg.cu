@@ -51,13 +51,30 @@ __device__ __forceinline__ void row_apply(const int *__restrict__ rowptr, const 
     for (int k = rowptr[row] + q; k < k1; k += 16) {
       const int c = colind[k];
       const float *a = A + (size_t)k * BS * BS;
-      float xv[BS];
+      float xv[BS], av[BS * BS];
+      if constexpr (BS == 6) {
+        /* a 6x6 block is 144 bytes and a 6-vector 24 bytes, so the block
+           comes in nine 16-byte loads and the vector in three 8-byte ones */
 #pragma unroll
-      for (int s = 0; s < BS; s++) xv[s] = x[(size_t)c * BS + s];
+        for (int j = 0; j < 9; j++) {
+          const float4 v4 = __ldg(reinterpret_cast<const float4 *>(a) + j);
+          av[4 * j] = v4.x; av[4 * j + 1] = v4.y; av[4 * j + 2] = v4.z; av[4 * j + 3] = v4.w;
+        }
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          const float2 v2 = *(reinterpret_cast<const float2 *>(x + (size_t)c * BS) + j);
+          xv[2 * j] = v2.x; xv[2 * j + 1] = v2.y;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < BS * BS; j++) av[j] = a[j];
+#pragma unroll
+        for (int s = 0; s < BS; s++) xv[s] = x[(size_t)c * BS + s];
+      }
 #pragma unroll
       for (int r = 0; r < BS; r++)
 #pragma unroll
-        for (int s = 0; s < BS; s++) acc[r] = fmaf(a[r * BS + s], xv[s], acc[r]);
+        for (int s = 0; s < BS; s++) acc[r] = fmaf(av[r * BS + s], xv[s], acc[r]);
     }
   }
 #pragma unroll
