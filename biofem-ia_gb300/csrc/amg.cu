@@ -98,6 +98,38 @@ __device__ __forceinline__ void dmul(const float *__restrict__ D, int i, const f
 
 __device__ __forceinline__ bool is_done(const int *done) { return done && *(volatile const int *)done; }
 
+/* A prolongation block of BS x 6 floats: the 144-byte blocks of BS = 6 start
+   on 16 bytes, the 72-byte blocks of BS = 3 on 8 bytes (cudaMalloc bases,
+   whole blocks per index). */
+template <int BS>
+__device__ __forceinline__ void load_pblock(const float *__restrict__ p, float out[BS * kAmgCoarseBs])
+{
+  static_assert(kAmgCoarseBs == 6, "block loads assume 6 coarse components");
+  if constexpr (BS == 6) {
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+      const float4 v = __ldg(reinterpret_cast<const float4 *>(p) + j);
+      out[4 * j] = v.x; out[4 * j + 1] = v.y; out[4 * j + 2] = v.z; out[4 * j + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < BS * 3; j++) {
+      const float2 v = __ldg(reinterpret_cast<const float2 *>(p) + j);
+      out[2 * j] = v.x; out[2 * j + 1] = v.y;
+    }
+  }
+}
+
+/* a 6-component node vector (24 bytes, 8-byte aligned) */
+__device__ __forceinline__ void load6(const float *__restrict__ v, float out[6])
+{
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const float2 w = reinterpret_cast<const float2 *>(v)[j];
+    out[2 * j] = w.x; out[2 * j + 1] = w.y;
+  }
+}
+
 /* ---------------- numeric setup kernels ---------------- */
 __global__ void k_to_f32(long long n, const double *__restrict__ a, float *__restrict__ b)
 {
@@ -598,12 +630,18 @@ __global__ void __launch_bounds__(256) k_restrict(int na, const int *__restrict_
   for (int c = 0; c < C; c++) acc[c] = 0.f;
   for (int t = rrow[I] + lane; t < rrow[I + 1]; t += 32) {
     const int i = rcol[t];
-    const float *p = P + (size_t)rmap[t] * BS * C;
+    float pb[BS * C], rv[BS];
+    load_pblock<BS>(P + (size_t)rmap[t] * BS * C, pb);
+    if constexpr (BS == 6) {
+      load6(res + (size_t)i * BS, rv);
+    } else {
+#pragma unroll
+      for (int s = 0; s < BS; s++) rv[s] = res[(size_t)i * BS + s];
+    }
 #pragma unroll
     for (int s = 0; s < BS; s++) {
-      const float rs = res[(size_t)i * BS + s];
 #pragma unroll
-      for (int c = 0; c < C; c++) acc[c] = fmaf(p[s * C + c], rs, acc[c]);
+      for (int c = 0; c < C; c++) acc[c] = fmaf(pb[s * C + c], rv[s], acc[c]);
     }
   }
 #pragma unroll
@@ -631,15 +669,13 @@ __global__ void k_prolong(int n, const int *__restrict__ prow, const int *__rest
 #pragma unroll
   for (int s = 0; s < BS; s++) acc[s] = 0.f;
   for (int k = prow[i]; k < prow[i + 1]; k++) {
-    const float *p = P + (size_t)k * BS * C;
-    const float *xv = xc + (size_t)pcol[k] * C;
-    float xl[C];
-#pragma unroll
-    for (int c = 0; c < C; c++) xl[c] = xv[c];
+    float pb[BS * C], xl[C];
+    load_pblock<BS>(P + (size_t)k * BS * C, pb);
+    load6(xc + (size_t)pcol[k] * C, xl);
 #pragma unroll
     for (int s = 0; s < BS; s++)
 #pragma unroll
-      for (int c = 0; c < C; c++) acc[s] = fmaf(p[s * C + c], xl[c], acc[s]);
+      for (int c = 0; c < C; c++) acc[s] = fmaf(pb[s * C + c], xl[c], acc[s]);
   }
 #pragma unroll
   for (int s = 0; s < BS; s++) x[(size_t)i * BS + s] += acc[s];
