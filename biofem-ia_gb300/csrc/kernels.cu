@@ -8,17 +8,23 @@
  *   k_elem_residual  one thread per element: geometry, closed-form stress,
  *                    element forces Fb (ElemUpdFint) and the follower-pressure
  *                    corner force (SurfaceNormalPressure, external.c:589-624)
- *   k_elem_tangent   16 lanes per element: lane j carries d/dy_j through the
- *                    same code (forward mode), giving column j of df/dy; the
- *                    half-warp then forms K_e = N^T (df/dy) N in shared memory
- *   k_node_gather    one thread per node: Fint / Fext summed over the node's
- *                    element contributions in element order (the order
- *                    FInternalAct's VecSetValues loop adds them), R = Fint - Fext,
- *                    clamp rows R = x - X, ghost rows 0 (main.c:844-1016)
+ *                    (and, for the tangent, the thickness-point metrics)
+ *   k_elem_tangent   16 lanes per element: the stress is differentiated along
+ *                    the metric components of each thickness point (one job
+ *                    per lane), then lane j carries d/dy_j through the
+ *                    geometry and the chain rule, giving column j of df/dy;
+ *                    the half-warp then forms K_e = N^T (df/dy) N in shared memory
+ *   k_node_gather    one thread per node: Fint / Fext (and FDynamic's Fdyn)
+ *                    summed over the node's element contributions in element
+ *                    order (the order FInternalAct's VecSetValues loop adds
+ *                    them), R = Fint - Fext + Fdyn, clamp rows R = x - X,
+ *                    ghost rows 0 (main.c:844-1016)
  *   k_block_gather   one thread per tangent value: sum of the element-matrix
  *                    entries mapped to that 3x3 block, in element order
  *   k_scale          R *= 1 / max(|Fext|_inf, 1) (main.c:1020-1026); the block
  *                    gathers apply the same factor to K as they write it
+ *   k_elem_thickness UpdateElementThickness (output); k_dyn_diag / k_dyn_update
+ *                    the dynamic term's tangent diagonal and xAccVel
  *
  * Assembly is deterministic: every sum runs in a fixed order given by the
  * precomputed element-to-node / element-to-block maps, independent of the
