@@ -286,6 +286,30 @@ __host__ __device__ __forceinline__ ElemGeom<T> elem_geom(const T y[15], const E
   return g;
 }
 
+/* Primal geometry the FP64 tangent's chain rule reads, stored once per element
+   by the residual kernel of the same call (SoA over elements): n, 1/|a1 x a2|,
+   t1 = a2 x n, t2 = n x a1, 1/(a1.t1), 1/(a2.t2), u31 = Aaa x a2 + a1 x Aab,
+   u32 = Aab x a2 + a1 x Abb (elem_geom's intermediates); kGeomPrimal values. */
+
+template <class R>
+__host__ __device__ __forceinline__ void elem_geom_store(const R y[15], R *gp, size_t stride)
+{
+  const R one = R(1);
+  const V3<R> a1 = {y[0], y[1], y[2]}, a2 = {y[3], y[4], y[5]};
+  const V3<R> Aaa = {y[6], y[7], y[8]}, Abb = {y[9], y[10], y[11]}, Aab = {y[12], y[13], y[14]};
+  const V3<R> cr = cross(a1, a2);
+  const R cn = dsqrt(dot(cr, cr));
+  const R icn = one / cn;
+  const V3<R> n = scl(icn, cr);
+  const V3<R> t1 = cross(a2, n), t2 = cross(n, a1);
+  const R s1 = one / dot(a1, t1), s2 = one / dot(a2, t2);
+  const V3<R> u31 = cross(Aaa, a2) + cross(a1, Aab), u32 = cross(Aab, a2) + cross(a1, Abb);
+  const R v[kGeomPrimal] = {n.x, n.y, n.z, icn, t1.x, t1.y, t1.z, t2.x, t2.y, t2.z, s1, s2,
+                            u31.x, u31.y, u31.z, u32.x, u32.y, u32.z};
+#pragma unroll
+  for (int k = 0; k < kGeomPrimal; k++) gp[k * stride] = v[k];
+}
+
 /* Metric (00 11 01 02 12 22) of the thickness point theta3 (ElemUpdateG). */
 template <class T, class R>
 __host__ __device__ __forceinline__ void qp_metric(const ElemGeom<T> &g, R th3, T gm[6])
@@ -500,6 +524,111 @@ __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &
     M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
   }
   elem_out(g, N0, N1, N2, M0, M1, M2, pref0, f);
+}
+
+/* The chain rule of elem_forces_split along y_lane in tangent-linear form: the
+   primal geometry comes from elem_geom_store (gp, SoA stride), the primal
+   resultants from the constitutive jobs (jac), so only derivatives are
+   computed here (the dual form recomputes every primal value in every lane).
+   The derivatives follow elem_geom, qp_metric and elem_out operation by
+   operation:
+     dcr = da1 x a2 + a1 x da2,  d|cr| = n.dcr,  dn = (dcr - n d|cr|)/|cr|,
+     d(1/|cr|) = -d|cr|/|cr|^2,  dt1 = da2 x n + a2 x dn,
+     d(1/(a1.t1)) = -(da1.t1 + a1.dt1)/(a1.t1)^2,  gc1 = t1/(a1.t1), ...
+   df holds d f_r / d y_lane. */
+template <class R>
+__device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R> &p, const R *ref, int stride,
+                                                     const R *gp, int lane, R *jac, R df[15], int &status,
+                                                     const R *gmq)
+{
+  const int nq = p.nq;
+  const R gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];
+  const R gamp = ref[(size_t)(kRefPerQp * nq + 1) * stride];
+  const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
+  const R pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
+  const int ndirs = metric_dirs(p);
+  if (ndirs * nq <= 16) constitutive_jobs<R, 1>(nullptr, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
+  else if (((ndirs + 1) / 2) * nq <= 16) constitutive_jobs<R, 2>(nullptr, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
+  else constitutive_jobs<R, 3>(nullptr, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
+  __syncwarp();
+  const R one = R(1), two = R(2);
+  R g[kGeomPrimal];
+#pragma unroll
+  for (int k = 0; k < kGeomPrimal; k++) g[k] = gp[(size_t)k * stride];
+  const V3<R> n = {g[0], g[1], g[2]}, t1 = {g[4], g[5], g[6]}, t2 = {g[7], g[8], g[9]};
+  const R icn = g[3], s1 = g[10], s2 = g[11];
+  const V3<R> u31 = {g[12], g[13], g[14]}, u32 = {g[15], g[16], g[17]};
+  const V3<R> a1 = {y[0], y[1], y[2]}, a2 = {y[3], y[4], y[5]};
+  const V3<R> Aaa = {y[6], y[7], y[8]}, Abb = {y[9], y[10], y[11]}, Aab = {y[12], y[13], y[14]};
+  R dy[15];
+#pragma unroll
+  for (int c = 0; c < 15; c++) dy[c] = c == lane ? one : R(0);
+  const V3<R> da1 = {dy[0], dy[1], dy[2]}, da2 = {dy[3], dy[4], dy[5]};
+  const V3<R> dAaa = {dy[6], dy[7], dy[8]}, dAbb = {dy[9], dy[10], dy[11]}, dAab = {dy[12], dy[13], dy[14]};
+  /* geometry */
+  const V3<R> dcr = cross(da1, a2) + cross(a1, da2);
+  const R dcn = dot(n, dcr);
+  const V3<R> dn = scl(icn, dcr - scl(dcn, n));
+  const R dicn = -(icn * icn) * dcn;
+  const V3<R> dt1 = cross(da2, n) + cross(a2, dn);
+  const R ds1 = -(s1 * s1) * (dot(da1, t1) + dot(a1, dt1));
+  const V3<R> gc1 = scl(s1, t1), dgc1 = scl(ds1, t1) + scl(s1, dt1);
+  const V3<R> dt2 = cross(dn, a1) + cross(n, da1);
+  const R ds2 = -(s2 * s2) * (dot(da2, t2) + dot(a2, dt2));
+  const V3<R> gc2 = scl(s2, t2), dgc2 = scl(ds2, t2) + scl(s2, dt2);
+  const V3<R> du31 = cross(dAaa, a2) + cross(Aaa, da2) + cross(da1, Aab) + cross(a1, dAab);
+  const V3<R> du32 = cross(dAab, a2) + cross(Aab, da2) + cross(da1, Abb) + cross(a1, dAbb);
+  V3<R> a31 = scl(icn, u31), a32 = scl(icn, u32);
+  V3<R> da31 = scl(icn, du31) + scl(dicn, u31), da32 = scl(icn, du32) + scl(dicn, u32);
+  if (p.tnormal) {   /* a3,alpha - (a3,alpha . n) n */
+    const R p31 = dot(a31, n), p32 = dot(a32, n);
+    const R dp31 = dot(da31, n) + dot(a31, dn), dp32 = dot(da32, n) + dot(a32, dn);
+    da31 = da31 - scl(dp31, n) - scl(p31, dn);
+    da32 = da32 - scl(dp32, n) - scl(p32, dn);
+    a31 = a31 - scl(p31, n);
+    a32 = a32 - scl(p32, n);
+  }
+  /* resultants: primal from the jobs' stresses, derivative by the chain rule */
+  R N0 = R(0), N1 = R(0), N2 = R(0), M0 = R(0), M1 = R(0), M2 = R(0);
+  R dN0 = R(0), dN1 = R(0), dN2 = R(0), dM0 = R(0), dM1 = R(0), dM2 = R(0);
+  for (int q = 0; q < nq; q++) {
+    const R th3 = p.hhalf * p.theta[q];
+    const V3<R> g1 = a1 + scl(th3, a31), g2 = a2 + scl(th3, a32);
+    const V3<R> dg1 = da1 + scl(th3, da31), dg2 = da2 + scl(th3, da32);
+    const R dgm[5] = {dot(dg1, g1) + dot(g1, dg1), dot(dg2, g2) + dot(g2, dg2), dot(dg1, g2) + dot(g1, dg2),
+                      dot(dg1, n) + dot(g1, dn), dot(dg2, n) + dot(g2, dn)};
+    R sv[3], dsv[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      R d = R(0);
+#pragma unroll
+      for (int c = 0; c < 5; c++)
+        if (c < ndirs) d += jac[q * 21 + 6 * i + c] * dgm[c];
+      sv[i] = jac[q * 21 + 18 + i];
+      dsv[i] = d;
+    }
+    const R wq = p.w[q], wt = p.w[q] * th3;
+    N0 = N0 + wq * sv[0]; N1 = N1 + wq * sv[1]; N2 = N2 + wq * sv[2];
+    M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
+    dN0 = dN0 + wq * dsv[0]; dN1 = dN1 + wq * dsv[1]; dN2 = dN2 + wq * dsv[2];
+    dM0 = dM0 + wt * dsv[0]; dM1 = dM1 + wt * dsv[1]; dM2 = dM2 + wt * dsv[2];
+  }
+  /* elem_out */
+  N0 = pref0 * N0; N1 = pref0 * N1; N2 = pref0 * N2; M0 = pref0 * M0; M1 = pref0 * M1; M2 = pref0 * M2;
+  dN0 = pref0 * dN0; dN1 = pref0 * dN1; dN2 = pref0 * dN2; dM0 = pref0 * dM0; dM1 = pref0 * dM1; dM2 = pref0 * dM2;
+  const R twoM2 = two * M2, dtwoM2 = two * dM2;
+  const V3<R> Q = scl(M0, Aaa) + scl(M1, Abb) + scl(twoM2, Aab);
+  const V3<R> dQ = scl(dM0, Aaa) + scl(M0, dAaa) + scl(dM1, Abb) + scl(M1, dAbb) + scl(dtwoM2, Aab) + scl(twoM2, dAab);
+  const R q1 = dot(gc1, Q), dq1 = dot(dgc1, Q) + dot(gc1, dQ);
+  const R q2 = dot(gc2, Q), dq2 = dot(dgc2, Q) + dot(gc2, dQ);
+  const V3<R> df1 = scl(dN0, a1) + scl(N0, da1) + scl(dN2, a2) + scl(N2, da2) - scl(dq1, n) - scl(q1, dn);
+  const V3<R> df2 = scl(dN1, a2) + scl(N1, da2) + scl(dN2, a1) + scl(N2, da1) - scl(dq2, n) - scl(q2, dn);
+  df[0] = df1.x; df[1] = df1.y; df[2] = df1.z;
+  df[3] = df2.x; df[4] = df2.y; df[5] = df2.z;
+  const V3<R> dm0 = scl(dM0, n) + scl(M0, dn), dm1 = scl(dM1, n) + scl(M1, dn), dm2 = scl(dtwoM2, n) + scl(twoM2, dn);
+  df[6] = -dm0.x; df[7] = -dm0.y; df[8] = -dm0.z;
+  df[9] = -dm1.x; df[10] = -dm1.y; df[11] = -dm1.z;
+  df[12] = -dm2.x; df[13] = -dm2.y; df[14] = -dm2.z;
 }
 
 } /* namespace biofem */

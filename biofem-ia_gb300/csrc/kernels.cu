@@ -209,7 +209,8 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
 }
 
 /* ---------------- residual element kernel ---------------- */
-__global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, double *__restrict__ gm_out)
+__global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, double *__restrict__ gm_out,
+                                                       double *__restrict__ gp_out)
 {
   __shared__ double tabs[kNumTables * 80];
   for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
@@ -225,6 +226,7 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
   int st = 0;
   const EPar<double> ep = epar<double>(p);
   elem_forces<double, double>(y, ep, m.eref + e, p.ne, f, st, gm_out ? gm_out + e : nullptr);
+  if (gp_out) elem_geom_store<double>(y, gp_out + e, (size_t)p.ne);   /* the tangent's primal geometry */
   set_status(m.status, st);
   /* Fb_a = sum_r N[r][a] f_r, stored slot-major: fb[(3a+d)*ne + e] */
   const size_t ne = p.ne;
@@ -275,17 +277,18 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   const double *tab = tabs + tabi * 80;
   double y[15];
   gather_y_group(m.pos, m.patch, ee, nen, tab, lane, y);
-  D1d fd[15];
+  double fd[15];
   int st = 0;
   const EPar<double> ep = epar<double>(p);
-  /* the thickness-point metrics come from k_elem_residual, launched before this kernel */
-  elem_forces_split<double>(y, ep, m.eref + ee, p.ne, lane, Jsh[slot], fd, st, m.gmq + ee);
+  /* the thickness-point metrics and the primal geometry come from
+     k_elem_residual, launched before this kernel */
+  elem_forces_split_tl<double>(y, ep, m.eref + ee, p.ne, m.gpr + ee, lane, Jsh[slot], fd, st, m.gmq + ee);
   if (live) set_status(m.status, st);
   const size_t ne = p.ne;
   /* column `lane` of D = df/dy */
   if (lane < 15) {
 #pragma unroll
-    for (int r = 0; r < 15; r++) Dsh[slot][r * 16 + lane] = fd[r].d;
+    for (int r = 0; r < 15; r++) Dsh[slot][r * 16 + lane] = fd[r];
   }
   /* the element forces come from k_elem_residual, launched before this kernel */
   __syncwarp();
@@ -657,7 +660,8 @@ int launch_positions(const DevMesh &m, const KParams &p, const double *x, void *
 
 int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream, bool store_metric)
 {
-  k_elem_residual<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p, store_metric ? m.gmq : nullptr);
+  k_elem_residual<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p, store_metric ? m.gmq : nullptr,
+                                                                          store_metric ? m.gpr : nullptr);
   return (int)cudaGetLastError();
 }
 
