@@ -86,6 +86,7 @@ struct DevMesh {
   double *dyn_diag;          /* nt: d Fdyn / d x on the diagonal of each free row */
   double *gmq;               /* FP64 handles: 6 nq x ne thickness-point metrics, k_elem_residual -> k_elem_tangent */
   double *gpr;               /* FP64 handles: kGeomPrimal x ne primal geometry, k_elem_residual -> k_elem_tangent */
+  double *gtape;             /* FP64 handles: nq x (6 + 23 C33 iterations) x ne primal stress values, likewise */
   unsigned long long *fmax;  /* max |Fext| as ordered bits */
 };
 

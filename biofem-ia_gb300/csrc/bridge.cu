@@ -565,7 +565,8 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   if (params->precision == BIOFEM_FP64) {
     double *dK = nullptr;
     if ((rc = dalloc(m, &dm.ke, 9 * keblocks)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb)) ||
-        (rc = dalloc(m, &dm.gmq, 6 * (size_t)kp.nq * ne)) || (rc = dalloc(m, &dm.gpr, (size_t)kGeomPrimal * ne))) {
+        (rc = dalloc(m, &dm.gmq, 6 * (size_t)kp.nq * ne)) || (rc = dalloc(m, &dm.gpr, (size_t)kGeomPrimal * ne)) ||
+        (rc = dalloc(m, &dm.gtape, (size_t)(6 + 23 * kp.iters) * kp.nq * ne))) {
       free_mesh(m);
       return rc;
     }

@@ -172,18 +172,32 @@ __host__ __device__ __forceinline__ T qform(const T &c00, const T &c11, const T 
   return x[0] * (c00 * y[0] + c01 * y[1]) + x[1] * (c01 * y[0] + c11 * y[1]) + (x[2] * y[2]) * c22;
 }
 
+/* Primal values of the C33 sub-iterations of one thickness point that the
+   FP64 tangent's derivative-only form reads (qp_stress_tl): the residual
+   kernel of the same call records them (SoA over elements).  Slots: the
+   initial cofactors and inverses, then per sub-iteration it (base
+   kTapeInit + kTapeIt * it) the values named in qp_stress. */
+constexpr int kTapeInit = 6;    /* cof00 cof11 cof01 cofx 1/det 1/(g00 g11 - g01^2) */
+constexpr int kTapeIt = 23;
+enum {
+  kTpC00, kTpC11, kTpC01, kTpC22, kTpPre, kTpQd, kTpHJ, kTpJe, kTpAlpha, kTpBeta, kTpB33,
+  kTpQvv, kTpQww, kTpQee, kTpQvw, kTpQve, kTpQwe, kTpICC, kTpDC, kTpLo, kTpB0, kTpB1, kTpB2
+};
+__host__ __device__ __forceinline__ int tape_per_qp(int iters) { return kTapeInit + kTapeIt * iters; }
+
 /* Stress of one thickness point after the C33 sub-iterations:
    returns S^11, S^22, S^12 in sv[0..2]; status bit 1 on a vanishing CC3333.
    Every sub-iteration ends with the C33 update (ModElemC33); the stress is
    taken before the last one, so final_update = false skips that update
    (CC3333 and its check included) when only the stress is wanted and another
    kernel of the same call performs the check.  c33_out receives C33 after
-   the last update. */
+   the last update; tape (stride ts) receives the primal values of
+   qp_stress_tl (the arithmetic is the same with or without it). */
 template <class T, class R>
 __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 12 22 */, const QpRef<R> &r,
                                                    R gam, R gamp, R c1, R mu, R K,
                                                    int iters, T sv[3], int &status, T *c33_out = nullptr,
-                                                   bool final_update = true)
+                                                   bool final_update = true, R *tape = nullptr, size_t ts = 0)
 {
   const R one = R(1), two = R(2), half = R(0.5), quarter = R(0.25);
   const T &g00 = gm[0], &g11 = gm[1], &g01 = gm[2], &g02 = gm[3], &g12 = gm[4], &g22 = gm[5];
@@ -191,32 +205,46 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
   T cof00 = g11 * g22 - g12 * g12;
   T cof11 = g00 * g22 - g02 * g02;
   T cof01 = g02 * g12 - g01 * g22;
-  T det = g00 * cof00 + g01 * cof01 + g02 * (g01 * g12 - g11 * g02);
+  const T cofx = g01 * g12 - g11 * g02;
+  T det = g00 * cof00 + g01 * cof01 + g02 * cofx;
   T idet = one / det;
   T c00 = cof00 * idet, c11 = cof11 * idet, c01 = cof01 * idet;
   T c22 = T{one};
   T C33 = T{one};
+  if (tape) {
+    tape[0] = val(cof00); tape[ts] = val(cof11); tape[2 * ts] = val(cof01); tape[3 * ts] = val(cofx);
+    tape[4 * ts] = val(idet);
+  }
   for (int it = 0; it < iters; it++) {
+    R *tp = tape ? tape + (size_t)(kTapeInit + kTapeIt * it) * ts : nullptr;
     const T u0 = c00 * r.t[0] + c01 * r.t[1];
     const T u1 = c01 * r.t[0] + c11 * r.t[1];
     const T u2 = c22 * r.t[2];
     const T tau = r.t[0] * u0 + r.t[1] * u1 + r.t[2] * u2;
-    const T detci = (c00 * c11 - c01 * c01) * c22;
-    const T Je = dsqrt(r.rho / detci);
+    const T pre = c00 * c11 - c01 * c01;
+    const T detci = pre * c22;
+    const T qrd = r.rho / detci;
+    const T Je = dsqrt(qrd);
     const T alpha = K * (Je * Je - Je) - mu;
     const T beta = (half * K) * Je * (two * Je - one);
     const T half_a = half * alpha;
     const R gg = gam * gamp;
     /* S^33 */
-    const T S33 = mu * (r.gc22 + c1 * r.s[2] * r.s[2])
-                + half_a * (two * c22 + (gamp - gam) * r.s[2] * u2 - gg * r.s[2] * r.s[2] * tau);
+    const T B33 = two * c22 + (gamp - gam) * r.s[2] * u2 - gg * r.s[2] * r.s[2] * tau;
+    const T S33 = mu * (r.gc22 + c1 * r.s[2] * r.s[2]) + half_a * B33;
+    if (tp) {
+      tp[kTpC00 * ts] = val(c00); tp[kTpC11 * ts] = val(c11); tp[kTpC01 * ts] = val(c01); tp[kTpC22 * ts] = val(c22);
+      tp[kTpPre * ts] = val(pre); tp[kTpQd * ts] = val(qrd) / val(detci); tp[kTpHJ * ts] = half / val(Je);
+      tp[kTpJe * ts] = val(Je); tp[kTpAlpha * ts] = val(alpha); tp[kTpBeta * ts] = val(beta); tp[kTpB33 * ts] = val(B33);
+    }
     if (it == iters - 1) {
-      sv[0] = mu * (r.gc00 + c1 * r.s[0] * r.s[0])
-            + half_a * (two * c00 + (gamp - gam) * r.s[0] * u0 - gg * r.s[0] * r.s[0] * tau);
-      sv[1] = mu * (r.gc11 + c1 * r.s[1] * r.s[1])
-            + half_a * (two * c11 + (gamp - gam) * r.s[1] * u1 - gg * r.s[1] * r.s[1] * tau);
-      sv[2] = mu * (r.gc01 + c1 * r.s[0] * r.s[1])
-            + half_a * (two * c01 + gamp * r.s[1] * u0 - gam * r.s[0] * u1 - gg * r.s[0] * r.s[1] * tau);
+      const T B0 = two * c00 + (gamp - gam) * r.s[0] * u0 - gg * r.s[0] * r.s[0] * tau;
+      const T B1 = two * c11 + (gamp - gam) * r.s[1] * u1 - gg * r.s[1] * r.s[1] * tau;
+      const T B2 = two * c01 + gamp * r.s[1] * u0 - gam * r.s[0] * u1 - gg * r.s[0] * r.s[1] * tau;
+      sv[0] = mu * (r.gc00 + c1 * r.s[0] * r.s[0]) + half_a * B0;
+      sv[1] = mu * (r.gc11 + c1 * r.s[1] * r.s[1]) + half_a * B1;
+      sv[2] = mu * (r.gc01 + c1 * r.s[0] * r.s[1]) + half_a * B2;
+      if (tp) { tp[kTpB0 * ts] = val(B0); tp[kTpB1 * ts] = val(B1); tp[kTpB2 * ts] = val(B2); }
     }
     if (!final_update && it == iters - 1) break;
     /* CC3333 */
@@ -232,6 +260,11 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
     /* ModElemC33 (active_strain.c:1654-1707) */
     if (!(dabs(val(CC)) > R(1e-14))) { status |= 1; return; }
     T dC = -S33 / CC;
+    if (tp) {
+      tp[kTpQvv * ts] = val(qvv); tp[kTpQww * ts] = val(qww); tp[kTpQee * ts] = val(qee);
+      tp[kTpQvw * ts] = val(qvw); tp[kTpQve * ts] = val(qve); tp[kTpQwe * ts] = val(qwe);
+      tp[kTpICC * ts] = one / val(CC); tp[kTpDC * ts] = val(dC); tp[kTpLo * ts] = one;
+    }
     T Ct = C33 + dC;
     if (val(g00) * (val(g11) * val(Ct)) - val(g01) * (val(g01) * val(Ct)) <= R(0)) {
       R lo = R(0), hi = one;
@@ -242,6 +275,7 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
       }
       dC = dC * lo;
       Ct = C33 + dC;
+      if (tp) tp[kTpLo * ts] = lo;
     }
     C33 = Ct;
     if (it + 1 < iters) {
@@ -250,11 +284,118 @@ __host__ __device__ __forceinline__ void qp_stress(const T gm[6] /* 00 11 01 02 
       if (it == 0) {
         const T id2 = one / (g00 * g11 - g01 * g01);
         c00 = g11 * id2; c11 = g00 * id2; c01 = -g01 * id2;
+        if (tape) tape[5 * ts] = val(id2);
       }
       c22 = one / C33;
     }
   }
   if (c33_out) *c33_out = C33;
+}
+
+/* Derivative of qp_stress along KD directions dgm of the metric, from the
+   primal values qp_stress recorded in tp (stride ts): only derivatives are
+   computed, operation by operation.  The C33 update after the last stress is
+   not differentiated (the tangent needs the stress only). */
+template <class R, int KD>
+__device__ __forceinline__ void qp_stress_tl(const R gm[6], const R dgm[6][KD], const QpRef<R> &r, R gam, R gamp,
+                                             R c1, R mu, R K, int iters, const R *tp0, size_t ts, R sv[3],
+                                             R dsv[3][KD])
+{
+  const R two = R(2), half = R(0.5), quarter = R(0.25), four = R(4);
+  const R g00 = gm[0], g11 = gm[1], g01 = gm[2], g02 = gm[3], g12 = gm[4], g22 = gm[5];
+  const R cof00 = tp0[0], cof01 = tp0[2 * ts], cofx = tp0[3 * ts], idet = tp0[4 * ts];
+  const R cof11 = tp0[ts];
+  R dc00[KD], dc11[KD], dc01[KD], dc22[KD], dC33[KD];
+#pragma unroll
+  for (int i = 0; i < KD; i++) {
+    const R d00 = dgm[0][i], d11 = dgm[1][i], d01 = dgm[2][i], d02 = dgm[3][i], d12 = dgm[4][i], d22 = dgm[5][i];
+    const R dcof00 = d11 * g22 + g11 * d22 - two * g12 * d12;
+    const R dcof11 = d00 * g22 + g00 * d22 - two * g02 * d02;
+    const R dcof01 = d02 * g12 + g02 * d12 - d01 * g22 - g01 * d22;
+    const R dcofx = d01 * g12 + g01 * d12 - d11 * g02 - g11 * d02;
+    const R ddet = d00 * cof00 + g00 * dcof00 + d01 * cof01 + g01 * dcof01 + d02 * cofx + g02 * dcofx;
+    const R didet = -(idet * idet) * ddet;
+    dc00[i] = dcof00 * idet + cof00 * didet;
+    dc11[i] = dcof11 * idet + cof11 * didet;
+    dc01[i] = dcof01 * idet + cof01 * didet;
+    dc22[i] = R(0);
+    dC33[i] = R(0);
+  }
+  const R gg = gam * gamp;
+  for (int it = 0; it < iters; it++) {
+    const R *tp = tp0 + (size_t)(kTapeInit + kTapeIt * it) * ts;
+    const R c00 = tp[kTpC00 * ts], c11 = tp[kTpC11 * ts], c01 = tp[kTpC01 * ts], c22 = tp[kTpC22 * ts];
+    const R pre = tp[kTpPre * ts], qd = tp[kTpQd * ts], hJ = tp[kTpHJ * ts], Je = tp[kTpJe * ts];
+    const R alpha = tp[kTpAlpha * ts], beta = tp[kTpBeta * ts], B33 = tp[kTpB33 * ts];
+    const R half_a = half * alpha;
+    const bool last = it == iters - 1;
+    R B0 = R(0), B1 = R(0), B2 = R(0);
+    if (last) {
+      B0 = tp[kTpB0 * ts]; B1 = tp[kTpB1 * ts]; B2 = tp[kTpB2 * ts];
+      sv[0] = mu * (r.gc00 + c1 * r.s[0] * r.s[0]) + half_a * B0;
+      sv[1] = mu * (r.gc11 + c1 * r.s[1] * r.s[1]) + half_a * B1;
+      sv[2] = mu * (r.gc01 + c1 * r.s[0] * r.s[1]) + half_a * B2;
+    }
+    R qvv = R(0), qww = R(0), qee = R(0), qvw = R(0), qve = R(0), qwe = R(0), iCC = R(0), dC = R(0), lo = R(1);
+    if (!last) {
+      qvv = tp[kTpQvv * ts]; qww = tp[kTpQww * ts]; qee = tp[kTpQee * ts];
+      qvw = tp[kTpQvw * ts]; qve = tp[kTpQve * ts]; qwe = tp[kTpQwe * ts];
+      iCC = tp[kTpICC * ts]; dC = tp[kTpDC * ts]; lo = tp[kTpLo * ts];
+    }
+#pragma unroll
+    for (int i = 0; i < KD; i++) {
+      const R du0 = dc00[i] * r.t[0] + dc01[i] * r.t[1];
+      const R du1 = dc01[i] * r.t[0] + dc11[i] * r.t[1];
+      const R du2 = dc22[i] * r.t[2];
+      const R dtau = r.t[0] * du0 + r.t[1] * du1 + r.t[2] * du2;
+      const R dpre = dc00[i] * c11 + c00 * dc11[i] - two * c01 * dc01[i];
+      const R ddetci = dpre * c22 + pre * dc22[i];
+      const R dJe = hJ * (-(qd * ddetci));
+      const R dalpha = K * (two * Je - R(1)) * dJe;
+      const R dbeta = (half * K) * (four * Je - R(1)) * dJe;
+      const R dhalf_a = half * dalpha;
+      const R dB33 = two * dc22[i] + (gamp - gam) * r.s[2] * du2 - gg * r.s[2] * r.s[2] * dtau;
+      const R dS33 = dhalf_a * B33 + half_a * dB33;
+      if (last) {
+        const R dB0 = two * dc00[i] + (gamp - gam) * r.s[0] * du0 - gg * r.s[0] * r.s[0] * dtau;
+        const R dB1 = two * dc11[i] + (gamp - gam) * r.s[1] * du1 - gg * r.s[1] * r.s[1] * dtau;
+        const R dB2 = two * dc01[i] + gamp * r.s[1] * du0 - gam * r.s[0] * du1 - gg * r.s[0] * r.s[1] * dtau;
+        dsv[0][i] = dhalf_a * B0 + half_a * dB0;
+        dsv[1][i] = dhalf_a * B1 + half_a * dB1;
+        dsv[2][i] = dhalf_a * B2 + half_a * dB2;
+        continue;
+      }
+      const R dqvv = qform(dc00[i], dc11[i], dc01[i], dc22[i], r.av, r.av);
+      const R dqww = qform(dc00[i], dc11[i], dc01[i], dc22[i], r.aw, r.aw);
+      const R dqee = qform(dc00[i], dc11[i], dc01[i], dc22[i], r.ae, r.ae);
+      const R dqvw = qform(dc00[i], dc11[i], dc01[i], dc22[i], r.av, r.aw);
+      const R dqve = qform(dc00[i], dc11[i], dc01[i], dc22[i], r.av, r.ae);
+      const R dqwe = qform(dc00[i], dc11[i], dc01[i], dc22[i], r.aw, r.ae);
+      const R dCC = quarter * (two * (dbeta - dalpha) * qvv * qvv + four * (beta - alpha) * qvv * dqvv
+                               + four * dbeta * qvv * qwe + four * beta * (dqvv * qwe + qvv * dqwe)
+                               - four * dalpha * qvw * qve - four * alpha * (dqvw * qve + qvw * dqve)
+                               + (two * dbeta - dalpha) * qwe * qwe + two * (two * beta - alpha) * qwe * dqwe
+                               - dalpha * qww * qee - alpha * (dqww * qee + qww * dqee));
+      const R ddC = lo * (-(dS33 + dC * dCC) * iCC);
+      dC33[i] = dC33[i] + ddC;
+    }
+    if (last) break;
+    /* the in-plane inverse from iteration 1 on, and c22 = 1/C33 */
+    const R *tpn = tp0 + (size_t)(kTapeInit + kTapeIt * (it + 1)) * ts;
+    const R c22n = tpn[kTpC22 * ts];
+    const R id2 = tp0[5 * ts];
+#pragma unroll
+    for (int i = 0; i < KD; i++) {
+      if (it == 0) {
+        const R dden = dgm[0][i] * g11 + g00 * dgm[1][i] - two * g01 * dgm[2][i];
+        const R did2 = -(id2 * id2) * dden;
+        dc00[i] = dgm[1][i] * id2 + g11 * did2;
+        dc11[i] = dgm[0][i] * id2 + g00 * did2;
+        dc01[i] = -(dgm[2][i] * id2 + g01 * did2);
+      }
+      dc22[i] = -(c22n * c22n) * dC33[i];
+    }
+  }
 }
 
 /* Mid-surface geometry of the element from y = (a1, a2, Aaa, Abb, Aab). */
@@ -359,7 +500,7 @@ __host__ __device__ __forceinline__ void elem_out(const ElemGeom<T> &g, T N0, T 
    ref points at the element's first SoA constant (type R); stride = ne. */
 template <class T, class R>
 __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R> &p, const R *ref, int stride,
-                                                     T f[15], int &status, R *gm_out = nullptr)
+                                                     T f[15], int &status, R *gm_out = nullptr, R *tape_out = nullptr)
 {
   const ElemGeom<T> g = elem_geom<T, R>(y, p);
   const int nq = p.nq;
@@ -377,7 +518,8 @@ __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R
     if (gm_out)   /* the metric of every thickness point, SoA over elements, for the tangent */
       for (int c = 0; c < 6; c++) gm_out[(size_t)(6 * q + c) * stride] = val(gm[c]);
     T sv[3];
-    qp_stress(gm, r, gam, gamp, c1, p.mu, p.K, p.iters, sv, status);
+    qp_stress(gm, r, gam, gamp, c1, p.mu, p.K, p.iters, sv, status, (T *)nullptr, true,
+              tape_out ? tape_out + (size_t)q * tape_per_qp(p.iters) * stride : nullptr, (size_t)stride);
     const R wq = p.w[q], wt = p.w[q] * th3;
     N0 = N0 + wq * sv[0]; N1 = N1 + wq * sv[1]; N2 = N2 + wq * sv[2];
     M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
@@ -526,6 +668,40 @@ __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &
   elem_out(g, N0, N1, N2, M0, M1, M2, pref0, f);
 }
 
+/* constitutive_jobs in derivative-only form: the primal metric (gmq) and the
+   primal C33 sub-iteration values (tape) come from the residual kernel. */
+template <class R, int KD>
+__device__ __forceinline__ void constitutive_jobs_tl(const R *gmq, const R *tape, const EPar<R> &p, const R *ref,
+                                                     int stride, int lane, R gam, R gamp, R c1, R *jac)
+{
+  const int ndirs = metric_dirs(p);
+  const int per_q = (ndirs + KD - 1) / KD;
+  const int tq = tape_per_qp(p.iters);
+  for (int job = lane; job < per_q * p.nq; job += 16) {
+    const int q = job / per_q, k0 = (job - per_q * q) * KD;
+    R gmv[6], dgm[6][KD];
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+      gmv[c] = gmq[(size_t)(6 * q + c) * stride];
+#pragma unroll
+      for (int i = 0; i < KD; i++) dgm[c][i] = (c == k0 + i && c < ndirs) ? R(1) : R(0);
+    }
+    R sv[3], dsv[3][KD];
+    qp_stress_tl<R, KD>(gmv, dgm, load_qpref(ref, stride, q), gam, gamp, c1, p.mu, p.K, p.iters,
+                        tape + (size_t)q * tq * stride, (size_t)stride, sv, dsv);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+#pragma unroll
+      for (int t = 0; t < KD; t++)
+        if (k0 + t < ndirs) jac[q * 21 + 6 * i + k0 + t] = dsv[i][t];
+    }
+    if (k0 == 0) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) jac[q * 21 + 18 + i] = sv[i];
+    }
+  }
+}
+
 /* The chain rule of elem_forces_split along y_lane in tangent-linear form: the
    primal geometry comes from elem_geom_store (gp, SoA stride), the primal
    resultants from the constitutive jobs (jac), so only derivatives are
@@ -538,8 +714,8 @@ __device__ __forceinline__ void elem_forces_split(const R y[15], const EPar<R> &
    df holds d f_r / d y_lane. */
 template <class R>
 __device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R> &p, const R *ref, int stride,
-                                                     const R *gp, int lane, R *jac, R df[15], int &status,
-                                                     const R *gmq)
+                                                     const R *gp, int lane, R *jac, R df[15], const R *gmq,
+                                                     const R *tape)
 {
   const int nq = p.nq;
   const R gam = ref[(size_t)(kRefPerQp * nq + 0) * stride];
@@ -547,9 +723,9 @@ __device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R
   const R c1 = ref[(size_t)(kRefPerQp * nq + 2) * stride];
   const R pref0 = ref[(size_t)(kRefPerQp * nq + 3) * stride];
   const int ndirs = metric_dirs(p);
-  if (ndirs * nq <= 16) constitutive_jobs<R, 1>(nullptr, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
-  else if (((ndirs + 1) / 2) * nq <= 16) constitutive_jobs<R, 2>(nullptr, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
-  else constitutive_jobs<R, 3>(nullptr, gmq, p, ref, stride, lane, gam, gamp, c1, jac, status);
+  if (ndirs * nq <= 16) constitutive_jobs_tl<R, 1>(gmq, tape, p, ref, stride, lane, gam, gamp, c1, jac);
+  else if (((ndirs + 1) / 2) * nq <= 16) constitutive_jobs_tl<R, 2>(gmq, tape, p, ref, stride, lane, gam, gamp, c1, jac);
+  else constitutive_jobs_tl<R, 3>(gmq, tape, p, ref, stride, lane, gam, gamp, c1, jac);
   __syncwarp();
   const R one = R(1), two = R(2);
   R g[kGeomPrimal];

@@ -210,7 +210,7 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
 
 /* ---------------- residual element kernel ---------------- */
 __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, double *__restrict__ gm_out,
-                                                       double *__restrict__ gp_out)
+                                                       double *__restrict__ gp_out, double *__restrict__ tape_out)
 {
   __shared__ double tabs[kNumTables * 80];
   for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
@@ -225,7 +225,8 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
   double f[15];
   int st = 0;
   const EPar<double> ep = epar<double>(p);
-  elem_forces<double, double>(y, ep, m.eref + e, p.ne, f, st, gm_out ? gm_out + e : nullptr);
+  elem_forces<double, double>(y, ep, m.eref + e, p.ne, f, st, gm_out ? gm_out + e : nullptr,
+                              tape_out ? tape_out + e : nullptr);
   if (gp_out) elem_geom_store<double>(y, gp_out + e, (size_t)p.ne);   /* the tangent's primal geometry */
   set_status(m.status, st);
   /* Fb_a = sum_r N[r][a] f_r, stored slot-major: fb[(3a+d)*ne + e] */
@@ -278,12 +279,11 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   double y[15];
   gather_y_group(m.pos, m.patch, ee, nen, tab, lane, y);
   double fd[15];
-  int st = 0;
   const EPar<double> ep = epar<double>(p);
-  /* the thickness-point metrics and the primal geometry come from
-     k_elem_residual, launched before this kernel */
-  elem_forces_split_tl<double>(y, ep, m.eref + ee, p.ne, m.gpr + ee, lane, Jsh[slot], fd, st, m.gmq + ee);
-  if (live) set_status(m.status, st);
+  /* the thickness-point metrics, the primal geometry and the primal C33
+     sub-iteration values come from k_elem_residual, launched before this
+     kernel (which also performs the CC3333 checks) */
+  elem_forces_split_tl<double>(y, ep, m.eref + ee, p.ne, m.gpr + ee, lane, Jsh[slot], fd, m.gmq + ee, m.gtape + ee);
   const size_t ne = p.ne;
   /* column `lane` of D = df/dy */
   if (lane < 15) {
@@ -661,7 +661,8 @@ int launch_positions(const DevMesh &m, const KParams &p, const double *x, void *
 int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream, bool store_metric)
 {
   k_elem_residual<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p, store_metric ? m.gmq : nullptr,
-                                                                          store_metric ? m.gpr : nullptr);
+                                                                          store_metric ? m.gpr : nullptr,
+                                                                          store_metric ? m.gtape : nullptr);
   return (int)cudaGetLastError();
 }
 
