@@ -37,10 +37,10 @@ for _p in (ROOT, ROOT / "biofem-ia_gb300"):
 
 METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_elem_tangent launch on
-# the 256x192 workload (ncu --set full; 76.4 MB read, 1,055 MB written)
-TANGENT_DRAM_BYTES_C2 = 76.383e6 + 1054.585e6
+# the 256x192 workload (ncu --set full; 226.5 MB read, 994.7 MB written)
+TANGENT_DRAM_BYTES_C2 = 226.529e6 + 994.744e6
 # sm__pipe_fp64_cycles_active (of peak sustained active) of the same capture
-FP64_PIPE_ACTIVE_C2 = 0.888
+FP64_PIPE_ACTIVE_C2 = 0.885
 UNIT = "elems/s"
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_ELEMS = 2048
@@ -586,8 +586,9 @@ def run_ours(args):
                      "peak_source": peak_src, "step_achieved_gbs": step_gbs,
                      "note": "achieved = canonical algorithmic bytes of the R+K step (the dominant kernel's "
                              "inputs and the assembled outputs) / k_elem_tangent's live launch time; traffic = "
-                             "dram read + write of one k_elem_tangent launch on C2 from an ncu capture (element-"
-                             "matrix scratch); the kernel is FP64-pipe bound, see compute_roofline"},
+                             "dram read + write of one k_elem_tangent launch on C2 from an ncu capture (writes: element-"
+                             "matrix scratch; reads: mesh, positions and the primal values k_elem_residual stores); "
+                             "the kernel is FP64-pipe bound, see compute_roofline"},
         "compute_roofline": {"kernel": "k_elem_tangent", "bound": "fp64", "kernel_ms": k_tan,
                              "canonical_flops_per_step": f_alg,
                              "achieved_tflops_canonical": f_alg / (k_tan * 1e-3) / 1e12,
