@@ -18,7 +18,8 @@ namespace biofem {
 constexpr int kMaxQp = 6;
 constexpr int kRefPerQp = 20;     /* FP64 reference constants per (element, qp) */
 constexpr int kRefPerElem = 4;    /* gamma, gamma', c1, pref0 */
-constexpr int kGeomPrimal = 18;   /* primal element geometry stored for the FP64 tangent (elem_geom_store) */
+constexpr int kGeomShape = 18;    /* primal element geometry stored for the FP64 tangent (elem_geom_store) */
+constexpr int kGeomPrimal = kGeomShape + 17;   /* + the primal resultants (elem_res_store) */
 constexpr int kNumTables = 11;    /* 0 = regular 12-node patch, v = 3..10 irregular */
 
 /* Topology in IBMNodes layout (see topology.cpp). */
@@ -85,7 +86,7 @@ struct DevMesh {
   double *xn, *xnm1, *xd, *xdd;   /* 3*nt dynamic state (previous positions, velocity, acceleration) */
   double *dyn_diag;          /* nt: d Fdyn / d x on the diagonal of each free row */
   double *gmq;               /* FP64 handles: 6 nq x ne thickness-point metrics, k_elem_residual -> k_elem_tangent */
-  double *gpr;               /* FP64 handles: kGeomPrimal x ne primal geometry, k_elem_residual -> k_elem_tangent */
+  double *gpr;               /* FP64 handles: kGeomPrimal x ne primal geometry and resultants, k_elem_residual -> k_elem_tangent */
   double *gtape;             /* FP64 handles: nq x (6 + 23 C33 iterations) x ne primal stress values, likewise */
   unsigned long long *fmax;  /* max |Fext| as ordered bits */
 };

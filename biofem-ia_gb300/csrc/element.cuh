@@ -131,6 +131,50 @@ template <class T> __host__ __device__ __forceinline__ V3<T> cross(const V3<T> &
   return {a.y * b.z - b.y * a.z, b.x * a.z - a.x * b.z, a.x * b.y - b.x * a.y};
 }
 
+/* One-hot directions of the FP64 tangent's chain rule.  Lane 3 r + c of an
+   element group differentiates along the Cartesian component c of the r-th
+   of (a1, a2, Aaa, Abb, Aab); a product with that unit vector is a selection
+   of primal values (integer pipe), not FP64 arithmetic. */
+__device__ __forceinline__ double ineg(double x)
+{
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)(1ull << 63));
+}
+__device__ __forceinline__ float ineg(float x) { return __int_as_float(__float_as_int(x) ^ (int)(1u << 31)); }
+
+template <class R> __device__ __forceinline__ R comp(const V3<R> &v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
+
+/* e_c x v */
+template <class R> __device__ __forceinline__ V3<R> ecross(int c, const V3<R> &v)
+{
+  return {c == 1 ? v.z : (c == 2 ? ineg(v.y) : R(0)), c == 0 ? ineg(v.z) : (c == 2 ? v.x : R(0)),
+          c == 0 ? v.y : (c == 1 ? ineg(v.x) : R(0))};
+}
+
+/* v, -v or 0 */
+template <class R> __device__ __forceinline__ V3<R> sel_sign(const V3<R> &v, bool on, bool neg)
+{
+  return {on ? (neg ? ineg(v.x) : v.x) : R(0), on ? (neg ? ineg(v.y) : v.y) : R(0),
+          on ? (neg ? ineg(v.z) : v.z) : R(0)};
+}
+
+/* v + s e_c: one add */
+template <class R> __device__ __forceinline__ V3<R> add_at(const V3<R> &v, int c, R s)
+{
+  const R t = comp(v, c) + s;
+  return {c == 0 ? t : v.x, c == 1 ? t : v.y, c == 2 ? t : v.z};
+}
+
+/* a x b + acc and a.b + acc as FMA chains */
+template <class R> __device__ __forceinline__ V3<R> cross_acc(const V3<R> &a, const V3<R> &b, const V3<R> &acc)
+{
+  return {fma(a.y, b.z, fma(-b.y, a.z, acc.x)), fma(b.x, a.z, fma(-a.x, b.z, acc.y)),
+          fma(a.x, b.y, fma(-b.x, a.y, acc.z))};
+}
+template <class R> __device__ __forceinline__ R dot_acc(const V3<R> &a, const V3<R> &b, R acc)
+{
+  return fma(a.z, b.z, fma(a.y, b.y, fma(a.x, b.x, acc)));
+}
+
 /* Reference constants of one (element, qp), see the header comment. */
 template <class R> struct QpRef {
   R gc00, gc11, gc01, gc22;   /* G^-1 entries used by S */
@@ -430,7 +474,8 @@ __host__ __device__ __forceinline__ ElemGeom<T> elem_geom(const T y[15], const E
 /* Primal geometry the FP64 tangent's chain rule reads, stored once per element
    by the residual kernel of the same call (SoA over elements): n, 1/|a1 x a2|,
    t1 = a2 x n, t2 = n x a1, 1/(a1.t1), 1/(a2.t2), u31 = Aaa x a2 + a1 x Aab,
-   u32 = Aab x a2 + a1 x Abb (elem_geom's intermediates); kGeomPrimal values. */
+   u32 = Aab x a2 + a1 x Abb (elem_geom's intermediates); kGeomShape values,
+   followed by elem_res_store's. */
 
 template <class R>
 __host__ __device__ __forceinline__ void elem_geom_store(const R y[15], R *gp, size_t stride)
@@ -448,7 +493,27 @@ __host__ __device__ __forceinline__ void elem_geom_store(const R y[15], R *gp, s
   const R v[kGeomPrimal] = {n.x, n.y, n.z, icn, t1.x, t1.y, t1.z, t2.x, t2.y, t2.z, s1, s2,
                             u31.x, u31.y, u31.z, u32.x, u32.y, u32.z};
 #pragma unroll
-  for (int k = 0; k < kGeomPrimal; k++) gp[k * stride] = v[k];
+  for (int k = 0; k < kGeomShape; k++) gp[k * stride] = v[k];
+}
+
+/* The rest of the tangent's primal values (slots kGeomShape.. of the same
+   block): the pref0-scaled resultants N0 N1 N2 M0 M1 M2, Q, gc1.Q, gc2.Q,
+   gc1, gc2 (elem_out's intermediates, the same expressions). */
+template <class T, class R>
+__host__ __device__ __forceinline__ void elem_res_store(const ElemGeom<T> &g, T N0, T N1, T N2, T M0, T M1, T M2,
+                                                        R pref0, R *gp, size_t stride)
+{
+  const R two = R(2);
+  N0 = pref0 * N0; N1 = pref0 * N1; N2 = pref0 * N2;
+  M0 = pref0 * M0; M1 = pref0 * M1; M2 = pref0 * M2;
+  const T twoM2 = two * M2;
+  const V3<T> Q = scl(M0, g.Aaa) + scl(M1, g.Abb) + scl(twoM2, g.Aab);
+  const R v[kGeomPrimal - kGeomShape] = {
+      val(N0), val(N1), val(N2), val(M0), val(M1), val(M2), val(Q.x), val(Q.y), val(Q.z),
+      val(dot(g.gc1, Q)), val(dot(g.gc2, Q)),
+      val(g.gc1.x), val(g.gc1.y), val(g.gc1.z), val(g.gc2.x), val(g.gc2.y), val(g.gc2.z)};
+#pragma unroll
+  for (int k = 0; k < kGeomPrimal - kGeomShape; k++) gp[(kGeomShape + k) * stride] = v[k];
 }
 
 /* Metric (00 11 01 02 12 22) of the thickness point theta3 (ElemUpdateG). */
@@ -500,7 +565,8 @@ __host__ __device__ __forceinline__ void elem_out(const ElemGeom<T> &g, T N0, T 
    ref points at the element's first SoA constant (type R); stride = ne. */
 template <class T, class R>
 __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R> &p, const R *ref, int stride,
-                                                     T f[15], int &status, R *gm_out = nullptr, R *tape_out = nullptr)
+                                                     T f[15], int &status, R *gm_out = nullptr, R *tape_out = nullptr,
+                                                     R *gp_out = nullptr)
 {
   const ElemGeom<T> g = elem_geom<T, R>(y, p);
   const int nq = p.nq;
@@ -524,6 +590,7 @@ __host__ __device__ __forceinline__ void elem_forces(const T y[15], const EPar<R
     N0 = N0 + wq * sv[0]; N1 = N1 + wq * sv[1]; N2 = N2 + wq * sv[2];
     M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
   }
+  if (gp_out) elem_res_store(g, N0, N1, N2, M0, M1, M2, pref0, gp_out, (size_t)stride);
   elem_out(g, N0, N1, N2, M0, M1, M2, pref0, f);
 }
 
@@ -689,11 +756,12 @@ __device__ __forceinline__ void constitutive_jobs_tl(const R *gmq, const R *tape
     R sv[3], dsv[3][KD];
     qp_stress_tl<R, KD>(gmv, dgm, load_qpref(ref, stride, q), gam, gamp, c1, p.mu, p.K, p.iters,
                         tape + (size_t)q * tq * stride, (size_t)stride, sv, dsv);
+    /* columns g00 and g11 doubled: the chain rule forms d g00 / 2 = dg1.g1 and d g11 / 2 = dg2.g2 */
 #pragma unroll
     for (int i = 0; i < 3; i++) {
 #pragma unroll
       for (int t = 0; t < KD; t++)
-        if (k0 + t < ndirs) jac[q * 21 + 6 * i + k0 + t] = dsv[i][t];
+        if (k0 + t < ndirs) jac[q * 21 + 6 * i + k0 + t] = k0 + t < 2 ? R(2) * dsv[i][t] : dsv[i][t];
     }
     if (k0 == 0) {
 #pragma unroll
@@ -703,14 +771,16 @@ __device__ __forceinline__ void constitutive_jobs_tl(const R *gmq, const R *tape
 }
 
 /* The chain rule of elem_forces_split along y_lane in tangent-linear form: the
-   primal geometry comes from elem_geom_store (gp, SoA stride), the primal
-   resultants from the constitutive jobs (jac), so only derivatives are
-   computed here (the dual form recomputes every primal value in every lane).
-   The derivatives follow elem_geom, qp_metric and elem_out operation by
-   operation:
-     dcr = da1 x a2 + a1 x da2,  d|cr| = n.dcr,  dn = (dcr - n d|cr|)/|cr|,
-     d(1/|cr|) = -d|cr|/|cr|^2,  dt1 = da2 x n + a2 x dn,
-     d(1/(a1.t1)) = -(da1.t1 + a1.dt1)/(a1.t1)^2,  gc1 = t1/(a1.t1), ...
+   primal geometry and resultants come from the residual kernel (gp, SoA
+   stride: elem_geom_store, elem_res_store), the stress derivatives from the
+   constitutive jobs (jac), so only derivatives are computed here.  Lane
+   3 r + c carries the unit direction of component c of the r-th of
+   (a1, a2, Aaa, Abb, Aab) (lane 15: none), and every product with it is a
+   selection (one-hot helpers above).  The derivatives follow elem_geom,
+   qp_metric and elem_out operation by operation:
+     dcr = da1 x a2 + a1 x da2,  d|cr| = n.dcr (= t1_c or t2_c),
+     dn = (dcr - n d|cr|)/|cr|,  d(1/|cr|) = -d|cr|/|cr|^2,
+     dt1 = da2 x n + a2 x dn,  d(1/(a1.t1)) = -(da1.t1 + a1.dt1)/(a1.t1)^2, ...
    df holds d f_r / d y_lane. */
 template <class R>
 __device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R> &p, const R *ref, int stride,
@@ -727,33 +797,37 @@ __device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R
   else if (((ndirs + 1) / 2) * nq <= 16) constitutive_jobs_tl<R, 2>(gmq, tape, p, ref, stride, lane, gam, gamp, c1, jac);
   else constitutive_jobs_tl<R, 3>(gmq, tape, p, ref, stride, lane, gam, gamp, c1, jac);
   __syncwarp();
-  const R one = R(1), two = R(2);
+  const R zero = R(0), one = R(1), two = R(2);
   R g[kGeomPrimal];
 #pragma unroll
   for (int k = 0; k < kGeomPrimal; k++) g[k] = gp[(size_t)k * stride];
   const V3<R> n = {g[0], g[1], g[2]}, t1 = {g[4], g[5], g[6]}, t2 = {g[7], g[8], g[9]};
   const R icn = g[3], s1 = g[10], s2 = g[11];
   const V3<R> u31 = {g[12], g[13], g[14]}, u32 = {g[15], g[16], g[17]};
+  const R N0 = g[18], N1 = g[19], N2 = g[20], M0 = g[21], M1 = g[22], M2 = g[23];   /* pref0-scaled */
+  const V3<R> Q = {g[24], g[25], g[26]};
+  const R q1 = g[27], q2 = g[28];
+  const V3<R> gc1 = {g[29], g[30], g[31]}, gc2 = {g[32], g[33], g[34]};
   const V3<R> a1 = {y[0], y[1], y[2]}, a2 = {y[3], y[4], y[5]};
   const V3<R> Aaa = {y[6], y[7], y[8]}, Abb = {y[9], y[10], y[11]}, Aab = {y[12], y[13], y[14]};
-  R dy[15];
-#pragma unroll
-  for (int c = 0; c < 15; c++) dy[c] = c == lane ? one : R(0);
-  const V3<R> da1 = {dy[0], dy[1], dy[2]}, da2 = {dy[3], dy[4], dy[5]};
-  const V3<R> dAaa = {dy[6], dy[7], dy[8]}, dAbb = {dy[9], dy[10], dy[11]}, dAab = {dy[12], dy[13], dy[14]};
+  const int r = lane / 3, c = lane - 3 * r;
   /* geometry */
-  const V3<R> dcr = cross(da1, a2) + cross(a1, da2);
-  const R dcn = dot(n, dcr);
+  const V3<R> dcr = sel_sign(ecross(c, r == 0 ? a2 : a1), r < 2, r == 1);
+  const R dcn = r == 0 ? comp(t1, c) : (r == 1 ? comp(t2, c) : zero);
   const V3<R> dn = scl(icn, dcr - scl(dcn, n));
   const R dicn = -(icn * icn) * dcn;
-  const V3<R> dt1 = cross(da2, n) + cross(a2, dn);
-  const R ds1 = -(s1 * s1) * (dot(da1, t1) + dot(a1, dt1));
-  const V3<R> gc1 = scl(s1, t1), dgc1 = scl(ds1, t1) + scl(s1, dt1);
-  const V3<R> dt2 = cross(dn, a1) + cross(n, da1);
-  const R ds2 = -(s2 * s2) * (dot(da2, t2) + dot(a2, dt2));
-  const V3<R> gc2 = scl(s2, t2), dgc2 = scl(ds2, t2) + scl(s2, dt2);
-  const V3<R> du31 = cross(dAaa, a2) + cross(Aaa, da2) + cross(da1, Aab) + cross(a1, dAab);
-  const V3<R> du32 = cross(dAab, a2) + cross(Aab, da2) + cross(da1, Abb) + cross(a1, dAbb);
+  const V3<R> dt1 = cross_acc(a2, dn, sel_sign(ecross(c, n), r == 1, false));
+  const R ds1 = -(s1 * s1) * dot_acc(a1, dt1, r == 0 ? comp(t1, c) : zero);
+  const V3<R> dgc1 = scl(ds1, t1) + scl(s1, dt1);
+  const V3<R> dt2 = cross_acc(dn, a1, sel_sign(ecross(c, n), r == 0, true));
+  const R ds2 = -(s2 * s2) * dot_acc(a2, dt2, r == 1 ? comp(t2, c) : zero);
+  const V3<R> dgc2 = scl(ds2, t2) + scl(s2, dt2);
+  /* du31 = dAaa x a2 + Aaa x da2 + da1 x Aab + a1 x dAab and
+     du32 = dAab x a2 + Aab x da2 + da1 x Abb + a1 x dAbb: one term each */
+  const V3<R> v31 = r == 0 ? Aab : (r == 1 ? Aaa : (r == 2 ? a2 : a1));
+  const V3<R> du31 = sel_sign(ecross(c, v31), r < 3 || r == 4, r == 1 || r == 4);
+  const V3<R> v32 = r == 0 ? Abb : (r == 1 ? Aab : (r == 3 ? a1 : a2));
+  const V3<R> du32 = sel_sign(ecross(c, v32), r < 2 || r == 3 || r == 4, r == 1 || r == 3);
   V3<R> a31 = scl(icn, u31), a32 = scl(icn, u32);
   V3<R> da31 = scl(icn, du31) + scl(dicn, u31), da32 = scl(icn, du32) + scl(dicn, u32);
   if (p.tnormal) {   /* a3,alpha - (a3,alpha . n) n */
@@ -764,41 +838,43 @@ __device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R
     a31 = a31 - scl(p31, n);
     a32 = a32 - scl(p32, n);
   }
-  /* resultants: primal from the jobs' stresses, derivative by the chain rule */
-  R N0 = R(0), N1 = R(0), N2 = R(0), M0 = R(0), M1 = R(0), M2 = R(0);
-  R dN0 = R(0), dN1 = R(0), dN2 = R(0), dM0 = R(0), dM1 = R(0), dM2 = R(0);
+  const V3<R> da1 = {r == 0 && c == 0 ? one : zero, r == 0 && c == 1 ? one : zero, r == 0 && c == 2 ? one : zero};
+  const V3<R> da2 = {r == 1 && c == 0 ? one : zero, r == 1 && c == 1 ? one : zero, r == 1 && c == 2 ? one : zero};
+  /* resultant derivatives by the chain rule through each thickness point's metric */
+  R dN0 = zero, dN1 = zero, dN2 = zero, dM0 = zero, dM1 = zero, dM2 = zero;
   for (int q = 0; q < nq; q++) {
     const R th3 = p.hhalf * p.theta[q];
     const V3<R> g1 = a1 + scl(th3, a31), g2 = a2 + scl(th3, a32);
     const V3<R> dg1 = da1 + scl(th3, da31), dg2 = da2 + scl(th3, da32);
-    const R dgm[5] = {dot(dg1, g1) + dot(g1, dg1), dot(dg2, g2) + dot(g2, dg2), dot(dg1, g2) + dot(g1, dg2),
-                      dot(dg1, n) + dot(g1, dn), dot(dg2, n) + dot(g2, dn)};
-    R sv[3], dsv[3];
+    /* halves of d g00 and d g11: their stress columns are stored doubled */
+    const R dgm[5] = {dot(dg1, g1), dot(dg2, g2), dot_acc(g1, dg2, dot(dg1, g2)), dot_acc(g1, dn, dot(dg1, n)),
+                      dot_acc(g2, dn, dot(dg2, n))};
+    R dsv[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      R d = R(0);
+      R d = zero;
 #pragma unroll
-      for (int c = 0; c < 5; c++)
-        if (c < ndirs) d += jac[q * 21 + 6 * i + c] * dgm[c];
-      sv[i] = jac[q * 21 + 18 + i];
+      for (int k = 0; k < 5; k++)
+        if (k < ndirs) d += jac[q * 21 + 6 * i + k] * dgm[k];
       dsv[i] = d;
     }
     const R wq = p.w[q], wt = p.w[q] * th3;
-    N0 = N0 + wq * sv[0]; N1 = N1 + wq * sv[1]; N2 = N2 + wq * sv[2];
-    M0 = M0 + wt * sv[0]; M1 = M1 + wt * sv[1]; M2 = M2 + wt * sv[2];
     dN0 = dN0 + wq * dsv[0]; dN1 = dN1 + wq * dsv[1]; dN2 = dN2 + wq * dsv[2];
     dM0 = dM0 + wt * dsv[0]; dM1 = dM1 + wt * dsv[1]; dM2 = dM2 + wt * dsv[2];
   }
   /* elem_out */
-  N0 = pref0 * N0; N1 = pref0 * N1; N2 = pref0 * N2; M0 = pref0 * M0; M1 = pref0 * M1; M2 = pref0 * M2;
   dN0 = pref0 * dN0; dN1 = pref0 * dN1; dN2 = pref0 * dN2; dM0 = pref0 * dM0; dM1 = pref0 * dM1; dM2 = pref0 * dM2;
   const R twoM2 = two * M2, dtwoM2 = two * dM2;
-  const V3<R> Q = scl(M0, Aaa) + scl(M1, Abb) + scl(twoM2, Aab);
-  const V3<R> dQ = scl(dM0, Aaa) + scl(M0, dAaa) + scl(dM1, Abb) + scl(M1, dAbb) + scl(dtwoM2, Aab) + scl(twoM2, dAab);
-  const R q1 = dot(gc1, Q), dq1 = dot(dgc1, Q) + dot(gc1, dQ);
-  const R q2 = dot(gc2, Q), dq2 = dot(dgc2, Q) + dot(gc2, dQ);
-  const V3<R> df1 = scl(dN0, a1) + scl(N0, da1) + scl(dN2, a2) + scl(N2, da2) - scl(dq1, n) - scl(q1, dn);
-  const V3<R> df2 = scl(dN1, a2) + scl(N1, da2) + scl(dN2, a1) + scl(N2, da1) - scl(dq2, n) - scl(q2, dn);
+  /* dQ = dM0 Aaa + M0 dAaa + dM1 Abb + M1 dAbb + d(2 M2) Aab + 2 M2 dAab */
+  const V3<R> dQ = add_at(scl(dM0, Aaa) + scl(dM1, Abb) + scl(dtwoM2, Aab), c,
+                          r == 2 ? M0 : (r == 3 ? M1 : (r == 4 ? twoM2 : zero)));
+  const R dq1 = dot_acc(gc1, dQ, dot(dgc1, Q)), dq2 = dot_acc(gc2, dQ, dot(dgc2, Q));
+  /* df1 = dN0 a1 + N0 da1 + dN2 a2 + N2 da2 - dq1 n - q1 dn,
+     df2 = dN1 a2 + N1 da2 + dN2 a1 + N2 da1 - dq2 n - q2 dn */
+  const V3<R> df1 = add_at(scl(dN0, a1) + scl(dN2, a2) - scl(dq1, n) - scl(q1, dn), c,
+                           r == 0 ? N0 : (r == 1 ? N2 : zero));
+  const V3<R> df2 = add_at(scl(dN1, a2) + scl(dN2, a1) - scl(dq2, n) - scl(q2, dn), c,
+                           r == 1 ? N1 : (r == 0 ? N2 : zero));
   df[0] = df1.x; df[1] = df1.y; df[2] = df1.z;
   df[3] = df2.x; df[4] = df2.y; df[5] = df2.z;
   const V3<R> dm0 = scl(dM0, n) + scl(M0, dn), dm1 = scl(dM1, n) + scl(M1, dn), dm2 = scl(dtwoM2, n) + scl(twoM2, dn);

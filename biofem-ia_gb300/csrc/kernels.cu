@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
   int st = 0;
   const EPar<double> ep = epar<double>(p);
   elem_forces<double, double>(y, ep, m.eref + e, p.ne, f, st, gm_out ? gm_out + e : nullptr,
-                              tape_out ? tape_out + e : nullptr);
+                              tape_out ? tape_out + e : nullptr, gp_out ? gp_out + e : nullptr);
   if (gp_out) elem_geom_store<double>(y, gp_out + e, (size_t)p.ne);   /* the tangent's primal geometry */
   set_status(m.status, st);
   /* Fb_a = sum_r N[r][a] f_r, stored slot-major: fb[(3a+d)*ne + e] */
