@@ -126,10 +126,11 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0):
+def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0, residual_only=False):
     """The reference's element algorithm on the host: R and element tangents
-    for a bounded element sample; returns elems/s.  The subdivision tables come
-    from the library's host builder (bitwise equal to the reference's)."""
+    (or, with residual_only, R alone) for a bounded element sample; returns
+    elems/s.  The subdivision tables come from the library's host builder
+    (bitwise equal to the reference's)."""
     from oracle.pyoracle import Oracle
     from biofem import configs
     o = Oracle().setup_given_topology(mesh, w, topo, configs.MU, configs.BULK, configs.H0)
@@ -138,13 +139,14 @@ def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0):
     n_elems = min(n_elems, mesh.n_elmt)
     # spread the sample over the mesh: a strided window of consecutive elements
     e0 = max(0, mesh.n_elmt // 2 - n_elems // 2)
+    fn = o.lib.oracle_r_sample if residual_only else o.lib.oracle_rk_sample
     times = []
     for s in range(warmup + steps):
         t0 = time.perf_counter()
-        rc = o.lib.oracle_rk_sample(x.ctypes.data_as(ctypes.c_void_p), e0, e0 + n_elems, threads, ctypes.byref(chk))
+        rc = fn(x.ctypes.data_as(ctypes.c_void_p), e0, e0 + n_elems, threads, ctypes.byref(chk))
         dt = time.perf_counter() - t0
         if rc:
-            raise RuntimeError(f"oracle_rk_sample failed: {rc}")
+            raise RuntimeError(f"oracle element sample failed: {rc}")
         if s >= warmup:
             times.append(dt)
     return n_elems * len(times) / sum(times), sum(times), n_elems
@@ -394,6 +396,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     sample = 1024
     val, tot, n = cpu_rk(w, mesh, topo, x, sample, threads, steps=args.steps, warmup=args.warmup)
+    rval, rtot, rn = cpu_rk(w, mesh, topo, x, 8 * sample, threads, residual_only=True)
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
@@ -404,7 +407,9 @@ def run_reference(args):
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n} consecutive elements of {w.name} per step: reference element algorithm "
                                    f"(oracle/oracle.cpp, bitwise equal to the reference build) + exact element "
-                                   f"tangent by Dual<48> forward mode, OpenMP over elements"},
+                                   f"tangent by Dual<48> forward mode, OpenMP over elements",
+                         "residual_only": {"value": rval, "unit": UNIT, "cores": threads,
+                                           "sample": f"{rn} elements, element forces only ({rtot:.2f} s)"}},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -572,6 +577,12 @@ def run_ours(args):
                "sample": f"{cn} consecutive elements of {w.name}: reference element algorithm (oracle/oracle.cpp, "
                          f"bitwise equal to the reference build) + exact element tangent by Dual<48> forward mode, "
                          f"{ctot:.1f} s"}
+        # the residual alone, what the reference evaluates (its Newton is Jacobian-free): all cores and one
+        rval, rtot, rn = cpu_rk(w, mesh, topo, x_host, 4 * CPU_SAMPLE_ELEMS, threads, residual_only=True)
+        r1val, r1tot, r1n = cpu_rk(w, mesh, topo, x_host, 4 * CPU_SAMPLE_ELEMS, 1, residual_only=True)
+        cpu["residual_only"] = {"value": rval, "unit": UNIT, "cores": threads, "one_core_value": r1val,
+                                "sample": f"{rn} elements on {threads} threads ({rtot:.2f} s), {r1n} on one "
+                                          f"({r1tot:.2f} s): element forces only"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",

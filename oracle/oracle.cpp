@@ -1196,6 +1196,44 @@ int oracle_rk_sample(const double *x, int e0, int e1, int threads, double *chk)
   return 0;
 }
 
+/* CPU baseline of the residual alone (the only thing the reference evaluates:
+   its Newton is Jacobian-free, main.c:464-466): the element forces of
+   elements [e0, e1) by the reference's per-element algorithm
+   (FInternalAct's loop body, active_strain.c:2226-2267) on `threads` OpenMP
+   threads, checksum in *chk. */
+int oracle_r_sample(const double *x, int e0, int e1, int threads, double *chk)
+{
+  if (!g_body || !g_body->ready) return 58;
+  const Body &B = *g_body;
+  const Mesh &m = B.m;
+  if (e0 < 0 || e1 > m.n_elmt || e0 > e1) return 63;
+  const int ntot = m.n_v + m.n_ghosts;
+  std::vector<double> xb(ntot), yb(ntot), zb(ntot);
+  for (int v = 0; v < m.n_v; v++) { xb[v] = x[3 * v]; yb[v] = x[3 * v + 1]; zb[v] = x[3 * v + 2]; }
+  for (int v = m.n_v; v < ntot; v++) { xb[v] = m.x0[v]; yb[v] = m.y0[v]; zb[v] = m.z0[v]; }
+  global_ghost(m, xb.data(), yb.data(), zb.data());
+  const int ne = e1 - e0;
+  std::vector<double> part((size_t)ne, 0.0);
+  std::vector<int> rcs(ne, 0);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads > 0 ? threads : 1)
+#endif
+  for (int k = 0; k < ne; k++) {
+    const int ec = e0 + k;
+    const int nen = (m.ire[ec] == 0) ? 12 : m.val[ec] + 6;
+    double Fb[48];
+    rcs[k] = elem_forces<double>(m, B.P, ec, B.ref[ec], xb.data(), yb.data(), zb.data(), Fb);
+    double s = 0.0;
+    for (int i = 0; i < 3 * nen; i++) s += Fb[i];
+    part[k] = s;
+  }
+  for (int k = 0; k < ne; k++) if (rcs[k]) return rcs[k];
+  double c = 0.0;
+  for (int k = 0; k < ne; k++) c += part[k];
+  *chk = c;
+  return 0;
+}
+
 void oracle_teardown(void) { delete g_body; g_body = nullptr; }
 
 } /* extern "C" */
