@@ -8,12 +8,15 @@
  *   k_elem_residual  one thread per element: geometry, closed-form stress,
  *                    element forces Fb (ElemUpdFint) and the follower-pressure
  *                    corner force (SurfaceNormalPressure, external.c:589-624)
- *                    (and, for the tangent, the thickness-point metrics)
+ *                    (and, for the FP64 tangent, the primal values its
+ *                    derivative-only form reads: thickness-point metrics,
+ *                    geometry, resultants, C33 sub-iteration values)
  *   k_elem_tangent   16 lanes per element: the stress is differentiated along
  *                    the metric components of each thickness point (one job
  *                    per lane), then lane j carries d/dy_j through the
  *                    geometry and the chain rule, giving column j of df/dy;
- *                    the half-warp then forms K_e = N^T (df/dy) N in shared memory
+ *                    the half-warp then forms K_e = N^T (df/dy) N
+ *                    (contract_element: T = (df/dy) N held in registers)
  *   k_node_gather    one thread per node: Fint / Fext (and FDynamic's Fdyn)
  *                    summed over the node's element contributions in element
  *                    order (the order FInternalAct's VecSetValues loop adds
@@ -259,12 +262,85 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
 
 /* ---------------- tangent element kernel ---------------- */
 constexpr int kTanElemsPerCta = 8;   /* 16 lanes per element, 128 threads */
+constexpr int kKRounds = (9 * 16 + 15) / 16;   /* offsets per lane of a 9 nen block row, nen <= 16 */
+
+/* Entry (i, j) of the follower-pressure block d c / d x_k = [s v]x (the cross
+   product matrix of s v), for runtime i, j. */
+template <class R>
+__device__ __forceinline__ R skew_entry(int i, int j, const R v[3], R s)
+{
+  if (i == j) return R(0);
+  const int m3 = 3 - i - j;
+  const R vm = m3 == 0 ? v[0] : (m3 == 1 ? v[1] : v[2]);
+  const R t = s * vm;
+  return (j - i + 3) % 3 == 1 ? -t : t;
+}
+
+/* K_e = N^T D N of one element in its 16 lanes, T = D N kept in registers.
+   Lane l owns the offsets o = l + 16k (k < kKRounds, o < 9 nen) of a block
+   row, o = 9b + 3i + j, and forms T[(r,i)][(b,j)] = sum_s D[3r+i][3s+j] N[s][b]
+   (r < 5) for them once; then for every row node a it writes
+   K[(a,i)][(b,j)] = sum_r N[r][a] T[(r,i)][(b,j)], plus the follower-pressure
+   block when a and b are corner slots, to ke[9 nen a + o] (block layout
+   (a nen + b) 9 + 3i + j): consecutive lanes write consecutive values.  The
+   summation order of every entry is that of the two-pass form (T, then K).
+   D: this element's D = df/dy, row stride drow.  vv, sc: the pressure block
+   of corner k is the cross-product matrix of sc vv[k]. */
+template <class R>
+__device__ __forceinline__ void contract_element(const R *D, int drow, const R *tab, int nen, int lane,
+                                                 const int cslot[3], bool pressure, const R vv[3][3], R sc, R *ke)
+{
+  const int lim = 9 * nen;
+  R T[kKRounds][5], P[kKRounds];
+#pragma unroll
+  for (int k = 0; k < kKRounds; k++) {
+    if (16 * k < lim) {   /* the same for the 16 lanes of the element */
+      const int o = lane + 16 * k;
+      const int oc = o < lim ? o : 0;
+      const int b = oc / 9, w = oc - 9 * b, i = w / 3, j = w - 3 * i;
+#pragma unroll
+      for (int r = 0; r < 5; r++) {
+        R acc = R(0);
+#pragma unroll
+        for (int sr = 0; sr < 5; sr++) acc = fma(D[(3 * r + i) * drow + 3 * sr + j], tab[sr * 16 + b], acc);
+        T[k][r] = acc;
+      }
+      R pk = R(0);
+      if (pressure) {
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          if (b == cslot[c]) pk = pk + skew_entry(i, j, vv[c], sc);
+      }
+      P[k] = pk;
+    }
+  }
+  for (int a = 0; a < nen; a++) {
+    R Na[5];
+#pragma unroll
+    for (int r = 0; r < 5; r++) Na[r] = tab[r * 16 + a];
+    const bool corner = pressure && (a == cslot[0] || a == cslot[1] || a == cslot[2]);
+    R *row = ke + (size_t)a * lim;
+#pragma unroll
+    for (int k = 0; k < kKRounds; k++) {
+      if (16 * k < lim) {
+        const int o = lane + 16 * k;
+        R acc = R(0);
+#pragma unroll
+        for (int r = 0; r < 5; r++) acc = fma(Na[r], T[k][r], acc);
+        if (corner) acc += P[k];
+        if (o < lim) row[o] = acc;
+      }
+    }
+  }
+}
 
 __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
 {
   __shared__ double tabs[kNumTables * 80];
-  __shared__ double Dsh[kTanElemsPerCta][15 * 16];   /* D[r][s] at r*16+s */
-  __shared__ double Tsh[kTanElemsPerCta][15 * 48];   /* T[r3][c] : (D N) */
+  /* D = df/dy per element, row stride 19 (3 mod 16 eight-byte banks: the 9
+     (i, j) rows and columns the lanes read fall in distinct banks) */
+  constexpr int kDRow = 19, kDSlot = 15 * kDRow;
+  __shared__ double Dsh[kTanElemsPerCta * kDSlot];
   __shared__ double Jsh[kTanElemsPerCta][kMaxQp * 21]; /* constitutive derivatives per thickness point */
   for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
   __syncthreads();
@@ -284,24 +360,13 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
      sub-iteration values come from k_elem_residual, launched before this
      kernel (which also performs the CC3333 checks) */
   elem_forces_split_tl<double>(y, ep, m.eref + ee, p.ne, m.gpr + ee, lane, Jsh[slot], fd, m.gmq + ee, m.gtape + ee);
-  const size_t ne = p.ne;
   /* column `lane` of D = df/dy */
+  double *D = Dsh + slot * kDSlot;
   if (lane < 15) {
 #pragma unroll
-    for (int r = 0; r < 15; r++) Dsh[slot][r * 16 + lane] = fd[r];
+    for (int r = 0; r < 15; r++) D[r * kDRow + lane] = fd[r];
   }
   /* the element forces come from k_elem_residual, launched before this kernel */
-  __syncwarp();
-  /* T[(r,i)][(b,j)] = sum_s D[(r,i)][(s,j)] N[s][b] */
-  const int ncol = 3 * nen;
-  for (int idx = lane; idx < 15 * ncol; idx += 16) {
-    const int ri = idx / ncol, c = idx - ri * ncol;
-    const int b = c / 3, j = c - 3 * b;
-    double s = 0.0;
-#pragma unroll
-    for (int sr = 0; sr < 5; sr++) s += Dsh[slot][ri * 16 + 3 * sr + j] * tab[sr * 16 + b];
-    Tsh[slot][ri * 48 + c] = s;
-  }
   __syncwarp();
   if (!live) return;
   /* Follower-pressure load stiffness: every corner carries P/6 (x2-x1)x(x3-x1),
@@ -309,37 +374,13 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
      entering K = dR/dx with a minus sign at the corner rows. */
   const int cs = m.ecorner[e];
   const int cslot[3] = {cs & 31, (cs >> 5) & 31, (cs >> 10) & 31};
-  double dc[3][3][3];   /* dc[k] = d c / d x_k as a 3x3 matrix */
-  {
-    double X[3][3];
-    for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
-    const double av[3] = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
-    const double bv[3] = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
-    const double vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
-    const double sc = -p.pressure / 6.0;
-    for (int k = 0; k < 3; k++) {
-      const double *v = vv[k];
-      dc[k][0][0] = 0.0;        dc[k][0][1] = -sc * v[2]; dc[k][0][2] = sc * v[1];
-      dc[k][1][0] = sc * v[2];  dc[k][1][1] = 0.0;        dc[k][1][2] = -sc * v[0];
-      dc[k][2][0] = -sc * v[1]; dc[k][2][1] = sc * v[0];  dc[k][2][2] = 0.0;
-    }
-  }
-  /* K_e[(a,i)][(b,j)] = sum_r N[r][a] T[(r,i)][(b,j)], block layout (a*nen+b)*9 + 3i + j */
-  double *ke = m.ke + (size_t)m.kofs[e] * 9;
-  const int nval = 9 * nen * nen;
-  for (int idx = lane; idx < nval; idx += 16) {
-    const int blk = idx / 9, w = idx - 9 * blk;
-    const int a = blk / nen, b = blk - a * nen;
-    const int i = w / 3, j = w - 3 * i;
-    double s = 0.0;
-#pragma unroll
-    for (int r = 0; r < 5; r++) s += tab[r * 16 + a] * Tsh[slot][(3 * r + i) * 48 + 3 * b + j];
-    if (p.pressure != 0.0 && (a == cslot[0] || a == cslot[1] || a == cslot[2])) {
-      for (int k = 0; k < 3; k++)
-        if (b == cslot[k]) s += dc[k][i][j];
-    }
-    ke[idx] = s;
-  }
+  double X[3][3];
+  for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
+  const double av[3] = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
+  const double bv[3] = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
+  const double vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
+  contract_element<double>(D, kDRow, tab, nen, lane, cslot, p.pressure != 0.0, vv, -p.pressure / 6.0,
+                           m.ke + (size_t)m.kofs[e] * 9);
 }
 
 /* ---------------- FP32-bulk tangent ---------------- */
@@ -353,8 +394,10 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
 {
   __shared__ float tabs[kNumTables * 80];
   __shared__ float tsum[kNumTables * 5];
-  __shared__ float Dsh[kTanElemsPerCta][15 * 16];
-  __shared__ float Tsh[kTanElemsPerCta][15 * 48];
+  /* D = df/dy per element: row stride 20 and element stride 323 (3 mod 32
+     banks) keep the 9 (i, j) rows and columns the lanes read in distinct banks */
+  constexpr int kDRow = 20, kDSlot = 323;
+  __shared__ float Dsh[kTanElemsPerCta * kDSlot];
   __shared__ float JshF[kTanElemsPerCta][kMaxQp * 21];
   for (int i = threadIdx.x; i < kNumTables * 85; i += blockDim.x) {
     if (i < kNumTables * 80) tabs[i] = m.ntabF[i]; else tsum[i - kNumTables * 80] = m.ntabF[i];
@@ -401,9 +444,10 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
   const EPar<float> ep = epar<float>(p);
   elem_forces_split<float>(y, ep, m.erefF + ee, p.ne, lane, JshF[slot], fd, st);
   if (live) set_status(m.status, st);
+  float *D = Dsh + slot * kDSlot;
   if (lane < 15) {
 #pragma unroll
-    for (int r = 0; r < 15; r++) Dsh[slot][r * 16 + lane] = fd[r].d;
+    for (int r = 0; r < 15; r++) D[r * kDRow + lane] = fd[r].d;
   }
   /* pressure stiffness from the shifted corner coordinates */
   const int cs = m.ecorner[ee];
@@ -415,45 +459,12 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
     xk[k][2] = __shfl_sync(hmask, dz, cslot[k], 16);
   }
   __syncwarp();
-  const int ncol = 3 * nen;
-  for (int idx = lane; idx < 15 * ncol; idx += 16) {
-    const int ri = idx / ncol, c = idx - ri * ncol;
-    const int b = c / 3, j = c - 3 * b;
-    float sacc = 0.f;
-#pragma unroll
-    for (int sr = 0; sr < 5; sr++) sacc = fmaf(Dsh[slot][ri * 16 + 3 * sr + j], tab[sr * 16 + b], sacc);
-    Tsh[slot][ri * 48 + c] = sacc;
-  }
-  __syncwarp();
   if (!live) return;
-  float dc[3][3][3];
-  {
-    const float av[3] = {xk[1][0] - xk[0][0], xk[1][1] - xk[0][1], xk[1][2] - xk[0][2]};
-    const float bv[3] = {xk[2][0] - xk[0][0], xk[2][1] - xk[0][1], xk[2][2] - xk[0][2]};
-    const float vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
-    const float sc = -p.pres6f;
-    for (int k = 0; k < 3; k++) {
-      const float *v = vv[k];
-      dc[k][0][0] = 0.f;        dc[k][0][1] = -sc * v[2]; dc[k][0][2] = sc * v[1];
-      dc[k][1][0] = sc * v[2];  dc[k][1][1] = 0.f;        dc[k][1][2] = -sc * v[0];
-      dc[k][2][0] = -sc * v[1]; dc[k][2][1] = sc * v[0];  dc[k][2][2] = 0.f;
-    }
-  }
-  float *ke = m.keF + (size_t)m.kofs[e] * 9;
-  const int nval = 9 * nen * nen;
-  for (int idx = lane; idx < nval; idx += 16) {
-    const int blk = idx / 9, w = idx - 9 * blk;
-    const int a = blk / nen, b = blk - a * nen;
-    const int i = w / 3, j = w - 3 * i;
-    float sacc = 0.f;
-#pragma unroll
-    for (int r = 0; r < 5; r++) sacc = fmaf(tab[r * 16 + a], Tsh[slot][(3 * r + i) * 48 + 3 * b + j], sacc);
-    if (p.pres6f != 0.f && (a == cslot[0] || a == cslot[1] || a == cslot[2])) {
-      for (int k = 0; k < 3; k++)
-        if (b == cslot[k]) sacc += dc[k][i][j];
-    }
-    ke[idx] = sacc;
-  }
+  const float av[3] = {xk[1][0] - xk[0][0], xk[1][1] - xk[0][1], xk[1][2] - xk[0][2]};
+  const float bv[3] = {xk[2][0] - xk[0][0], xk[2][1] - xk[0][1], xk[2][2] - xk[0][2]};
+  const float vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
+  contract_element<float>(D, kDRow, tab, nen, lane, cslot, p.pres6f != 0.f, vv, -p.pres6f,
+                          m.keF + (size_t)m.kofs[e] * 9);
 }
 
 /* FP32 block gather with compensated (Kahan) summation in element order. */
