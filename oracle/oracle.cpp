@@ -142,8 +142,8 @@ static int set_basis_tables(int kind)
 }
 static const int g_tables_init = set_basis_tables(0);
 
+/* Gauss-Legendre points/weights on [-1,1] (active_strain.c:174-230 for n = 1..5;
    n = 6 is an extension: the reference stops at 5). */
-   n = 6 is an extension of this build, the reference stops at 5). */
 static int gauss_rule(int n, double *th, double *w)
 {
   switch (n) {
