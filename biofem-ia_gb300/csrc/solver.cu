@@ -295,9 +295,11 @@ __device__ __forceinline__ bool gm_done(const GmState *gs) { return gs->done != 
 
 /* Second projection and normalisation in one pass: v = (w - V h) / h_{j+1,j}.
    With nv = 0 it starts a cycle: v0 = r / beta.  Skipped once the cycle has
-   converged (the next basis vector is unused). */
-__global__ void k_gs_update(int n, int nv, const double *__restrict__ V, size_t ld, const double *__restrict__ h,
-                            const double *__restrict__ w, double *__restrict__ v, const GmState *__restrict__ gs)
+   converged (the next basis vector is unused).  w and v may be the same
+   vector, and v may be a column of V beyond the nv read (no restrict on
+   them). */
+__global__ void k_gs_update(int n, int nv, const double *V, size_t ld, const double *__restrict__ h,
+                            const double *w, double *v, const GmState *__restrict__ gs)
 {
   if (gs->done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -565,7 +567,7 @@ int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, doub
   Gmres gm(dm, kp, f32, dK, w, amg, st);
   int rc;
   auto norm = [&](const double *v, double &out) -> int {
-    double d2;
+    double d2 = 0.0;
     int r = gm.dot2(v, v, d2);
     out = std::sqrt(d2);
     return r;
