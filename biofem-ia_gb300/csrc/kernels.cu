@@ -262,78 +262,6 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
 
 /* ---------------- tangent element kernel ---------------- */
 constexpr int kTanElemsPerCta = 8;   /* 16 lanes per element, 128 threads */
-constexpr int kKRounds = (9 * 16 + 15) / 16;   /* offsets per lane of a 9 nen block row, nen <= 16 */
-
-/* Entry (i, j) of the follower-pressure block d c / d x_k = [s v]x (the cross
-   product matrix of s v), for runtime i, j. */
-template <class R>
-__device__ __forceinline__ R skew_entry(int i, int j, const R v[3], R s)
-{
-  if (i == j) return R(0);
-  const int m3 = 3 - i - j;
-  const R vm = m3 == 0 ? v[0] : (m3 == 1 ? v[1] : v[2]);
-  const R t = s * vm;
-  return (j - i + 3) % 3 == 1 ? -t : t;
-}
-
-/* K_e = N^T D N of one element in its 16 lanes, T = D N kept in registers.
-   Lane l owns the offsets o = l + 16k (k < kKRounds, o < 9 nen) of a block
-   row, o = 9b + 3i + j, and forms T[(r,i)][(b,j)] = sum_s D[3r+i][3s+j] N[s][b]
-   (r < 5) for them once; then for every row node a it writes
-   K[(a,i)][(b,j)] = sum_r N[r][a] T[(r,i)][(b,j)], plus the follower-pressure
-   block when a and b are corner slots, to ke[9 nen a + o] (block layout
-   (a nen + b) 9 + 3i + j): consecutive lanes write consecutive values.  The
-   summation order of every entry is that of the two-pass form (T, then K).
-   D: this element's D = df/dy, row stride drow.  vv, sc: the pressure block
-   of corner k is the cross-product matrix of sc vv[k]. */
-template <class R>
-__device__ __forceinline__ void contract_element(const R *D, int drow, const R *tab, int nen, int lane,
-                                                 const int cslot[3], bool pressure, const R vv[3][3], R sc, R *ke)
-{
-  const int lim = 9 * nen;
-  R T[kKRounds][5], P[kKRounds];
-#pragma unroll
-  for (int k = 0; k < kKRounds; k++) {
-    if (16 * k < lim) {   /* the same for the 16 lanes of the element */
-      const int o = lane + 16 * k;
-      const int oc = o < lim ? o : 0;
-      const int b = oc / 9, w = oc - 9 * b, i = w / 3, j = w - 3 * i;
-#pragma unroll
-      for (int r = 0; r < 5; r++) {
-        R acc = R(0);
-#pragma unroll
-        for (int sr = 0; sr < 5; sr++) acc = fma(D[(3 * r + i) * drow + 3 * sr + j], tab[sr * 16 + b], acc);
-        T[k][r] = acc;
-      }
-      R pk = R(0);
-      if (pressure) {
-#pragma unroll
-        for (int c = 0; c < 3; c++)
-          if (b == cslot[c]) pk = pk + skew_entry(i, j, vv[c], sc);
-      }
-      P[k] = pk;
-    }
-  }
-  for (int a = 0; a < nen; a++) {
-    R Na[5];
-#pragma unroll
-    for (int r = 0; r < 5; r++) Na[r] = tab[r * 16 + a];
-    const bool corner = pressure && (a == cslot[0] || a == cslot[1] || a == cslot[2]);
-    R *row = ke + (size_t)a * lim;
-#pragma unroll
-    for (int k = 0; k < kKRounds; k++) {
-      if (16 * k < lim) {
-        const int o = lane + 16 * k;
-        R acc = R(0);
-#pragma unroll
-        for (int r = 0; r < 5; r++) acc = fma(Na[r], T[k][r], acc);
-        if (corner) acc += P[k];
-        if (o < lim) row[o] = acc;
-      }
-    }
-  }
-}
-
 __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
 {
   __shared__ double tabs[kNumTables * 80];

@@ -1,0 +1,56 @@
+/* Host driver of contract_element (element.cuh) for tests/test_contraction_host.py:
+   reads one case (nen, corner slots, pressure flag, D 15x15, the 5x16 basis
+   table, the three corner vectors and the scale) from argv[1], runs the 16
+   lanes one after another in double and in float, and writes both element
+   matrices (9 nen^2 values each, as double; entries never written keep NaN)
+   to argv[2]. */
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "../biofem-ia_gb300/csrc/element.cuh"
+
+using namespace biofem;
+
+template <class R>
+static void run(const double *Din, const double *tabin, int nen, const int cs[3], bool pres, const double *vvin,
+                double sc, double *out)
+{
+  const int drow = 20;
+  std::vector<R> D(15 * drow, R(0)), tab(80, R(0)), ke((size_t)9 * nen * nen, R(NAN));
+  for (int r = 0; r < 15; r++)
+    for (int c = 0; c < 15; c++) D[r * drow + c] = (R)Din[15 * r + c];
+  for (int i = 0; i < 80; i++) tab[i] = (R)tabin[i];
+  R vv[3][3];
+  for (int k = 0; k < 3; k++)
+    for (int d = 0; d < 3; d++) vv[k][d] = (R)vvin[3 * k + d];
+  for (int lane = 0; lane < 16; lane++)
+    contract_element<R>(D.data(), drow, tab.data(), nen, lane, cs, pres, vv, (R)sc, ke.data());
+  for (size_t i = 0; i < ke.size(); i++) out[i] = (double)ke[i];
+}
+
+int main(int argc, char **argv)
+{
+  if (argc != 3) return 2;
+  FILE *f = std::fopen(argv[1], "rb");
+  if (!f) return 3;
+  int hdr[5];
+  double D[225], tab[80], vv[9], sc;
+  const bool ok = std::fread(hdr, sizeof(int), 5, f) == 5 && std::fread(D, sizeof(double), 225, f) == 225 &&
+                  std::fread(tab, sizeof(double), 80, f) == 80 && std::fread(vv, sizeof(double), 9, f) == 9 &&
+                  std::fread(&sc, sizeof(double), 1, f) == 1;
+  std::fclose(f);
+  if (!ok) return 4;
+  const int nen = hdr[0], cs[3] = {hdr[1], hdr[2], hdr[3]};
+  const bool pres = hdr[4] != 0;
+  if (nen < 1 || nen > 16) return 5;
+  std::vector<double> o64((size_t)9 * nen * nen), o32(o64.size());
+  run<double>(D, tab, nen, cs, pres, vv, sc, o64.data());
+  run<float>(D, tab, nen, cs, pres, vv, sc, o32.data());
+  FILE *g = std::fopen(argv[2], "wb");
+  if (!g) return 6;
+  std::fwrite(o64.data(), sizeof(double), o64.size(), g);
+  std::fwrite(o32.data(), sizeof(double), o32.size(), g);
+  std::fclose(g);
+  return 0;
+}
