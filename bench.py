@@ -152,6 +152,29 @@ def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0, residual_
     return n_elems * len(times) / sum(times), sum(times), n_elems
 
 
+def cpu_jfnk_step(threads):
+    """One Newton step of the reference's own solver path (Jacobian-free
+    Newton, unpreconditioned GMRES(30) on finite-difference J v) on C1, on
+    the oracle residual with `threads` OpenMP threads: its wall time and how
+    many residual evaluations it took."""
+    from oracle.pyoracle import Oracle
+    from biofem import configs
+    from biofem.gpu import GpuShell
+    w = configs.C1
+    mesh = w.build_mesh()
+    host = GpuShell(mesh, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    topo = host.topology()
+    host.close()
+    o = Oracle().setup_given_topology(mesh, w, topo, configs.MU, configs.BULK, configs.H0)
+    o.set_threads(threads)
+    x0 = w.initial_x(mesh, topo["xyz0_full"])
+    _, _, st = o.jfnk_newton_step(x0)
+    return {"workload": f"{w.name} ({mesh.n_elmt} triangles), first Newton step from the reference state",
+            "seconds": st["seconds"], "residual_evaluations": st["residual_evaluations"],
+            "gmres_its": st["gmres_its"], "lin_converged": bool(st["lin_converged"]), "cores": threads,
+            "kind": "port"}
+
+
 def max_over_ranks(x: float, dist, device) -> float:
     """The slowest rank's time: every rank's timed region is reduced with MAX
     (replicas: no data exchange inside the timed region)."""
@@ -583,6 +606,10 @@ def run_ours(args):
         cpu["residual_only"] = {"value": rval, "unit": UNIT, "cores": threads, "one_core_value": r1val,
                                 "sample": f"{rn} elements on {threads} threads ({rtot:.2f} s), {r1n} on one "
                                           f"({r1tot:.2f} s): element forces only"}
+        try:   # the reference's solver step, for scale beside the device Newton load step
+            cpu["jfnk_newton_step"] = cpu_jfnk_step(threads)
+        except Exception as exc:   # reported, never fatal to the line
+            cpu["jfnk_newton_step"] = {"error": f"{type(exc).__name__}: {exc}"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",

@@ -323,6 +323,62 @@ class Oracle(_Base):
                 print(f"newton {it}: |R| = {hist[-1]:.3e} alpha {alpha}")
         return x, hist
 
+    def jfnk_newton_step(self, x: np.ndarray, rtol_lin: float = 1e-5, restart: int = 30, max_lin: int = 1000):
+        """One Newton step of the reference's own solver, restated on the
+        oracle residual: SNES newtonls with a matrix-free Jacobian
+        (MatCreateSNESMF, main.c:461-466), J v by the MatMFFD 'wp' difference
+        (R(x + h v) - R(x)) / h with h = sqrt(eps) sqrt(1 + |x|) / |v|,
+        unpreconditioned GMRES(30) to the default relative tolerance 1e-5 (PETSc
+        defaults; PETSc itself is absent here), then backtracking on ||R||
+        (halving; PETSc's bt line search fits a cubic).  Returns
+        (x_new, R_new, stats) with stats: residual_evaluations, gmres_its,
+        lin_converged, seconds."""
+        import time
+        import scipy.sparse.linalg as spla
+        t0 = time.perf_counter()
+        x = np.array(x, dtype=np.float64)
+        nres = 0
+        R = self.residual(x)
+        nres += 1
+        eps_rel = float(np.sqrt(np.finfo(np.float64).eps))
+        unorm = float(np.linalg.norm(x))
+
+        def mv(v):
+            nonlocal nres
+            vn = float(np.linalg.norm(v))
+            if vn == 0.0:
+                return np.zeros_like(v)
+            h = eps_rel * np.sqrt(1.0 + unorm) / vn
+            nres += 1
+            return (self.residual(x + h * v) - R) / h
+
+        n = R.size
+        A = spla.LinearOperator((n, n), matvec=mv, dtype=np.float64)
+        its = [0]
+
+        def cb(_):
+            its[0] += 1
+
+        cycles = max(1, (max_lin + restart - 1) // restart)
+        try:
+            dx, info = spla.gmres(A, -R, rtol=rtol_lin, atol=0.0, restart=restart, maxiter=cycles,
+                                  callback=cb, callback_type="pr_norm")
+        except TypeError:   # scipy before the rtol keyword
+            dx, info = spla.gmres(A, -R, tol=rtol_lin, atol=0.0, restart=restart, maxiter=cycles,
+                                  callback=cb, callback_type="pr_norm")
+        rn = float(np.linalg.norm(R))
+        alpha = 1.0
+        for _ in range(12):
+            xt = x + alpha * dx
+            Rt = self.residual(xt)
+            nres += 1
+            if np.linalg.norm(Rt) <= (1 - 1e-4 * alpha) * rn:
+                break
+            alpha *= 0.5
+        stats = {"residual_evaluations": nres, "gmres_its": its[0], "lin_converged": info == 0,
+                 "step_length": alpha, "seconds": time.perf_counter() - t0}
+        return xt, Rt, stats
+
     def elem_state(self, x: np.ndarray, ec: int, n_qp: int):
         x = np.ascontiguousarray(x, dtype=np.float64)
         S = np.zeros((n_qp, 3, 3))
