@@ -292,13 +292,19 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   }
   for (int i = 0; i < nt; i++) rptr[i + 1] += rptr[i];
   ridx.assign(rptr[nt], 0);
+  std::vector<int> r_elem(rptr[nt]), r_slot(rptr[nt]);   /* ridx split, for the host loops below */
   {
     std::vector<int> fill(rptr.begin(), rptr.end() - 1);
     for (int e = 0; e < ne; e++) {
       const int nen = einfo[e] & 0xff;
       for (int a = 0; a < nen; a++) {
         const int node = T.patch[16 * (size_t)e + a];
-        if (node < nv) ridx[fill[node]++] = (int)((long long)3 * a * ne + e);
+        if (node < nv) {
+          const int c = fill[node]++;
+          ridx[c] = (int)((long long)3 * a * ne + e);
+          r_elem[c] = e;
+          r_slot[c] = a;
+        }
       }
     }
   }
@@ -323,75 +329,81 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
     return 3;
   };
 
-  /* BSR pattern */
-  m->rowptr.assign(nt + 1, 0);
-  std::vector<std::vector<int>> rows_tmp;  /* built row by row below */
-  std::vector<int> mark(nt, -1);
-  std::vector<int> cols_acc;
-  m->colind.clear();
-  for (int i = 0; i < nt; i++) {
-    cols_acc.clear();
-    if (rowkind[i] != 0) {
-      cols_acc.push_back(i);
-    } else {
-      cols_acc.push_back(i);
-      mark[i] = i;
-      for (int c = rptr[i]; c < rptr[i + 1]; c++) {
-        const int e = ridx[c] % ne;
-        const int nen = einfo[e] & 0xff;
-        for (int b = 0; b < nen; b++) {
-          int cols[3], sg[3];
-          const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
-          for (int q = 0; q < k; q++)
-            if (mark[cols[q]] != i) { mark[cols[q]] = i; cols_acc.push_back(cols[q]); }
-        }
-      }
-      std::sort(cols_acc.begin(), cols_acc.end());
-    }
-    m->colind.insert(m->colind.end(), cols_acc.begin(), cols_acc.end());
-    m->rowptr[i + 1] = (int)m->colind.size();
-  }
-  m->nnzb = (long long)m->colind.size();
-  blkrow.assign(m->nnzb, 0);
-  for (int i = 0; i < nt; i++) for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) blkrow[k] = i;
-
-  /* element-block -> tangent-block contributions, element order.  Built row
-     by row: the row's (element, slot) list is in increasing element order
+  /* BSR pattern and element-block -> tangent-block contributions, row by
+     row in one sweep: the row's columns are collected and sorted while the
+     contributions per column are counted, then the same (element, slot)
+     list is walked again, still in cache, to fill the row's contribution
+     lists.  The row's (element, slot) list is in increasing element order
      and a real node fills one slot of a patch, so each block receives its
      contributions in element order, then slot b, then ghost parent q.  A
      column -> block table of the current row makes each lookup O(1). */
-  cptr.assign(m->nnzb + 1, 0);
+  m->rowptr.assign(nt + 1, 0);
+  m->colind.clear();
+  cptr.assign(1, 0);
+  cidx.clear();
+  std::vector<int> mark(nt, -1), ccount(nt, 0);
   std::vector<long long> colpos(nt, -1);
-  for (int pass = 0; pass < 2; pass++) {
-    std::vector<long long> fill;
-    if (pass == 1) {
-      for (long long k = 0; k < m->nnzb; k++) cptr[k + 1] += cptr[k];
-      m->ncontrib = cptr[m->nnzb];
-      if (m->ncontrib >= (1LL << 31)) return fail(63, "assembly map exceeds int32");
-      cidx.assign(m->ncontrib, 0);
-      fill.assign(cptr.begin(), cptr.end() - 1);
+  std::vector<int> cols_acc;
+  std::vector<long long> fill;
+  m->colind.reserve((size_t)nt * 40);
+  cptr.reserve((size_t)nt * 40 + 1);
+  cidx.reserve((size_t)rptr[nt] * 14);
+  for (int i = 0; i < nt; i++) {
+    cols_acc.clear();
+    const long long row0 = (long long)m->colind.size();
+    if (rowkind[i] != 0) {
+      m->colind.push_back(i);
+      cptr.push_back(cptr.back());
+      m->rowptr[i + 1] = (int)m->colind.size();
+      continue;
     }
-    for (int i = 0; i < nv; i++) {
-      if (rowkind[i] != 0) continue;
-      for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) colpos[m->colind[k]] = k;
-      for (int c = rptr[i]; c < rptr[i + 1]; c++) {
-        const int e = ridx[c] % ne, a = ridx[c] / (3 * ne);
-        const int nen = einfo[e] & 0xff;
-        for (int b = 0; b < nen; b++) {
-          int cols[3], sg[3];
-          const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
-          const long long blk_id = kofs[e] + (long long)a * nen + b;
-          for (int q = 0; q < k; q++) {
-            const long long kb = colpos[cols[q]];
-            if (kb < 0) return fail(77, "tangent pattern is missing an element block");
-            if (pass == 0) cptr[kb + 1]++;
-            else cidx[fill[kb]++] = sg[q] > 0 ? (int)blk_id : (int)(-(blk_id + 1));
-          }
+    cols_acc.push_back(i);
+    mark[i] = i;
+    for (int c = rptr[i]; c < rptr[i + 1]; c++) {
+      const int e = r_elem[c];
+      const int nen = einfo[e] & 0xff;
+      for (int b = 0; b < nen; b++) {
+        int cols[3], sg[3];
+        const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
+        for (int q = 0; q < k; q++) {
+          if (mark[cols[q]] != i) { mark[cols[q]] = i; cols_acc.push_back(cols[q]); }
+          ccount[cols[q]]++;
         }
       }
-      for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) colpos[m->colind[k]] = -1;
     }
+    std::sort(cols_acc.begin(), cols_acc.end());
+    fill.clear();
+    for (size_t t = 0; t < cols_acc.size(); t++) {
+      const int col = cols_acc[t];
+      m->colind.push_back(col);
+      colpos[col] = row0 + (long long)t;
+      fill.push_back(cptr.back());
+      cptr.push_back(cptr.back() + ccount[col]);
+      ccount[col] = 0;
+    }
+    if (cptr.back() >= (1LL << 31)) return fail(63, "assembly map exceeds int32");
+    cidx.resize(cptr.back());
+    for (int c = rptr[i]; c < rptr[i + 1]; c++) {
+      const int e = r_elem[c], a = r_slot[c];
+      const int nen = einfo[e] & 0xff;
+      const long long blk0 = kofs[e] + (long long)a * nen;
+      for (int b = 0; b < nen; b++) {
+        int cols[3], sg[3];
+        const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
+        const long long blk_id = blk0 + b;
+        for (int q = 0; q < k; q++) {
+          const long long kb = colpos[cols[q]];
+          if (kb < row0) return fail(77, "tangent pattern is missing an element block");
+          cidx[fill[kb - row0]++] = sg[q] > 0 ? (int)blk_id : (int)(-(blk_id + 1));
+        }
+      }
+    }
+    m->rowptr[i + 1] = (int)m->colind.size();
   }
+  m->nnzb = (long long)m->colind.size();
+  m->ncontrib = cptr.back();
+  blkrow.assign(m->nnzb, 0);
+  for (int i = 0; i < nt; i++) for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) blkrow[k] = i;
   /* dA0 on the host too (GetGpuTopology) */
   m->dA0.assign(ne, 0.0);
   for (int e = 0; e < ne; e++) m->dA0[e] = tri_area0(T, e);
