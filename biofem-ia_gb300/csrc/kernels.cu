@@ -262,6 +262,7 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
 
 /* ---------------- tangent element kernel ---------------- */
 constexpr int kTanElemsPerCta = 8;   /* 16 lanes per element, 128 threads */
+
 __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
 {
   __shared__ double tabs[kNumTables * 80];
@@ -284,9 +285,9 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
   gather_y_group(m.pos, m.patch, ee, nen, tab, lane, y);
   double fd[15];
   const EPar<double> ep = epar<double>(p);
-  /* the thickness-point metrics, the primal geometry and the primal C33
-     sub-iteration values come from k_elem_residual, launched before this
-     kernel (which also performs the CC3333 checks) */
+  /* the thickness-point metrics, the primal geometry and resultants and the
+     primal C33 sub-iteration values come from k_elem_residual, launched
+     before this kernel (which also performs the CC3333 checks) */
   elem_forces_split_tl<double>(y, ep, m.eref + ee, p.ne, m.gpr + ee, lane, Jsh[slot], fd, m.gmq + ee, m.gtape + ee);
   /* column `lane` of D = df/dy */
   double *D = Dsh + slot * kDSlot;
