@@ -1,25 +1,37 @@
-"""Build recipe for oracle/_ref/libbiofem_ref.so (TEST INFRASTRUCTURE ONLY).
+"""Build recipe for oracle/_ref/libbiofem_ref.so and oracle/_ref/libbiofem_ref_dyn.so
+(TEST INFRASTRUCTURE ONLY).
 
-Compiles the reference's own, unmodified hot-path C files where they lie
-(``/root/reference/src/{active_strain,math,bending,io,external}.c``) together
-with the petsc-lite shim (oracle/petsc_lite/) and the np = 1 driver
-(oracle/ref_driver.c).  The result is the checker that pins the restated oracle
-and generates tests/golden/.  It is built only where the reference sources
-exist; nothing on the product path links it.
+libbiofem_ref.so compiles the reference's own, unmodified hot-path C files
+where they lie (``<reference>/src/{active_strain,math,bending,io,external}.c``)
+together with the petsc-lite shim (oracle/petsc_lite/) and the np = 1 driver
+(oracle/ref_driver.c).  libbiofem_ref_dyn.so adds the reference's src/main.c
+(FDynamic, xAccVel; its ``main`` renamed) and src/material.c (Mass, Damp); the
+driver is compiled with -DREF_DRIVER_WITH_MAIN so that main.c's globals are
+the ones used, and every external that main.c names but the dynamic term
+never calls (SNES, DMPlex setup, LV mesh loaders, CUDA / Kokkos bridges, ...)
+is resolved by an abort stub generated here from the linker's list of
+undefined references.  The results are the checkers that pin the restated
+oracle and generate tests/golden/.  They are built only where the reference
+sources exist; nothing on the product path links them.
+
+The reference root is BIOFEM_REFERENCE_ROOT if set, else /root/reference.
 """
 from __future__ import annotations
 
 import os
+import re
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path("/root/reference")
+REFERENCE = Path(os.environ.get("BIOFEM_REFERENCE_ROOT", "/root/reference"))
 OUT_DIR = HERE / "_ref"
 LIB = OUT_DIR / "libbiofem_ref.so"
+LIB_DYN = OUT_DIR / "libbiofem_ref_dyn.so"
 REF_SOURCES = ["active_strain.c", "math.c", "bending.c", "io.c", "external.c"]
+DYN_SOURCES = ["main.c", "material.c"]
 # -ffp-contract=off keeps every multiply and add separately rounded, so the
 # reference build and the restated oracle agree bit for bit on any host.
 CFLAGS = ["-O2", "-ffp-contract=off", "-fPIC", "-w", "-std=gnu11"]
@@ -29,6 +41,25 @@ def available() -> bool:
     return (REFERENCE / "src" / "active_strain.c").is_file()
 
 
+def _inc() -> list[str]:
+    return ["-I", str(HERE / "petsc_lite"), "-iquote", str(REFERENCE / "include")]
+
+
+def _compile(src: Path, obj: Path, extra: list[str], verbose: bool) -> Path:
+    cmd = ["gcc", "-c", *CFLAGS, *extra, *_inc(), str(src), "-o", str(obj)]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.run(cmd, check=True)
+    return obj
+
+
+def _stale(lib: Path, deps: list[Path]) -> bool:
+    if not lib.exists():
+        return True
+    t = lib.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in deps)
+
+
 def build(force: bool = False, verbose: bool = False) -> Path | None:
     """Compile libbiofem_ref.so; returns its path, or None without the reference."""
     if not available():
@@ -36,31 +67,64 @@ def build(force: bool = False, verbose: bool = False) -> Path | None:
     srcs = [REFERENCE / "src" / s for s in REF_SOURCES]
     srcs += [HERE / "petsc_lite" / "petsc_lite.c", HERE / "ref_driver.c"]
     deps = srcs + list((HERE / "petsc_lite").glob("*.h"))
-    if LIB.exists() and not force:
-        t = LIB.stat().st_mtime
-        if all(p.stat().st_mtime <= t for p in deps):
-            return LIB
+    if not force and not _stale(LIB, deps):
+        return LIB
     OUT_DIR.mkdir(exist_ok=True)
-    inc = ["-I", str(HERE / "petsc_lite"), "-iquote", str(REFERENCE / "include")]
-    objs = []
-
-    def compile_one(src: Path) -> Path:
-        obj = OUT_DIR / (src.stem + ".o")
-        cmd = ["gcc", "-c", *CFLAGS, *inc, str(src), "-o", str(obj)]
-        if verbose:
-            print(" ".join(cmd))
-        subprocess.run(cmd, check=True)
-        return obj
-
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
-        objs = list(ex.map(compile_one, srcs))
-    cmd = ["gcc", "-shared", "-o", str(LIB), *map(str, objs), "-lm"]
-    subprocess.run(cmd, check=True)
+        objs = list(ex.map(lambda s: _compile(s, OUT_DIR / (s.stem + ".o"), [], verbose), srcs))
+    subprocess.run(["gcc", "-shared", "-o", str(LIB), *map(str, objs), "-lm"], check=True)
     for o in objs:
         o.unlink()
     return LIB
 
 
+def build_dyn(force: bool = False, verbose: bool = False) -> Path | None:
+    """Compile libbiofem_ref_dyn.so (the hot path plus main.c and material.c);
+    returns its path, or None without the reference."""
+    if not available():
+        return None
+    srcs = [REFERENCE / "src" / s for s in REF_SOURCES + DYN_SOURCES]
+    srcs += [HERE / "petsc_lite" / "petsc_lite.c", HERE / "ref_driver.c"]
+    deps = srcs + list((HERE / "petsc_lite").glob("*.h"))
+    if not force and not _stale(LIB_DYN, deps):
+        return LIB_DYN
+    OUT_DIR.mkdir(exist_ok=True)
+    work = OUT_DIR / "dyn_obj"
+    work.mkdir(exist_ok=True)
+
+    def one(src: Path) -> Path:
+        extra = []
+        if src.name == "main.c":
+            extra = ["-Dmain=biofem_reference_main_unused"]
+        elif src.name == "ref_driver.c":
+            extra = ["-DREF_DRIVER_WITH_MAIN"]
+        return _compile(src, work / (src.stem + ".o"), extra, verbose)
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(one, srcs))
+    # the externals nothing here defines: ask the linker, then stub them
+    probe = subprocess.run(["gcc", "-shared", "-Wl,--no-undefined", "-o", str(work / "probe.so"), *map(str, objs),
+                            "-lm"], capture_output=True, text=True)
+    missing = sorted(set(re.findall(r"undefined reference to `([A-Za-z_][A-Za-z0-9_]*)'", probe.stderr)))
+    stub = work / "abort_stubs.c"
+    with open(stub, "w") as f:
+        f.write("/* generated by oracle/build_ref.py: externals the dynamic term never calls */\n")
+        f.write("#include <stdio.h>\n#include <stdlib.h>\n")
+        for name in missing:
+            f.write(f"int {name}(void) {{ fprintf(stderr, \"oracle/_ref: {name} is off the dynamic path\\n\"); "
+                    f"abort(); }}\n")
+    stub_o = _compile(stub, work / "abort_stubs.o", [], verbose)
+    subprocess.run(["gcc", "-shared", "-Wl,--no-undefined", "-o", str(LIB_DYN), *map(str, objs), str(stub_o),
+                    "-lm"], check=True)
+    for o in list(objs) + [stub_o, stub, work / "probe.so"]:
+        if o.exists():
+            o.unlink()
+    work.rmdir()
+    return LIB_DYN
+
+
 if __name__ == "__main__":
     p = build(force="--force" in sys.argv, verbose=True)
+    print(p if p else "reference sources not present; nothing built")
+    p = build_dyn(force="--force" in sys.argv, verbose=True)
     print(p if p else "reference sources not present; nothing built")

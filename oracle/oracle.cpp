@@ -167,7 +167,12 @@ struct Params {
   int n_qp, c33_iters, clamp;
   double mu, K, h0, gamma, pressure;
   double theta[kMaxQp], w[kMaxQp];
+  int dead_load = 0;   /* 1: SurfaceConstNormalPressure (external.c:699-730) instead of the follower load */
+  int iso_act = 0;     /* 1: -cart_fib_act 0, the isotropic active gradient (active_strain.c:1238-1255) */
 };
+
+/* load / activation options of the next setup (oracle_set_load_options) */
+static int g_dead_load = 0, g_iso_act = 0;
 
 struct Mesh {
   int n_v = 0, n_elmt = 0, n_ghosts = 0, n_edge = 0;
@@ -180,12 +185,53 @@ struct Mesh {
 };
 
 /* ---------------- topology (bending.c) ---------------- */
+/* The reference's searches scan every triangle for each query
+   (O(N_e^2) overall).  Every query looks for triangles holding a given node,
+   and the result of each is the last match in triangle order, so scanning only
+   the triangles incident to that node, in increasing index, gives the same
+   tables (the fast mode, oracle_set_fast_topology; tests pin both modes
+   against the reference build).  scan_tris(node, f) calls f(i) for the
+   candidate triangles i in increasing order. */
+static int g_fast_topology = 0;
+
+struct TriScan {
+  const Mesh &m;
+  int ntri;
+  bool fast;
+  std::vector<int> ptr, idx;   /* node -> incident triangles (fast mode) */
+  TriScan(const Mesh &mm, int nt, int nnode, bool f) : m(mm), ntri(nt), fast(f)
+  {
+    if (!fast) return;
+    ptr.assign(nnode + 1, 0);
+    for (int i = 0; i < nt; i++) {
+      const int c[3] = {m.nv1[i], m.nv2[i], m.nv3[i]};
+      for (int k = 0; k < 3; k++)
+        if (c[k] >= 0 && c[k] < nnode && (k == 0 || c[k] != c[0]) && (k < 2 || c[k] != c[1])) ptr[c[k] + 1]++;
+    }
+    for (int v = 0; v < nnode; v++) ptr[v + 1] += ptr[v];
+    idx.assign(ptr[nnode], 0);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (int i = 0; i < nt; i++) {
+      const int c[3] = {m.nv1[i], m.nv2[i], m.nv3[i]};
+      for (int k = 0; k < 3; k++)
+        if (c[k] >= 0 && c[k] < nnode && (k == 0 || c[k] != c[0]) && (k < 2 || c[k] != c[1])) idx[fill[c[k]]++] = i;
+    }
+  }
+  template <class F> void operator()(int node, F f) const
+  {
+    if (!fast) { for (int i = 0; i < ntri; i++) f(i); return; }
+    if (node < 0 || node + 1 >= (int)ptr.size()) return;   /* no triangle holds it */
+    for (int k = ptr[node]; k < ptr[node + 1]; k++) f(idx[k]);
+  }
+};
+
 /* GlobalGhostInit, bending.c:1670-1757.  Writes ghost coordinates into
    (x, y, z) and the reference arrays, and the 2 triangles of every ghost. */
 static void global_ghost_init(Mesh &m, std::vector<double> &x, std::vector<double> &y, std::vector<double> &z)
 {
   int count = 0, nv3 = 0;
   m.ghost_nv3.assign(m.n_ghosts, 0);
+  const TriScan scan(m, m.n_elmt, m.n_v, g_fast_topology != 0);
   for (int edge_n = 0; edge_n < m.n_edge; edge_n++) {
     int start = 0, end = 0;
     for (int e = 0; e < edge_n + 1; e++) end += m.n_bnodes[e];
@@ -195,7 +241,7 @@ static void global_ghost_init(Mesh &m, std::vector<double> &x, std::vector<doubl
     for (int li = 0; li < n_local; li++) {
       const int i = start + li, inext = start + (li + 1) % n_local;
       const int nv1 = m.bnodes[inext], nv2 = m.bnodes[i];
-      for (int ec = 0; ec < m.n_elmt; ec++) {
+      scan(nv1, [&](int ec) {
         int c = 0;
         if (nv1 == m.nv1[ec] || nv1 == m.nv2[ec] || nv1 == m.nv3[ec]) c++;
         if (nv2 == m.nv1[ec] || nv2 == m.nv2[ec] || nv2 == m.nv3[ec]) c++;
@@ -204,7 +250,7 @@ static void global_ghost_init(Mesh &m, std::vector<double> &x, std::vector<doubl
           else if (m.nv2[ec] != nv1 && m.nv2[ec] != nv2) nv3 = m.nv2[ec];
           else nv3 = m.nv3[ec];
         }
-      }
+      });
       const int g = m.n_v + count;
       x[g] = x[nv2] + x[nv1] - x[nv3];
       y[g] = y[nv2] + y[nv1] - y[nv3];
@@ -230,12 +276,18 @@ static void irrver(Mesh &m)
   elmt.reserve(64);
   for (int ec = 0; ec < m.n_elmt; ec++) { m.ire[ec] = 0; m.irv[ec] = 0; m.val[ec] = 6; }
   const int nb = (int)m.bnodes.size();
+  const bool fast = g_fast_topology != 0;
+  const TriScan scan(m, m.n_elmt, m.n_v, fast);
+  std::vector<char> bflag;
+  if (fast) { bflag.assign(m.n_v, 0); for (int i = 0; i < nb; i++) if (m.bnodes[i] >= 0 && m.bnodes[i] < m.n_v) bflag[m.bnodes[i]] = 1; }
   for (int nc = 0; nc < m.n_v; nc++) {
     int count = 0, bcount = 0, is_b = 0;
     elmt.clear();
-    for (int i = 0; i < nb; i++) if (nc == m.bnodes[i]) { is_b = 1; break; }
-    for (int ec = 0; ec < m.n_elmt; ec++)
+    if (fast) is_b = bflag[nc];
+    else for (int i = 0; i < nb; i++) if (nc == m.bnodes[i]) { is_b = 1; break; }
+    scan(nc, [&](int ec) {
       if (nc == m.nv1[ec] || nc == m.nv2[ec] || nc == m.nv3[ec]) { elmt.push_back(ec); count++; }
+    });
     if (is_b) bcount = count + 3;
     if (bcount == 0) {
       if (count != 6) { irr[nc] = 1; for (int e : elmt) { m.ire[e] = 1; m.val[e] = count; } }
@@ -243,13 +295,26 @@ static void irrver(Mesh &m)
       if (bcount != 6) { irr[nc] = 1; for (int e : elmt) { m.ire[e] = 1; m.val[e] = bcount; } }
     }
   }
-  for (int ec = 0; ec < m.n_elmt; ec++)
+  for (int ec = 0; ec < m.n_elmt; ec++) {
+    if (fast) {   /* the corners in increasing node order: the scan over nc keeps the last */
+      int c[3] = {m.nv1[ec], m.nv2[ec], m.nv3[ec]};
+      std::sort(c, c + 3);
+      for (int k = 0; k < 3; k++) {
+        const int nc = c[k];
+        if (nc < 0 || nc >= m.n_v || irr[nc] != 1) continue;
+        if (nc == m.nv1[ec]) m.irv[ec] = 1;
+        if (nc == m.nv2[ec]) m.irv[ec] = 2;
+        if (nc == m.nv3[ec]) m.irv[ec] = 3;
+      }
+      continue;
+    }
     for (int nc = 0; nc < m.n_v; nc++)
       if (irr[nc] == 1) {
         if (nc == m.nv1[ec]) m.irv[ec] = 1;
         if (nc == m.nv2[ec]) m.irv[ec] = 2;
         if (nc == m.nv3[ec]) m.irv[ec] = 3;
       }
+  }
 }
 
 /* One shared-edge search step of Patch(): if triangle (a,b,c) holds both
@@ -267,24 +332,44 @@ static inline void patch_pick(int *p, int A, int B, int n1, int n2, int n3, int 
   }
 }
 
-/* Patch, bending.c:1270-1667 (n_elmt_base = 0). */
+/* Patch, bending.c:1270-1667 (n_elmt_base = 0).  In every pick the node
+   p[A] is a corner of the element (p[3], p[6], p[7] regular; p[0], p[1], p[v]
+   irregular), and no pick overwrites a corner slot for valence v >= 4, so a
+   triangle can match only if it holds one of the three corners: the fast mode
+   runs the reference's loops, picks in the same order, over the triangles
+   incident to the corners in increasing index (valence 3, where slot v - 2 = 1
+   is a corner, keeps the full scan). */
 static void patch_build(Mesh &m)
 {
   const int ntot = m.n_elmt + 2 * m.n_ghosts;
+  const bool fast = g_fast_topology != 0;
+  const TriScan scan(m, ntot, m.n_v + m.n_ghosts, fast);
+  std::vector<int> cand, all;
+  all.resize(ntot);
+  for (int i = 0; i < ntot; i++) all[i] = i;
   int p[64];
   for (int ec = 0; ec < m.n_elmt; ec++) {
     const int v = m.val[ec];
+    const std::vector<int> *tris = &all;
+    if (fast && v >= 4) {
+      cand.clear();
+      const int c[3] = {m.nv1[ec], m.nv2[ec], m.nv3[ec]};
+      for (int k = 0; k < 3; k++) scan(c[k], [&](int i) { cand.push_back(i); });
+      std::sort(cand.begin(), cand.end());
+      cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+      tris = &cand;
+    }
     for (int i = 0; i < v + 6; i++) p[i] = kMissing;
     if (m.ire[ec] == 0) {
       p[3] = m.nv1[ec]; p[6] = m.nv2[ec]; p[7] = m.nv3[ec];
-      for (int i = 0; i < ntot; i++) {
+      for (int i : *tris) {
         const int a = m.nv1[i], b = m.nv2[i], c = m.nv3[i];
         const bool g = (i != ec);
         patch_pick(p, 3, 6, a, b, c, p[3], p[6], p[6], g, 2);
         patch_pick(p, 3, 7, a, b, c, p[3], p[7], p[7], g, 4);
         patch_pick(p, 6, 7, a, b, c, p[6], p[7], p[7], g, 10);
       }
-      for (int i = 0; i < ntot; i++) {
+      for (int i : *tris) {
         const int a = m.nv1[i], b = m.nv2[i], c = m.nv3[i];
         patch_pick(p, 3, 2, a, b, c, p[3], p[2], p[6], true, 0);
         patch_pick(p, 3, 4, a, b, c, p[3], p[4], p[7], true, 1);
@@ -297,14 +382,14 @@ static void patch_build(Mesh &m)
       if (m.irv[ec] == 1) { p[0] = m.nv1[ec]; p[1] = m.nv2[ec]; p[v] = m.nv3[ec]; }
       else if (m.irv[ec] == 2) { p[0] = m.nv2[ec]; p[1] = m.nv3[ec]; p[v] = m.nv1[ec]; }
       else if (m.irv[ec] == 3) { p[0] = m.nv3[ec]; p[1] = m.nv1[ec]; p[v] = m.nv2[ec]; }
-      for (int i = 0; i < ntot; i++) {
+      for (int i : *tris) {
         const int a = m.nv1[i], b = m.nv2[i], c = m.nv3[i];
         const bool g = (i != ec);
         patch_pick(p, 0, 1, a, b, c, p[0], p[1], p[1], g, 2);
         patch_pick(p, 0, v, a, b, c, p[0], p[v], p[v], g, v - 1);
         patch_pick(p, 1, v, a, b, c, p[1], p[v], p[v], g, v + 1);
       }
-      for (int i = 0; i < ntot; i++) {
+      for (int i : *tris) {
         const int a = m.nv1[i], b = m.nv2[i], c = m.nv3[i];
         patch_pick(p, 0, 2, a, b, c, p[0], p[2], p[1], true, 3);
         patch_pick(p, 0, v - 1, a, b, c, p[0], p[v - 1], p[v], true, v - 2);
@@ -315,7 +400,7 @@ static void patch_build(Mesh &m)
       }
       if (m.val[ec] > 6) {
         for (int k = 0; k < v - 6; k++)
-          for (int i = 0; i < ntot; i++) {
+          for (int i : *tris) {
             const int a = m.nv1[i], b = m.nv2[i], c = m.nv3[i];
             patch_pick(p, 0, 3 + k, a, b, c, p[0], p[3 + k], p[2 + k], true, k + 4);
             patch_pick(p, 0, v - 2 - k, a, b, c, p[0], p[v - 2 - k], p[v - 1 - k], true, v - 3 - k);
@@ -488,7 +573,14 @@ static int ref_elem(const Mesh &m, const Params &P, int ec, RefElem &R)
   const double gam = P.gamma * m.gscale[ec];
   const double nf[3] = {m.fib[3 * ec], m.fib[3 * ec + 1], m.fib[3 * ec + 2]};
   double Fc[3][3], Fic[3][3], S[3][3], ST[3][3], tmp[3][3], FaCov[3][3];
-  for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) Fc[i][j] = (i == j ? 1.0 : 0.0) - gam * nf[i] * nf[j];
+  if (!P.iso_act) {   /* cart_fib_act = 1: I - gamma f f^T */
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) Fc[i][j] = (i == j ? 1.0 : 0.0) - gam * nf[i] * nf[j];
+  } else {            /* cart_fib_act = 0: diag(1 - gamma, 1 - gamma, 1 / ((1 - gamma)^2)) */
+    for (int i = 0; i < 3; i++) for (int j = 0; j < 3; j++) Fc[i][j] = 0.0;
+    Fc[0][0] = 1.0 - gam;
+    Fc[1][1] = 1.0 - gam;
+    Fc[2][2] = 1.0 / (Fc[0][0] * Fc[1][1]);
+  }
   for (int q = 0; q < P.n_qp; q++) {
     const double th3 = hhalf * P.theta[q];
     V3<double> g0[3];
@@ -662,7 +754,7 @@ struct Dyn {
   int central = 0, damp = 0;
   double dt = 0, rhoh0 = 0, dampf = 0;
   double M1 = 0, M2 = 0, M3 = 0, C1 = 0, C2 = 0, C3 = 0, U2 = 0, U3 = 0;
-  std::vector<double> dA0;                 /* flat reference area, n_elmt + 2 n_ghosts triangles */
+  std::vector<double> dA0;                 /* flat reference area of every triangle (real ones used) */
   std::vector<double> xn, xnm1, xd, xdd;   /* 3 (n_v + n_ghosts) */
 };
 
@@ -741,12 +833,20 @@ static int residual(const Body &B, const T *x, T *R, T *Fint_out = nullptr, T *F
       for (int d = 0; d < 3; d++) Fint[3 * node + d] = Fint[3 * node + d] + Fb[(size_t)ec * 48 + 3 * i + d];
     }
   }
-  /* SurfaceNormalPressure(P), external.c:589-624 */
+  /* SurfaceNormalPressure(P), external.c:589-624: current normal and area;
+     SurfaceConstNormalPressure(P), external.c:699-730: the reference normal
+     Nf and area dA0 of Init (AreaNormal on the reference coordinates) */
   if (B.P.pressure != 0.0) {
     const double Pp = B.P.pressure;
     for (int ec = 0; ec < m.n_elmt; ec++) {
       T dA; V3<T> n;
-      area_normal(m, xb.data(), yb.data(), zb.data(), ec, dA, n);
+      if (B.P.dead_load) {
+        double dA0; V3<double> N;
+        area_normal(m, m.x0.data(), m.y0.data(), m.z0.data(), ec, dA0, N);
+        dA = T(dA0); n = {T(N.x), T(N.y), T(N.z)};
+      } else {
+        area_normal(m, xb.data(), yb.data(), zb.data(), ec, dA, n);
+      }
       const int c[3] = {m.nv1[ec], m.nv2[ec], m.nv3[ec]};
       for (int k = 0; k < 3; k++) {
         Fext[3 * c[k]] = Fext[3 * c[k]] + n.x * Pp * dA / 3.;
@@ -755,14 +855,15 @@ static int residual(const Body &B, const T *x, T *R, T *Fint_out = nullptr, T *F
       }
     }
   }
-  /* FDynamic, main.c:1157-1360 (serial path): every triangle, ghosts and
-     bridging triangles included, adds M (M1 x - ...) per corner, M = rho h0 dA0 / 3
-     (Mass, material.c:100-119) and C = dampfactor M (Damp, material.c:122-137). */
+  /* FDynamic, main.c:1157-1270 (the path of an active-strain run, whose
+     DMPlex context is initialised, main.c:326-331): every real triangle, in
+     triangle order, adds M (M1 x - ...) per corner, M = rho h0 dA0 / 3 (Mass,
+     material.c:100-119) and C = dampfactor M (Damp, material.c:122-137). */
   std::vector<T> Fdyn(ndof, T(0.0));
   if (B.D.on) {
     const Dyn &D = B.D;
     const T *xc[3] = {xb.data(), yb.data(), zb.data()};
-    for (int ec = 0; ec < m.n_elmt + 2 * m.n_ghosts; ec++) {
+    for (int ec = 0; ec < m.n_elmt; ec++) {
       const double M = D.rhoh0 * D.dA0[ec] / 3;
       const double C = D.damp ? D.dampf * M : 0.0;
       const int c[3] = {m.nv1[ec], m.nv2[ec], m.nv3[ec]};
@@ -833,6 +934,7 @@ int oracle_setup(int n_v, int n_elmt, const int *tri, const double *xyz0,
   if (c33_iters < 1) return 62;
   P.n_qp = n_qp; P.c33_iters = c33_iters; P.mu = mu; P.K = K; P.h0 = h0;
   P.gamma = gamma; P.pressure = pressure; P.clamp = clamp_edge0;
+  P.dead_load = g_dead_load; P.iso_act = g_iso_act;
   m.n_v = n_v; m.n_elmt = n_elmt; m.n_edge = n_edge;
   m.n_bnodes.assign(n_bnodes, n_bnodes + n_edge);
   int sum = 0;
@@ -887,6 +989,7 @@ int oracle_setup_given_topology(int n_v, int n_elmt, const int *tri_all, const d
   if (c33_iters < 1) return 62;
   P.n_qp = n_qp; P.c33_iters = c33_iters; P.mu = mu; P.K = K; P.h0 = h0;
   P.gamma = gamma; P.pressure = pressure; P.clamp = clamp_edge0;
+  P.dead_load = g_dead_load; P.iso_act = g_iso_act;
   m.n_v = n_v; m.n_elmt = n_elmt; m.n_edge = n_edge;
   m.n_bnodes.assign(n_bnodes, n_bnodes + n_edge);
   int sum = 0;
@@ -919,6 +1022,20 @@ int oracle_setup_given_topology(int n_v, int n_elmt, const int *tri_all, const d
 }
 
 int oracle_set_threads(int n) { g_threads = n > 0 ? n : 1; return 0; }
+
+/* 1: oracle_setup builds the topology with the corner-incident scans (O(N),
+   same tables); 0: with the reference's full scans (O(N_e^2)). */
+int oracle_set_fast_topology(int on) { g_fast_topology = on != 0; return 0; }
+
+/* Options of the next setup: dead_load 1 takes SurfaceConstNormalPressure
+   (external.c:699-730) for the pressure, iso_act 1 the isotropic active
+   gradient of -cart_fib_act 0 (active_strain.c:1238-1255). */
+int oracle_set_load_options(int dead_load, int iso_act)
+{
+  g_dead_load = dead_load != 0;
+  g_iso_act = iso_act != 0;
+  return 0;
+}
 
 /* Switch the dynamic term on (dt > 0) or off (dt <= 0): the -dt, -rho,
    -newmark_gamma, -dampfactor, -timeinteg, -damping options of main.c.
@@ -978,14 +1095,14 @@ int oracle_get_dynamic_state(double *xn, double *xnm1, double *xd, double *xdd)
   return 0;
 }
 
-/* xAccVel (main.c:1367-1412, serial path over n_v + n_ghosts nodes), then
-   xnm1 <- xn, xn <- x (main.c:571-572). */
+/* xAccVel (main.c:1367-1412; with the DMPlex context over the n_v real
+   nodes), then xnm1 <- xn, xn <- x over every entry (main.c:571-572). */
 int oracle_dynamic_update(const double *x)
 {
   if (!g_body || !g_body->ready || !g_body->D.on) return 58;
   Dyn &D = g_body->D;
-  const size_t n = D.xn.size();
-  for (size_t j = 0; j < n; j++) {
+  const size_t n = D.xn.size(), nreal = 3 * (size_t)g_body->m.n_v;
+  for (size_t j = 0; j < nreal; j++) {
     const double xddn = D.xdd[j];
     D.xdd[j] = D.M1 * (x[j] - D.xn[j]) - D.M2 * D.xd[j] - D.M3 * D.xdd[j];
     D.xd[j] = D.xd[j] + D.U2 * xddn + D.U3 * D.xdd[j];

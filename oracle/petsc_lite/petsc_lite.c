@@ -230,7 +230,15 @@ PetscErrorCode VecGetOwnershipRange(Vec v, PetscInt *lo, PetscInt *hi) { *lo = 0
    (PetscBinaryWrite / PetscBinaryRead); VecView writes the record
    VEC_FILE_CLASSID (1211214), the length, the values, with 32-bit PetscInt.
    No ".info" side file is written. */
-struct PetscLiteOpaque_ { int fd; };
+/* The one object the opaque handles point at: a binary viewer (fd) or an
+   array-backed SeqBAIJ matrix (the rest); SNES, DM and the others are never created. */
+struct PetscLiteOpaque_ {
+  int fd;
+  PetscInt bs, mb, nb;
+  const PetscInt *i, *j;
+  PetscScalar *a;
+  int locked;   /* between MatSeqBAIJGetArray and MatSeqBAIJRestoreArray */
+};
 #define LITE_VEC_FILE_CLASSID 1211214
 
 static void lite_swap_(unsigned char *b, size_t size, size_t n)
@@ -320,3 +328,60 @@ PetscErrorCode MatZeroEntries(Mat m) { (void)m; LITE_UNSUPPORTED("MatZeroEntries
 PetscErrorCode MatGetSize(Mat m, PetscInt *a, PetscInt *b) { (void)m; (void)a; (void)b; LITE_UNSUPPORTED("MatGetSize"); }
 PetscErrorCode MatCreateSeqDense(MPI_Comm c, PetscInt a, PetscInt b, PetscScalar *d, Mat *m)
 { (void)c; (void)a; (void)b; (void)d; (void)m; LITE_UNSUPPORTED("MatCreateSeqDense"); }
+
+/* The block matrix of MatCreateSeqBAIJWithArrays is the only Mat kind the
+   shim creates (its fields are in struct PetscLiteOpaque_ above). */
+PetscErrorCode MatCreateSeqBAIJWithArrays(MPI_Comm c, PetscInt bs, PetscInt m, PetscInt n, PetscInt i[], PetscInt j[],
+                                          PetscScalar a[], Mat *mat)
+{
+  (void)c;
+  if (!mat || !i || !j || !a || bs < 1 || m % bs || n % bs)
+    return PetscLiteError_(PETSC_ERR_ARG_WRONG, __FILE__, __LINE__, "bad SeqBAIJ arguments");
+  struct PetscLiteOpaque_ *A = (struct PetscLiteOpaque_ *)calloc(1, sizeof(*A));
+  A->bs = bs; A->mb = m / bs; A->nb = n / bs; A->i = i; A->j = j; A->a = a;
+  *mat = A;
+  return 0;
+}
+
+PetscErrorCode MatSeqBAIJGetArray(Mat A, PetscScalar **a)
+{
+  if (!A || A->locked) return PetscLiteError_(PETSC_ERR_ORDER, __FILE__, __LINE__, "array already taken");
+  A->locked = 1;
+  *a = A->a;
+  return 0;
+}
+
+PetscErrorCode MatSeqBAIJRestoreArray(Mat A, PetscScalar **a)
+{
+  if (!A || !A->locked || *a != A->a) return PetscLiteError_(PETSC_ERR_ORDER, __FILE__, __LINE__, "array not taken");
+  A->locked = 0;
+  *a = NULL;
+  return 0;
+}
+
+PetscErrorCode MatAssemblyBegin(Mat A, MatAssemblyType t) { (void)t; return A && !A->locked ? 0 : PETSC_ERR_ORDER; }
+PetscErrorCode MatAssemblyEnd(Mat A, MatAssemblyType t) { (void)t; return A && !A->locked ? 0 : PETSC_ERR_ORDER; }
+
+/* y = A x with the column-by-column block storage */
+PetscErrorCode MatMult(Mat A, Vec x, Vec y)
+{
+  if (!A || x->n != A->nb * A->bs || y->n != A->mb * A->bs)
+    return PetscLiteError_(PETSC_ERR_ARG_SIZ, __FILE__, __LINE__, "MatMult sizes");
+  const PetscInt bs = A->bs;
+  for (PetscInt I = 0; I < A->mb; I++) {
+    for (PetscInt r = 0; r < bs; r++) y->a[I * bs + r] = 0.0;
+    for (PetscInt k = A->i[I]; k < A->i[I + 1]; k++) {
+      const PetscScalar *blk = A->a + (size_t)k * bs * bs;
+      const PetscScalar *xj = x->a + (size_t)A->j[k] * bs;
+      for (PetscInt cc = 0; cc < bs; cc++)
+        for (PetscInt r = 0; r < bs; r++) y->a[I * bs + r] += blk[cc * bs + r] * xj[cc];
+    }
+  }
+  return 0;
+}
+
+PetscErrorCode MatDestroy(Mat *A)
+{
+  if (A && *A) { free(*A); *A = NULL; }
+  return 0;
+}

@@ -12,6 +12,7 @@ extern "C" {
 typedef struct PetscLiteVec_ { PetscInt n; PetscScalar *a; } *Vec;
 typedef struct PetscLiteOpaque_ *Mat;
 typedef struct PetscLiteOpaque_ *SNES;
+typedef int SNESConvergedReason;   /* an enum in PETSc */
 typedef struct PetscLiteOpaque_ *DM;
 typedef struct PetscLiteOpaque_ *PetscSF;
 typedef struct PetscLiteOpaque_ *Tao;
@@ -60,6 +61,19 @@ PetscErrorCode MatSetUp(Mat m);
 PetscErrorCode MatZeroEntries(Mat m);
 PetscErrorCode MatGetSize(Mat m, PetscInt *a, PetscInt *b);
 PetscErrorCode MatCreateSeqDense(MPI_Comm c, PetscInt a, PetscInt b, PetscScalar *d, Mat *m);
+
+/* An array-backed sequential block matrix with PETSc SeqBAIJ's storage:
+   block rows by a CSR pattern (i, j over blocks), each bs x bs block's values
+   column by column (a[k bs^2 + c bs + r] is row r, column c of block k). */
+typedef enum { MAT_FINAL_ASSEMBLY = 0, MAT_FLUSH_ASSEMBLY = 1 } MatAssemblyType;
+PetscErrorCode MatCreateSeqBAIJWithArrays(MPI_Comm c, PetscInt bs, PetscInt m, PetscInt n, PetscInt i[], PetscInt j[],
+                                          PetscScalar a[], Mat *mat);
+PetscErrorCode MatSeqBAIJGetArray(Mat A, PetscScalar **a);
+PetscErrorCode MatSeqBAIJRestoreArray(Mat A, PetscScalar **a);
+PetscErrorCode MatAssemblyBegin(Mat A, MatAssemblyType t);
+PetscErrorCode MatAssemblyEnd(Mat A, MatAssemblyType t);
+PetscErrorCode MatMult(Mat A, Vec x, Vec y);
+PetscErrorCode MatDestroy(Mat *A);
 
 #ifdef __cplusplus
 }

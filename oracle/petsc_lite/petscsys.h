@@ -55,6 +55,7 @@ typedef void *PetscOptions;
 #define PETSC_ERR_SUP             56
 #define PETSC_ERR_ORDER           58
 #define PETSC_ERR_ARG_WRONG       62
+#define PETSC_ERR_ARG_SIZ         60
 #define PETSC_ERR_ARG_OUTOFRANGE  63
 #define PETSC_ERR_FILE_OPEN       65
 #define PETSC_ERR_FILE_READ       66

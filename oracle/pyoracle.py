@@ -56,6 +56,13 @@ class _Base:
             if rc:
                 raise RuntimeError(f"{self.prefix}_{name} failed with code {rc}")
 
+    def _select_load(self, w):
+        """Pressure kind (follower / dead load) and activation kind (fibre /
+        isotropic) of the workload for the next setup."""
+        f = self._fn("set_load_options")
+        f.argtypes = [_c_int, _c_int]
+        f(int(getattr(w, "dead_load", 0)), int(getattr(w, "iso_act", 0)))
+
     def setup(self, mesh, w, mu: float, bulk: float, h0: float, gamma: float = 1.0, clamp: bool = True):
         from_mesh = dict(
             tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),
@@ -67,6 +74,7 @@ class _Base:
         )
         self._keep = from_mesh
         self._select_basis(getattr(w, "basis", 0), getattr(w, "tnormal", 0))
+        self._select_load(w)
         f = self._fn("setup")
         f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp,
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
@@ -174,6 +182,7 @@ class Oracle(_Base):
                     gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64))
         self._keep = keep
         self._select_basis(getattr(w, "basis", 0), getattr(w, "tnormal", 0))
+        self._select_load(w)
         f = self.lib.oracle_setup_given_topology
         f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
@@ -190,6 +199,13 @@ class Oracle(_Base):
 
     def set_threads(self, n: int):
         self.lib.oracle_set_threads(int(n))
+
+    def set_fast_topology(self, on: bool = True):
+        """setup() then builds GlobalGhostInit / IrrVer / Patch with
+        corner-incident scans (O(N), the same tables as the reference's full
+        scans)."""
+        self.lib.oracle_set_fast_topology(int(bool(on)))
+        return self
 
     def topology(self) -> Topology:
         ne, ng, nv = self.n_elmt, self.n_ghosts, self.n_v
@@ -401,12 +417,40 @@ class Oracle(_Base):
 class RefOracle(_Base):
     prefix = "ref"
 
-    def __init__(self):
+    def __init__(self, dyn: bool = False):
+        """dyn: load oracle/_ref/libbiofem_ref_dyn.so, the build that also holds
+        the reference's main.c (FDynamic, xAccVel) and material.c."""
         from . import build_ref  # type: ignore
-        path = build_ref.build()
+        path = build_ref.build_dyn() if dyn else build_ref.build()
         if path is None:
             raise FileNotFoundError("reference sources are not present on this host")
         self.lib = ctypes.CDLL(str(path))
+
+    # ---- the reference's own dynamic term (main.c FDynamic / xAccVel) ----
+    def set_dynamics(self, dt, rho=0.0, newmark_gamma=0.5, dampfactor=0.0, timeinteg=0, damping=0):
+        f = self.lib.ref_set_dynamics
+        f.argtypes = [_c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_int]
+        f(float(dt), float(rho), float(newmark_gamma), float(dampfactor), int(timeinteg), int(damping))
+
+    def fdynamic(self, x, xn, xnm1, xd, xdd, dmplex: bool = True):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, xn, xnm1, xd, xdd)]
+        out = np.zeros(self.n_dof)
+        f = self.lib.ref_fdynamic
+        f.argtypes = [_vp] * 6 + [_c_int]
+        rc = f(*[_p(a) for a in arrs], _p(out), int(dmplex))
+        if rc:
+            raise RuntimeError(f"ref_fdynamic failed with code {rc}")
+        return out
+
+    def xaccvel(self, x, xn, xd, xdd, dmplex: bool = True):
+        x, xn = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, xn))
+        xd, xdd = (np.array(a, dtype=np.float64) for a in (xd, xdd))
+        f = self.lib.ref_xaccvel
+        f.argtypes = [_vp] * 4 + [_c_int]
+        rc = f(_p(x), _p(xn), _p(xd), _p(xdd), int(dmplex))
+        if rc:
+            raise RuntimeError(f"ref_xaccvel failed with code {rc}")
+        return xd, xdd
 
     def topology(self) -> Topology:
         ne, ng, nv = self.n_elmt, self.n_ghosts, self.n_v

@@ -8,6 +8,11 @@
  * reference sources; tests use it to pin the restated oracle
  * (oracle/oracle.cpp) and to generate the committed golden fixtures.
  *
+ * Built a second time with src/main.c (FDynamic, xAccVel) and src/material.c
+ * (Mass, Damp) into oracle/_ref/libbiofem_ref_dyn.so (-DREF_DRIVER_WITH_MAIN,
+ * main renamed, the externals main.c references but the dynamic term never
+ * calls resolved by abort stubs that oracle/build_ref.py generates).
+ *
  * What is restated here (everything else is the reference's own code):
  *   - main.c globals the compiled files read (main.c:22-77), with the values
  *     the hot path needs (-inverse 0, -bending 0, -curvature 6, tisteps 1);
@@ -18,13 +23,18 @@
  *     GlobalGhostInit -> IrrVer -> Patch, then geom0, then Init()'s
  *     AreaNormal/GlobalGhost/dA0 (main.c:1439-1452);
  *   - FormFunctionFEM's serial sequence (main.c:757-1032) with FExternal
- *     replaced by the follower SurfaceNormalPressure(P) (external.c:589) and
- *     the clamp EdgeDirectionalFix(0, d) for d = 0,1,2 (external.c:1706).
+ *     replaced by the follower SurfaceNormalPressure(P) (external.c:589), or
+ *     the dead-load SurfaceConstNormalPressure(P) (external.c:699), and the
+ *     clamp EdgeDirectionalFix(0, d) for d = 0,1,2 (external.c:1706).
  */
 #include "variables.h"
 #include "active_strain.h"
 
 /* ---- main.c globals read by the compiled reference files ---- */
+#ifndef REF_DRIVER_WITH_MAIN
+/* Built without src/main.c: its globals are restated here.  Built with it
+   (oracle/_ref/libbiofem_ref_dyn.so, for FDynamic and xAccVel) main.c defines
+   them, and ref_setup assigns the values the hot path needs. */
 PetscReal E = 0.0, mu = 0.0, rho = 0.0, h0 = 0.0, dt = 0.0;
 PetscReal char_length_x = 1.0, char_length_y = 1.0, char_length_z = 1.0;
 PetscInt  dof = 3, contact = 0, ConstitutiveLawNonLinear = 0, curvature = 6;
@@ -33,9 +43,15 @@ PetscInt  legacy_restart_in = 0, lv_geom_process = 0, muscle_activation = 1;
 PetscInt  manufactured_fexternal_export = 0, prescribed_force_field = 0;
 PetscInt  ressmooth = 0, par_jac = 0, Adam = 0;
 PetscInt  n_Fung_Coeffs = 9, n_lin_model_coeffs = 2;
-PetscReal manufactured_gamma0 = 0.0, manufactured_T = 1.0;
 char      in_dir[256] = "./";
 char      out_dir[256] = "./";
+#else
+extern PetscReal E, mu, rho, h0, dt, dampfactor, newmark_gamma;
+extern PetscInt  dof, contact, ConstitutiveLawNonLinear, curvature, ti, tistart, tisteps, manufactured, inverse;
+extern PetscInt  legacy_restart_in, lv_geom_process, muscle_activation, manufactured_fexternal_export;
+extern PetscInt  prescribed_force_field, ressmooth, par_jac, Adam, damping, timeinteg, bending;
+#endif
+PetscReal manufactured_gamma0 = 0.0, manufactured_T = 1.0;
 
 /* ---- reference functions defined in the compiled files ---- */
 extern PetscErrorCode Create(IBMNodes *ibm, FE *fem, PetscInt ibi);
@@ -46,16 +62,19 @@ extern PetscErrorCode GlobalGhost(IBMNodes *ibm);
 extern PetscErrorCode IrrVer(IBMNodes *ibm);
 extern PetscErrorCode Patch(IBMNodes *ibm);
 extern PetscErrorCode SurfaceNormalPressure(PetscReal P, FE *fem);
+extern PetscErrorCode SurfaceConstNormalPressure(PetscReal P, FE *fem);
 extern PetscErrorCode EdgeDirectionalFix(PetscInt edge_n, PetscInt dir, FE *fem, Vec R);
 
 /* ---- never-called externals of the legacy parts of the compiled files ---- */
 #define REF_ABORT_STUB(name) \
   PetscErrorCode name() { fprintf(stderr, "oracle/_ref: %s is off the hot path\n", #name); abort(); }
+#ifndef REF_DRIVER_WITH_MAIN
 REF_ABORT_STUB(BendingNonLinear)
 REF_ABORT_STUB(CalcCurvStressStrainxyz)
 REF_ABORT_STUB(MembraneNonLinear)
 REF_ABORT_STUB(StressLinear)
 REF_ABORT_STUB(StressManufactured)
+#endif
 REF_ABORT_STUB(GhostLoc)
 REF_ABORT_STUB(GetManufacturedActiveStrainOptions)
 REF_ABORT_STUB(ManufacturedKinematicsAndFExternalSetInitial)
@@ -126,6 +145,18 @@ static IBMNodes g_ibm;
 static int      g_ready = 0;
 static double   g_pressure = 0.0;
 static int      g_clamp = 1;
+static int      g_dead_load = 0;   /* SurfaceConstNormalPressure instead of SurfaceNormalPressure */
+static int      g_cart_fib_act = 1;
+
+/* Options of the next ref_setup: dead_load 1 applies the pressure with
+   SurfaceConstNormalPressure (external.c:699), iso_act 1 sets -cart_fib_act 0
+   (the isotropic active gradient, active_strain.c:1238-1255). */
+int ref_set_load_options(int dead_load, int iso_act)
+{
+  g_dead_load = dead_load != 0;
+  g_cart_fib_act = iso_act ? 0 : 1;
+  return 0;
+}
 
 static void RefFreeAll_(void)
 {
@@ -166,12 +197,16 @@ int ref_setup(int n_v, int n_elmt, const int *tri, const double *xyz0,
   PetscLiteClearOptions();
   RefSetOptionInt_("-num_gaussian_quad_points", n_qp);
   RefSetOptionInt_("-C33_subitr_nums", c33_iters);
-  RefSetOptionInt_("-cart_fib_act", 1);
+  RefSetOptionInt_("-cart_fib_act", g_cart_fib_act);
   RefSetOptionReal_("-muscle_act_gamma", gamma_in);
   RefSetOptionInt_("-gamma_ramp_type", 0);
   RefSetOptionReal_("-bulk_modulus", bulk_in);
   mu = mu_in;
   h0 = h0_in;
+  /* the hot path's switches (main.c defaults differ: -inverse 1, no muscle activation) */
+  contact = 0; ConstitutiveLawNonLinear = 0; curvature = 6; manufactured = 0; inverse = 0;
+  lv_geom_process = 0; muscle_activation = 1; ressmooth = 0; par_jac = 0; Adam = 0;
+  ti = 0; tistart = 0; tisteps = 1;
   g_pressure = pressure;
   g_clamp = clamp_edge0;
 
@@ -226,6 +261,10 @@ int ref_setup(int n_v, int n_elmt, const int *tri, const double *xyz0,
   return 0;
 }
 
+/* The body ref_setup built (for tests that hand the reference's FE to code
+   written against it, e.g. the PETSc adapter's FE -> mesh description). */
+FE *ref_fem(void) { return g_ready ? &g_fem : NULL; }
+
 int ref_sizes(int *n_ghosts, int *n_dof)
 {
   if (!g_ready) return PETSC_ERR_ORDER;
@@ -278,7 +317,10 @@ int ref_residual(const double *x, double *R, double *Fint_out, double *Fext_out)
   PetscCall(FInternalAct(fem));
   /* FExternal (bcs.c:96) wires no load on this path; the follower pressure
      helper is called in its place. */
-  if (g_pressure != 0.0) PetscCall(SurfaceNormalPressure(g_pressure, fem));
+  if (g_pressure != 0.0) {
+    if (g_dead_load) PetscCall(SurfaceConstNormalPressure(g_pressure, fem));
+    else PetscCall(SurfaceNormalPressure(g_pressure, fem));
+  }
   PetscCall(VecWAXPY(Rv, -1., fem->Fext, fem->Fint));
   PetscCall(VecAXPY(Rv, 1., fem->Fdyn));
   if (g_clamp) {
@@ -403,3 +445,71 @@ int ref_thickness(const char *dir, int ti_out, int ibi, const double *x, double 
   if (dir) PetscCall(Write3DShellVTK(fem, ti_out, ibi, dir));
   return 0;
 }
+
+#ifdef REF_DRIVER_WITH_MAIN
+/* ---- the dynamic term: main.c's own FDynamic and xAccVel ---- */
+extern PetscErrorCode FDynamic(FE *fem);
+extern PetscErrorCode xAccVel(FE *fem);
+
+/* The -dt, -rho, -newmark_gamma, -dampfactor, -timeinteg and -damping
+   options (main.c globals). */
+int ref_set_dynamics(double dt_in, double rho_in, double newmark_gamma_in, double dampfactor_in, int timeinteg_in,
+                     int damping_in)
+{
+  dt = dt_in; rho = rho_in; newmark_gamma = newmark_gamma_in; dampfactor = dampfactor_in;
+  timeinteg = timeinteg_in; damping = damping_in;
+  return 0;
+}
+
+static void RefSetVec_(Vec v, const double *a, PetscInt n) { for (PetscInt i = 0; i < n; i++) v->a[i] = a[i]; }
+
+/* FDynamic (main.c:1157-1364) at the state (x, xn, xnm1, xd, xdd), each
+   3 (n_v + n_ghosts): x goes to ibm->x_bp with the ghost positions by
+   GlobalGhost, as FormFunctionFEM does before FDynamic (main.c:767-813);
+   Fdyn receives fem->Fdyn.  dmplex = 1 runs it with the driver's DMPlex
+   context (the path an active-strain run takes, main.c:326-331: real
+   triangles, VecSetValues), 0 the serial path (every triangle, ghost and
+   bridging ones included). */
+int ref_fdynamic(const double *x, const double *xn, const double *xnm1, const double *xd, const double *xdd,
+                 double *Fdyn, int dmplex)
+{
+  if (!g_ready) return PETSC_ERR_ORDER;
+  FE *fem = &g_fem;
+  IBMNodes *ibm = &g_ibm;
+  const PetscInt ndof = dof * (ibm->n_v + ibm->n_ghosts);
+  for (PetscInt v = 0; v < ibm->n_v; v++) {
+    ibm->x_bp[v] = x[v * dof]; ibm->y_bp[v] = x[v * dof + 1]; ibm->z_bp[v] = x[v * dof + 2];
+  }
+  PetscCall(AreaNormal(ibm));
+  if (ibm->n_ghosts > 0) PetscCall(GlobalGhost(ibm));
+  RefSetVec_(fem->x, x, ndof); RefSetVec_(fem->xn, xn, ndof); RefSetVec_(fem->xnm1, xnm1, ndof);
+  RefSetVec_(fem->xd, xd, ndof); RefSetVec_(fem->xdd, xdd, ndof);
+  PetscCall(VecSet(fem->Fdyn, 0.0));
+  const PetscBool init = fem->geom_ctx.initialized;
+  fem->geom_ctx.initialized = dmplex ? PETSC_TRUE : PETSC_FALSE;
+  PetscErrorCode rc = FDynamic(fem);
+  fem->geom_ctx.initialized = init;
+  if (rc) return rc;
+  for (PetscInt i = 0; i < ndof; i++) Fdyn[i] = fem->Fdyn->a[i];
+  return 0;
+}
+
+/* xAccVel (main.c:1367-1412) from the converged x and the state (xn, xd,
+   xdd); xd and xdd are updated in place.  dmplex as for ref_fdynamic
+   (1: the n_v real nodes, 0: n_v + n_ghosts). */
+int ref_xaccvel(const double *x, const double *xn, double *xd, double *xdd, int dmplex)
+{
+  if (!g_ready) return PETSC_ERR_ORDER;
+  FE *fem = &g_fem;
+  const PetscInt ndof = dof * (g_ibm.n_v + g_ibm.n_ghosts);
+  RefSetVec_(fem->x, x, ndof); RefSetVec_(fem->xn, xn, ndof); RefSetVec_(fem->xd, xd, ndof);
+  RefSetVec_(fem->xdd, xdd, ndof);
+  const PetscBool init = fem->geom_ctx.initialized;
+  fem->geom_ctx.initialized = dmplex ? PETSC_TRUE : PETSC_FALSE;
+  PetscErrorCode rc = xAccVel(fem);
+  fem->geom_ctx.initialized = init;
+  if (rc) return rc;
+  for (PetscInt i = 0; i < ndof; i++) { xd[i] = fem->xd->a[i]; xdd[i] = fem->xdd->a[i]; }
+  return 0;
+}
+#endif

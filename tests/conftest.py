@@ -29,9 +29,10 @@ def golden_case(path):
     from biofem import configs
     d = np.load(path)
     meta = json.loads(str(d["meta"]))
+    opt = {k: meta[k] for k in ("dead_load", "iso_act") if k in meta}
     if meta.get("kind") == "lv":
         keys = ("name", "freq", "index", "n_qp", "c33_iters", "pressure", "lambda_a", "nflip", "jitter")
-        return configs.LVWorkload(**{k: meta[k] for k in keys}), meta, d
+        return configs.LVWorkload(**{k: meta[k] for k in keys}, **opt), meta, d
     keys = ("name", "nx", "ny", "n_qp", "c33_iters", "pressure", "z_sigma", "activation",
             "lambda_a", "disp_rel", "index")
-    return configs.Workload(**{k: meta[k] for k in keys}), meta, d
+    return configs.Workload(**{k: meta[k] for k in keys}, **opt), meta, d

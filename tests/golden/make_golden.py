@@ -9,13 +9,15 @@ Each fixture holds the workload parameters, the reference topology tables
 (GlobalGhostInit/IrrVer/Patch output), the SNES iterate x and the reference
 residual R, Fint and Fext for that x, plus per-element stress / C33 / geometry
 for a few sample elements.  Larger meshes store checksums and a strided
-sample of R instead of full arrays to keep fixtures small.
+sample of R instead of full arrays to keep fixtures small (C2 with --c2,
+the full-size ellipsoid C4 with --c4).
 """
 from __future__ import annotations
 
 import hashlib
 import json
 import sys
+from dataclasses import replace
 from pathlib import Path
 
 import numpy as np
@@ -35,13 +37,14 @@ def sha(a: np.ndarray) -> str:
 
 
 def workload_dict(w) -> dict:
+    extra = dict(dead_load=w.dead_load, iso_act=w.iso_act) if (w.dead_load or w.iso_act) else {}
     if isinstance(w, configs.LVWorkload):
         return dict(kind="lv", name=w.name, freq=w.freq, index=w.index, n_qp=w.n_qp, c33_iters=w.c33_iters,
                     pressure=w.pressure, lambda_a=w.lambda_a, nflip=w.nflip, jitter=w.jitter,
-                    mu=configs.MU, bulk=configs.BULK, h0=configs.H0)
+                    mu=configs.MU, bulk=configs.BULK, h0=configs.H0, **extra)
     return dict(name=w.name, nx=w.nx, ny=w.ny, n_qp=w.n_qp, c33_iters=w.c33_iters, pressure=w.pressure,
                 z_sigma=w.z_sigma, activation=w.activation, lambda_a=w.lambda_a, disp_rel=w.disp_rel,
-                index=w.index, mu=configs.MU, bulk=configs.BULK, h0=configs.H0)
+                index=w.index, mu=configs.MU, bulk=configs.BULK, h0=configs.H0, **extra)
 
 
 def make(w, full: bool, sample_elems=(0, 1, 5, 17)):
@@ -88,6 +91,10 @@ CASES_FULL = [
     # truncated ellipsoid caps: interior valence 5/7 and jagged-rim irregular patches
     configs.LVWorkload("lv_f3", 3, index=40),
     configs.LVWorkload("lv_f4_q5", 4, index=41, n_qp=5, c33_iters=2, pressure=5e-4),
+    # the dead-load pressure (SurfaceConstNormalPressure) and the isotropic active gradient (-cart_fib_act 0)
+    replace(configs.small(8, 7, index=14, pressure=2e-3, dead_load=1), name="flat_8x7_dead_load"),
+    replace(configs.small(9, 6, index=15, activation="random", iso_act=1), name="flat_9x6_isotropic"),
+    configs.LVWorkload("lv_f3_iso_dead", 3, index=42, iso_act=1, dead_load=1),
 ]
 
 if __name__ == "__main__":
@@ -97,3 +104,5 @@ if __name__ == "__main__":
             make(w, full=True)
     if "--c2" in sys.argv:
         make(configs.C2, full=False)
+    if "--c4" in sys.argv:   # the reference's O(N^2) Patch() on 200k triangles: tens of minutes
+        make(configs.C4, full=False)

@@ -90,3 +90,45 @@ def test_oracle_dense_jacobian_consistent_with_jvp(oracle_lib):
     v = np.random.default_rng(4).standard_normal(x.size)
     _, Jv = o.jvp(x, v)
     np.testing.assert_allclose(J @ v, Jv, rtol=1e-12, atol=1e-14 * np.abs(Jv).max())
+
+
+@pytest.mark.parametrize("path", FULL, ids=lambda p: p.stem)
+def test_oracle_fast_topology_equals_the_reference_tables(path):
+    """The oracle's corner-incident scans (O(N)) give the reference's tables
+    bit for bit on every golden mesh, and the same residual."""
+    from oracle.pyoracle import Oracle
+    w, meta, d = load_case(path)
+    m = w.build_mesh()
+    o = Oracle().set_fast_topology(True)
+    try:
+        o.setup(m, w, meta["mu"], meta["bulk"], meta["h0"])
+        t = o.topology()
+        for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0", "ghost_nv3"):
+            if k in d:
+                assert np.array_equal(getattr(t, k), d[k]), k
+        assert np.array_equal(o.residual(d["x"]), d["R"])
+    finally:
+        o.set_fast_topology(False)
+
+
+@pytest.mark.parametrize("name", ["C2_flat_256x192", "C4_lv_ellipsoid"])
+def test_oracle_fast_topology_matches_reference_checksum(name):
+    """C2 (98,304 triangles) and C4 (200,614 triangles, valence 5/7) through
+    the oracle's O(N) scans: the SHA-256 of the reference's own
+    Patch()/IrrVer() tables (tests/golden/C2_flat_256x192.npz,
+    C4_lv_ellipsoid.npz, made by the reference build's O(N^2) searches)."""
+    import hashlib
+    from oracle.pyoracle import Oracle
+    d = np.load(GOLDEN / f"{name}.npz")
+    meta = json.loads(str(d["meta"]))
+    w = configs.ALL[name]
+    m = w.build_mesh()
+    o = Oracle().set_fast_topology(True)
+    try:
+        o.setup(m, w, configs.MU, configs.BULK, configs.H0)
+        t = o.topology()
+    finally:
+        o.set_fast_topology(False)
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a, dtype=np.int32).tobytes()).hexdigest()
+    for k in ("patch", "ire", "val", "irv"):
+        assert sha(getattr(t, k)) == meta[f"sha_{k}"], k

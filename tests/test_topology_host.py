@@ -43,14 +43,16 @@ def test_host_topology_equals_oracle_ellipsoid(freq, oracle_lib):
     sh.close()
 
 
-def test_host_topology_matches_reference_checksum_C2():
-    """C2 (98,304 triangles): the reference's O(N^2) Patch() output is stored
-    as SHA-256 checksums in tests/golden/C2_flat_256x192.npz."""
+@pytest.mark.parametrize("name", ["C2_flat_256x192", "C4_lv_ellipsoid"])
+def test_host_topology_matches_reference_checksum(name):
+    """C2 (98,304 triangles) and C4 (200,614 triangles, valence-5/7 vertices):
+    the reference's O(N^2) GlobalGhostInit/IrrVer/Patch() output is stored as
+    SHA-256 checksums in tests/golden/{C2_flat_256x192,C4_lv_ellipsoid}.npz."""
     import hashlib
-    path = GOLDEN / "C2_flat_256x192.npz"
+    path = GOLDEN / f"{name}.npz"
     d = np.load(path)
     meta = json.loads(str(d["meta"]))
-    w = configs.C2
+    w = configs.ALL[name]
     m = w.build_mesh()
     sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
     t = sh.topology()
