@@ -38,6 +38,8 @@ class Workload:
     z_smooth: bool = False           # smooth imperfection instead of per-node noise
     basis: int = 0                   # 0 reference four-decimal basis tables, 1 exact (extension)
     tnormal: int = 0                 # 1: thickness metric from n,alpha only (extension)
+    dead_load: int = 0               # 1: dead-load pressure (SurfaceConstNormalPressure) instead of follower
+    iso_act: int = 0                 # 1: isotropic active gradient (-cart_fib_act 0) instead of along the fibre
 
     @property
     def seed(self) -> int:
@@ -93,6 +95,8 @@ class LVWorkload:
     jitter: float = 0.1
     basis: int = 0
     tnormal: int = 0
+    dead_load: int = 0
+    iso_act: int = 0
 
     @property
     def seed(self) -> int:
