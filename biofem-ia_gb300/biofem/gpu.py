@@ -31,6 +31,8 @@ BIOFEM_PC_AMG = 0
 BIOFEM_PC_BJACOBI = 1
 BIOFEM_FP64 = 0
 BIOFEM_FP32_BULK = 1
+BIOFEM_BLOCK_ROW_MAJOR = 0
+BIOFEM_BLOCK_COL_MAJOR = 1
 BIOFEM_CKPT_VERTEX_ORDER = 0
 BIOFEM_CKPT_VEC = 1
 
@@ -54,7 +56,8 @@ class Params(ctypes.Structure):
     _fields_ = [("n_qp", ctypes.c_int32), ("c33_subitr_nums", ctypes.c_int32), ("mu", ctypes.c_double),
                 ("bulk_modulus", ctypes.c_double), ("h0", ctypes.c_double), ("gamma", ctypes.c_double),
                 ("pressure", ctypes.c_double), ("clamp_edge", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("basis", ctypes.c_int32), ("thickness_normal", ctypes.c_int32)]
+                ("basis", ctypes.c_int32), ("thickness_normal", ctypes.c_int32), ("block_layout", ctypes.c_int32),
+                ("pressure_kind", ctypes.c_int32), ("activation_kind", ctypes.c_int32)]
 
 
 class MeshInfo(ctypes.Structure):
@@ -191,7 +194,8 @@ class GpuShell:
     """One mesh resident on the GPU (or, with host_only=True, only its host tables)."""
 
     def __init__(self, mesh, workload, mu: float, bulk: float, h0: float, gamma: float = 1.0,
-                 clamp_edge: int = 0, precision: int = BIOFEM_FP64, host_only: bool = False):
+                 clamp_edge: int = 0, precision: int = BIOFEM_FP64, host_only: bool = False,
+                 block_layout: int = BIOFEM_BLOCK_ROW_MAJOR):
         self.lib = load_library()
         self._arrays = dict(
             tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),
@@ -207,7 +211,8 @@ class GpuShell:
                              a["fib"].ctypes.data_as(_f64p), a["gs"].ctypes.data_as(_f64p))
         self.params = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure,
                              clamp_edge, precision, getattr(workload, "basis", BIOFEM_BASIS_REFERENCE),
-                             getattr(workload, "tnormal", 0))
+                             getattr(workload, "tnormal", 0), block_layout, getattr(workload, "dead_load", 0),
+                             getattr(workload, "iso_act", 0))
         self.host_only = host_only
         h = ctypes.c_void_p()
         fn = self.lib.BuildHostMesh if host_only else self.lib.PrepareGpuMesh
@@ -429,7 +434,8 @@ class Serve:
     def submit(self, mesh, workload, mu, bulk, h0, x0, gamma=1.0, clamp_edge=0, precision=BIOFEM_FP64, **newton):
         d, keep = mesh_desc(mesh)
         prm = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure, clamp_edge, precision,
-                     getattr(workload, "basis", BIOFEM_BASIS_REFERENCE), getattr(workload, "tnormal", 0))
+                     getattr(workload, "basis", BIOFEM_BASIS_REFERENCE), getattr(workload, "tnormal", 0), 0,
+                     getattr(workload, "dead_load", 0), getattr(workload, "iso_act", 0))
         o = NewtonOptions()
         self.lib.BiofemNewtonDefaults(ctypes.byref(o))
         for k, v in newton.items():

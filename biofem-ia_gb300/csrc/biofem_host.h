@@ -21,6 +21,9 @@ constexpr int kRefPerElem = 4;    /* gamma, gamma', c1, pref0 */
 constexpr int kGeomShape = 18;    /* primal element geometry stored for the FP64 tangent (elem_geom_store) */
 constexpr int kGeomPrimal = kGeomShape + 17;   /* + the primal resultants (elem_res_store) */
 constexpr int kNumTables = 11;    /* 0 = regular 12-node patch, v = 3..10 irregular */
+constexpr int kDeStride = 240;    /* per-element tangent block: D = df/dy (15 x 15, row-major), */
+constexpr int kDePres = 225;      /* then the three follower-pressure corner vectors (9) */
+constexpr int kMaxRowBlocks = 1023;   /* tangent blocks per row the row assembly handles (10-bit slot targets) */
 
 /* Topology in IBMNodes layout (see topology.cpp). */
 struct HostTopo {
@@ -37,6 +40,8 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err);
 struct KParams {
   int ne, nt, nv, ng, nq, iters;
   int tnormal;               /* thickness metric from the tangential part of a3,alpha */
+  int pres_dead;             /* pressure with the reference normal and area (no load stiffness) */
+  int iso_act;               /* isotropic active gradient (-cart_fib_act 0) */
   double mu, K, hhalf;
   double theta[kMaxQp], w[kMaxQp];
   double pressure;
@@ -58,31 +63,31 @@ struct DevMesh {
   const int *ecorner;        /* ne: patch slots of nv1, nv2, nv3 (5 bits each) */
   const double *eref;        /* (kRefPerQp*nq + kRefPerElem) * ne, SoA */
   const float *erefF;        /* the same in FP32 (FP32-bulk handles only) */
+  const void *erefFF;        /* the same as float-float pairs (FP32-bulk handles only; ff.cuh FF) */
+  const void *ntabFF;        /* basis tables and their row sums as float-float pairs (FP32-bulk handles) */
   const double *ntab;        /* kNumTables * 5 * 16 basis-derivative tables */
   const float *ntabF;        /* the same in FP32, followed by the kNumTables*5 row sums */
   const int *etri;           /* 3*ne triangle corners (pressure) */
   const int *ghost3;         /* 3*ng (nv1, nv2, nv3) */
-  const long long *kofs;     /* ne: first Ke block of the element */
   const double *X;           /* 3*nt reference positions (Vec layout) */
   const unsigned char *rowkind; /* nt: 0 free real row, 1 clamped row, 2 ghost row */
   /* residual gather lists */
   const int *rptr, *ridx;    /* nt+1, into fb scratch (slot*3*ne + e) */
+  const int *rcon;           /* the same contributions as e | slot << 27 (row assembly of the tangent) */
   const int *pptr, *pidx;    /* nt+1, elements whose corner is the node */
-  /* tangent pattern + gather lists */
-  const int *rowptr, *colind, *blkrow;   /* BSR pattern; block -> row */
-  const long long *cptr;     /* nnzb+1 */
-  const int *cidx;           /* contribution: Ke block id, negative = subtract (-(id+1)) */
-  const int *gperm;          /* nnzb: the gathers' block order (each row's blocks by decreasing count) */
+  /* tangent pattern */
+  const int *rowptr, *colind;   /* BSR pattern, columns sorted per row */
   long long nnzb;
+  int maxblk;                /* most blocks in one row */
   /* work arrays */
   double *pos;               /* 4*nt padded positions */
   double *fb;                /* 48*ne element forces */
   double *fp;                /* 3*ne element pressure forces */
-  double *ke;                /* 9*total blocks element matrices (FP64 handles) */
-  float *keF;                /* 9*total blocks element matrices (FP32-bulk handles) */
+  double *De;                /* kDeStride*ne element tangent blocks df/dy (FP64 handles) */
+  float *DeF;                /* the same in FP32 (FP32-bulk handles) */
   int *status;               /* device error flag */
-  double *dA0;               /* n_elmt + 2 n_ghosts flat reference areas of every triangle (AreaNormal at Init) */
-  int *dptr, *didx;          /* per node, the triangles with that corner (ghost and bridging ones included), in triangle order */
+  double *dA0;               /* n_elmt flat reference areas of the real triangles (AreaNormal at Init) */
+  int *dptr, *didx;          /* per node, the real triangles with that corner, in triangle order */
   double *xn, *xnm1, *xd, *xdd;   /* 3*nt dynamic state (previous positions, velocity, acceleration) */
   double *dyn_diag;          /* nt: d Fdyn / d x on the diagonal of each free row */
   double *gmq;               /* FP64 handles: 6 nq x ne thickness-point metrics, k_elem_residual -> k_elem_tangent */
@@ -99,10 +104,13 @@ int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream);
 int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, double *R, void *stream,
                        double *parts = nullptr);
 int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double *th, void *stream);
-int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream, bool k_on_host = false);
+int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, bool colmajor, void *stream);
+int row_assemble_configure(int maxblk, bool f32);   /* dynamic shared memory of the row assembly */
+size_t row_assemble_smem(int maxblk, bool f32);
 int launch_scale(const DevMesh &m, const KParams &p, double *R, void *stream);
 int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);
-int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream, bool k_on_host = false);
+int launch_elem_residual_ff(const DevMesh &m, const KParams &p, void *stream);
+int launch_to_ff(const double *a, void *b, long long n, void *stream);
 int launch_to_float(const double *a, float *b, long long n, void *stream);
 int launch_dyn_diag(const DevMesh &m, const KParams &p, void *stream);
 int launch_dyn_update(const DevMesh &m, const KParams &p, const double *x, void *stream);
@@ -114,6 +122,7 @@ SolverWork *solver_create(int n, int nb, int m, void *stream, int *rc);
 void solver_destroy(SolverWork *w);
 double *solver_xbuf(SolverWork *w);
 int solver_m(const SolverWork *w);
+long long solver_device_bytes(const SolverWork *w);
 typedef int (*ResidualFn)(void *ctx, const double *x, double *R, void *stream);
 typedef int (*JacobianFn)(void *ctx, const double *x, double *R, void *K, void *stream);
 struct AmgHier;

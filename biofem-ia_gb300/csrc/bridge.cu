@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "amg.h"
+#include "ff.cuh"
 #include "biofem_host.h"
 
 namespace biofem {
@@ -150,7 +151,7 @@ struct BiofemGpuMesh_ {
   std::vector<double> dA0;
   std::vector<int> rowptr, colind;
   long long nnzb = 0, ncontrib = 0;
-  int n_irregular = 0;
+  int n_irregular = 0, maxblk = 1;
   size_t bytes = 0;
   std::vector<void *> allocs;
   DevMesh dm{};
@@ -162,6 +163,7 @@ struct BiofemGpuMesh_ {
   std::vector<unsigned char> rowkind;       /* host copy: 0 free, 1 clamped, 2 ghost */
   cudaStream_t st = nullptr;                /* stream of the host-array calls and of setup/teardown */
   KernelTimer timer;
+  int device = -1;                          /* the device the handle's arrays live on */
 };
 
 static std::set<BiofemGpuMesh *> g_meshes;
@@ -172,10 +174,11 @@ namespace biofem {
 int noalloc_fail(int code, const std::string &msg) { return fail(code, msg); }
 /* the calling thread's last error for the host-only modules (formats.cpp) */
 int host_fail(int code, const std::string &msg) { return fail(code, msg); }
-const DevMesh *mesh_devview(const BiofemGpuMesh *m, const KParams **kp)
+const DevMesh *mesh_devview(const BiofemGpuMesh *m, const KParams **kp, int *device)
 {
   if (!m || !m->dm.patch) return nullptr;
   *kp = &m->kp;
+  *device = m->device;
   return &m->dm;
 }
 } /* namespace biofem */
@@ -237,9 +240,9 @@ static double tri_area0(const HostTopo &T, int t)
 }
 
 static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const BiofemParams &prm,
-                           std::vector<int> &einfo, std::vector<int> &ecorner, std::vector<long long> &kofs, std::vector<unsigned char> &rowkind,
-                           std::vector<int> &rptr, std::vector<int> &ridx, std::vector<int> &pptr, std::vector<int> &pidx,
-                           std::vector<int> &blkrow, std::vector<long long> &cptr, std::vector<int> &cidx)
+                           std::vector<int> &einfo, std::vector<int> &ecorner, std::vector<unsigned char> &rowkind,
+                           std::vector<int> &rptr, std::vector<int> &ridx, std::vector<int> &rcon, std::vector<int> &pptr,
+                           std::vector<int> &pidx)
 {
   std::string err;
   int rc = build_topology(d, m->topo, err);
@@ -248,10 +251,9 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   const int ne = T.n_elmt, nv = T.n_v, ng = T.n_ghosts, nt = nv + ng;
   if (prm.clamp_edge >= d.n_edge) return fail(63, "clamp_edge beyond the number of boundary rings");
 
+  if (ne >= (1 << 27)) return fail(63, "more than 2^27 elements");
   einfo.assign(ne, 0);
   ecorner.assign(ne, 0);
-  kofs.assign(ne, 0);
-  long long acc = 0;
   m->n_irregular = 0;
   for (int e = 0; e < ne; e++) {
     const int nen = T.ire[e] ? T.val[e] + 6 : 12;
@@ -268,10 +270,7 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
       packed |= slot << (5 * k);
     }
     ecorner[e] = packed;
-    kofs[e] = acc;
-    acc += (long long)nen * nen;
   }
-  if (acc >= (1LL << 31)) return fail(63, "element-matrix scratch exceeds the int32 block index");
 
   rowkind.assign(nt, 0);
   for (int g = nv; g < nt; g++) rowkind[g] = 2;
@@ -292,7 +291,8 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   }
   for (int i = 0; i < nt; i++) rptr[i + 1] += rptr[i];
   ridx.assign(rptr[nt], 0);
-  std::vector<int> r_elem(rptr[nt]), r_slot(rptr[nt]);   /* ridx split, for the host loops below */
+  rcon.assign(rptr[nt], 0);
+  std::vector<int> r_elem(rptr[nt]);   /* the contribution's element, for the pattern sweep below */
   {
     std::vector<int> fill(rptr.begin(), rptr.end() - 1);
     for (int e = 0; e < ne; e++) {
@@ -302,8 +302,8 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
         if (node < nv) {
           const int c = fill[node]++;
           ridx[c] = (int)((long long)3 * a * ne + e);
+          rcon[c] = e | (a << 27);
           r_elem[c] = e;
-          r_slot[c] = a;
         }
       }
     }
@@ -329,34 +329,24 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
     return 3;
   };
 
-  /* BSR pattern and element-block -> tangent-block contributions, row by
-     row in one sweep: the row's columns are collected and sorted while the
-     contributions per column are counted, then the same (element, slot)
-     list is walked again, still in cache, to fill the row's contribution
-     lists.  The row's (element, slot) list is in increasing element order
-     and a real node fills one slot of a patch, so each block receives its
-     contributions in element order, then slot b, then ghost parent q.  A
-     column -> block table of the current row makes each lookup O(1). */
+  /* BSR pattern: the columns of row i are the real nodes of every patch
+     holding i, a ghost slot standing for its three parents (the chain rule of
+     x_g = x_nv2 + x_nv1 - x_nv3), sorted; n_contrib counts the (element, row
+     slot, column slot, parent) terms the row assembly adds. */
   m->rowptr.assign(nt + 1, 0);
   m->colind.clear();
-  cptr.assign(1, 0);
-  cidx.clear();
-  std::vector<int> mark(nt, -1), ccount(nt, 0);
-  std::vector<long long> colpos(nt, -1);
-  std::vector<int> cols_acc;
-  std::vector<long long> fill;
   m->colind.reserve((size_t)nt * 40);
-  cptr.reserve((size_t)nt * 40 + 1);
-  cidx.reserve((size_t)rptr[nt] * 14);
+  std::vector<int> mark(nt, -1);
+  std::vector<int> cols_acc;
+  long long ncontrib = 0;
+  int maxblk = 1;
   for (int i = 0; i < nt; i++) {
-    cols_acc.clear();
-    const long long row0 = (long long)m->colind.size();
     if (rowkind[i] != 0) {
       m->colind.push_back(i);
-      cptr.push_back(cptr.back());
       m->rowptr[i + 1] = (int)m->colind.size();
       continue;
     }
+    cols_acc.clear();
     cols_acc.push_back(i);
     mark[i] = i;
     for (int c = rptr[i]; c < rptr[i + 1]; c++) {
@@ -365,45 +355,21 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
       for (int b = 0; b < nen; b++) {
         int cols[3], sg[3];
         const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
-        for (int q = 0; q < k; q++) {
+        ncontrib += k;
+        for (int q = 0; q < k; q++)
           if (mark[cols[q]] != i) { mark[cols[q]] = i; cols_acc.push_back(cols[q]); }
-          ccount[cols[q]]++;
-        }
       }
     }
     std::sort(cols_acc.begin(), cols_acc.end());
-    fill.clear();
-    for (size_t t = 0; t < cols_acc.size(); t++) {
-      const int col = cols_acc[t];
-      m->colind.push_back(col);
-      colpos[col] = row0 + (long long)t;
-      fill.push_back(cptr.back());
-      cptr.push_back(cptr.back() + ccount[col]);
-      ccount[col] = 0;
-    }
-    if (cptr.back() >= (1LL << 31)) return fail(63, "assembly map exceeds int32");
-    cidx.resize(cptr.back());
-    for (int c = rptr[i]; c < rptr[i + 1]; c++) {
-      const int e = r_elem[c], a = r_slot[c];
-      const int nen = einfo[e] & 0xff;
-      const long long blk0 = kofs[e] + (long long)a * nen;
-      for (int b = 0; b < nen; b++) {
-        int cols[3], sg[3];
-        const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
-        const long long blk_id = blk0 + b;
-        for (int q = 0; q < k; q++) {
-          const long long kb = colpos[cols[q]];
-          if (kb < row0) return fail(77, "tangent pattern is missing an element block");
-          cidx[fill[kb - row0]++] = sg[q] > 0 ? (int)blk_id : (int)(-(blk_id + 1));
-        }
-      }
-    }
+    m->colind.insert(m->colind.end(), cols_acc.begin(), cols_acc.end());
+    if (m->colind.size() >= (size_t)1 << 31) return fail(63, "tangent pattern exceeds int32");
+    maxblk = std::max(maxblk, (int)cols_acc.size());
     m->rowptr[i + 1] = (int)m->colind.size();
   }
+  if (maxblk > kMaxRowBlocks) return fail(63, "a tangent row has more blocks than the row assembly handles");
   m->nnzb = (long long)m->colind.size();
-  m->ncontrib = cptr.back();
-  blkrow.assign(m->nnzb, 0);
-  for (int i = 0; i < nt; i++) for (int k = m->rowptr[i]; k < m->rowptr[i + 1]; k++) blkrow[k] = i;
+  m->ncontrib = ncontrib;
+  m->maxblk = maxblk;
   /* dA0 on the host too (GetGpuTopology) */
   m->dA0.assign(ne, 0.0);
   for (int e = 0; e < ne; e++) m->dA0[e] = tri_area0(T, e);
@@ -418,6 +384,12 @@ static int check_params(const BiofemParams &p)
   if (p.precision != BIOFEM_FP64 && p.precision != BIOFEM_FP32_BULK) return fail(62, "unknown precision");
   if (p.basis != BIOFEM_BASIS_REFERENCE && p.basis != BIOFEM_BASIS_EXACT) return fail(62, "unknown basis tables");
   if (p.thickness_normal != 0 && p.thickness_normal != 1) return fail(62, "thickness_normal must be 0 or 1");
+  if (p.block_layout != BIOFEM_BLOCK_ROW_MAJOR && p.block_layout != BIOFEM_BLOCK_COL_MAJOR)
+    return fail(62, "unknown block layout");
+  if (p.pressure_kind != BIOFEM_PRESSURE_FOLLOWER && p.pressure_kind != BIOFEM_PRESSURE_DEAD)
+    return fail(62, "unknown pressure kind");
+  if (p.activation_kind != BIOFEM_ACTIVATION_FIBRE && p.activation_kind != BIOFEM_ACTIVATION_ISOTROPIC)
+    return fail(62, "unknown activation kind");
   return 0;
 }
 
@@ -485,10 +457,9 @@ int BuildHostMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofem
   if (rc) return rc;
   BiofemGpuMesh *m = new BiofemGpuMesh();
   m->prm = *params;
-  std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx, blkrow, cidx;
-  std::vector<long long> kofs, cptr;
+  std::vector<int> einfo, ecorner, rptr, ridx, rcon, pptr, pidx;
   std::vector<unsigned char> rowkind;
-  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, kofs, rowkind, rptr, ridx, pptr, pidx, blkrow, cptr, cidx);
+  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, rowkind, rptr, ridx, rcon, pptr, pidx);
   if (rc) { delete m; return rc; }
   *out = m;
   return 0;
@@ -511,10 +482,10 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   BiofemGpuMesh *m = new BiofemGpuMesh();
   m->prm = *params;
   m->st = stream ? (cudaStream_t)stream : g_stream;
-  std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx, blkrow, cidx;
-  std::vector<long long> kofs, cptr;
+  if (cudaGetDevice(&m->device) != cudaSuccess) { delete m; return fail(76, "cudaGetDevice failed"); }
+  std::vector<int> einfo, ecorner, rptr, ridx, rcon, pptr, pidx;
   std::vector<unsigned char> rowkind;
-  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, kofs, rowkind, rptr, ridx, pptr, pidx, blkrow, cptr, cidx);
+  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, rowkind, rptr, ridx, rcon, pptr, pidx);
   if (rc) { delete m; return rc; }
   m->rowkind = rowkind;
   const HostTopo &T = m->topo;
@@ -523,6 +494,8 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   KParams &kp = m->kp;
   kp.ne = ne; kp.nt = nt; kp.nv = nv; kp.ng = ng; kp.nq = params->n_qp; kp.iters = params->c33_subitr_nums;
   kp.tnormal = params->thickness_normal;
+  kp.pres_dead = params->pressure_kind == BIOFEM_PRESSURE_DEAD;
+  kp.iso_act = params->activation_kind == BIOFEM_ACTIVATION_ISOTROPIC;
   kp.mu = params->mu; kp.K = params->bulk_modulus; kp.hhalf = 0.5 * params->h0;
   kp.pressure = params->pressure; kp.gamma = params->gamma;
   gauss(params->n_qp, kp.theta, kp.w);
@@ -536,32 +509,27 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   std::vector<double> tabs(kNumTables * 80);
   host_tables(tabs.data(), params->basis);
   std::vector<float> tabsF(kNumTables * 85);
-  for (int i = 0; i < kNumTables * 80; i++) tabsF[i] = (float)tabs[i];
+  std::vector<FF> tabsFF(kNumTables * 85);
+  for (int i = 0; i < kNumTables * 80; i++) { tabsF[i] = (float)tabs[i]; tabsFF[i] = FF(tabs[i]); }
   for (int i = 0; i < kNumTables * 5; i++) {
     double acc = 0.0;
     for (int k = 0; k < 16; k++) acc += tabs[i * 16 + k];
     tabsF[kNumTables * 80 + i] = (float)acc;
+    tabsFF[kNumTables * 80 + i] = FF(acc);
   }
   std::vector<double> fib(mesh->n_fib, mesh->n_fib + 3 * (size_t)ne), gsc(mesh->gamma_scale, mesh->gamma_scale + ne);
 
 #define UP(field, vec) do { rc = dupload(m, const_cast<std::remove_const<std::remove_pointer<decltype(dm.field)>::type>::type **>(&dm.field), vec); if (rc) { free_mesh(m); return rc; } } while (0)
-  UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3); UP(kofs, kofs);
-  UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(pptr, pptr); UP(pidx, pidx);
-  /* block order of the gathers: within each row, blocks by decreasing
-     contribution count, so the threads of a warp run loops of nearly one
-     length (in row order a warp's blocks range from the diagonal, with the
-     most contributions, to the far ones; the loop's FP64 adds occupy the
-     pipe for every lane of the warp); writes stay inside the row */
-  std::vector<int> gperm((size_t)m->nnzb);
-  for (int i = 0; i < nt; i++) {
-    const int k0 = m->rowptr[i], k1 = m->rowptr[i + 1];
-    for (int k = k0; k < k1; k++) gperm[k] = k;
-    std::stable_sort(gperm.begin() + k0, gperm.begin() + k1,
-                     [&](int a, int b) { return cptr[a + 1] - cptr[a] > cptr[b + 1] - cptr[b]; });
-  }
-  UP(rowptr, m->rowptr); UP(colind, m->colind); UP(blkrow, blkrow); UP(cptr, cptr); UP(cidx, cidx); UP(gperm, gperm);
+  UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3);
+  UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(rcon, rcon); UP(pptr, pptr); UP(pidx, pidx);
+  UP(rowptr, m->rowptr); UP(colind, m->colind);
 #undef UP
   dm.nnzb = m->nnzb;
+  dm.maxblk = m->maxblk;
+  {
+    cudaError_t ce = (cudaError_t)row_assemble_configure(m->maxblk, params->precision != BIOFEM_FP64);
+    if (ce != cudaSuccess) { free_mesh(m); return fail(76, std::string("row assembly configuration: ") + cudaGetErrorString(ce)); }
+  }
   double *d_fib = nullptr, *d_gsc = nullptr, *d_eref = nullptr;
   const size_t nref = (size_t)(kRefPerQp * kp.nq + kRefPerElem) * ne;
   if ((rc = dupload(m, &d_fib, fib)) || (rc = dupload(m, &d_gsc, gsc)) || (rc = dalloc(m, &d_eref, nref)) ||
@@ -572,11 +540,10 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
     free_mesh(m);
     return rc;
   }
-  const size_t keblocks = (size_t)(kofs.empty() ? 0 : kofs.back() + 256);
   float *d_erefF = nullptr;
   if (params->precision == BIOFEM_FP64) {
     double *dK = nullptr;
-    if ((rc = dalloc(m, &dm.ke, 9 * keblocks)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb)) ||
+    if ((rc = dalloc(m, &dm.De, (size_t)kDeStride * ne)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb)) ||
         (rc = dalloc(m, &dm.gmq, 6 * (size_t)kp.nq * ne)) || (rc = dalloc(m, &dm.gpr, (size_t)kGeomPrimal * ne)) ||
         (rc = dalloc(m, &dm.gtape, (size_t)(6 + 23 * kp.iters) * kp.nq * ne))) {
       free_mesh(m);
@@ -585,8 +552,14 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
     m->d_K = dK;
   } else {
     float *dK = nullptr;
-    if ((rc = dalloc(m, &dm.keF, 9 * keblocks)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb)) ||
-        (rc = dalloc(m, &d_erefF, nref))) { free_mesh(m); return rc; }
+    FF *d_erefFF = nullptr, *d_ntabFF = nullptr;
+    if ((rc = dalloc(m, &dm.DeF, (size_t)kDeStride * ne)) || (rc = dalloc(m, &dK, 9 * (size_t)m->nnzb)) ||
+        (rc = dalloc(m, &d_erefF, nref)) || (rc = dalloc(m, &d_erefFF, nref)) || (rc = dupload(m, &d_ntabFF, tabsFF))) {
+      free_mesh(m);
+      return rc;
+    }
+    dm.erefFF = d_erefFF;
+    dm.ntabFF = d_ntabFF;
     m->d_K = dK;
   }
   dm.eref = d_eref;
@@ -599,7 +572,8 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
     free_mesh(m);
     return fail(76, std::string("reference preparation launch: ") + cudaGetErrorString((cudaError_t)rc));
   }
-  if (d_erefF && (rc = launch_to_float(d_eref, d_erefF, (long long)nref, m->st))) {
+  if (d_erefF && ((rc = launch_to_float(d_eref, d_erefF, (long long)nref, m->st)) ||
+                  (rc = launch_to_ff(d_eref, const_cast<void *>(dm.erefFF), (long long)nref, m->st)))) {
     free_mesh(m);
     return fail(76, std::string("reference conversion launch: ") + cudaGetErrorString((cudaError_t)rc));
   }
@@ -631,7 +605,8 @@ int GetGpuMeshInfo(const BiofemGpuMesh *m, BiofemMeshInfo *info)
   info->n_v = m->topo.n_v; info->n_ghosts = m->topo.n_ghosts; info->n_elmt = m->topo.n_elmt;
   info->n_dof = 3 * (m->topo.n_v + m->topo.n_ghosts);
   info->n_irregular = m->n_irregular;
-  info->nnzb = m->nnzb; info->n_contrib = m->ncontrib; info->device_bytes = (int64_t)m->bytes;
+  info->nnzb = m->nnzb; info->n_contrib = m->ncontrib;
+  info->device_bytes = (int64_t)m->bytes + solver_device_bytes(m->solver) + amg_device_bytes(m->amg);
   info->precision = m->prm.precision;
   return 0;
 }
@@ -674,7 +649,7 @@ int GetGpuLaunchCounts(const BiofemGpuMesh *m, int32_t *res, int32_t *jac)
   if (!m) return fail(85, "null argument");
   if (res) *res = 4;   /* positions, element residual, node gather, scale */
   /* positions, element residual (FP64), element tangent, node gather,
-     block gather, scale */
+     row assembly, scale */
   if (jac) *jac = 6;
   return 0;
 }
@@ -693,6 +668,14 @@ static void timer_collect(BiofemGpuMesh *m)
   t.n = 0;
 }
 
+/* The element residual of the handle's form: FP64 (k_elem_residual) or, for
+   FP32-bulk handles, float-float on the FP32 pipe (k_elem_residual_ff). */
+static int launch_residual_elements(BiofemGpuMesh *m, cudaStream_t st)
+{
+  return m->prm.precision == BIOFEM_FP64 ? launch_elem_residual(m->dm, m->kp, st)
+                                         : launch_elem_residual_ff(m->dm, m->kp, st);
+}
+
 int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *stream)
 {
   if (!m || !d_x || !d_R) return fail(85, "null argument");
@@ -700,7 +683,7 @@ int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void 
   int rc = 0;
   tmark(m, st, 0);
   if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
-  if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
+  if (!rc) { rc = launch_residual_elements(m, st); tmark(m, st, 2); }
   if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 3); }
   if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 4); }
   if (rc) return fail(76, std::string("residual launch: ") + cudaGetErrorString((cudaError_t)rc));
@@ -708,15 +691,19 @@ int RunGpuResidualDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void 
   return 0;
 }
 
-static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream, bool k_on_host);
+static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream, bool colmajor);
 
+/* d_K may also be the device view of a mapped page-locked host buffer: the
+   row assembly writes each row's values once, contiguously */
 int RunGpuResidualJacobianDevice(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream)
 {
-  return residual_jacobian(m, d_x, d_R, d_K, stream, false);
+  if (!m) return fail(85, "null argument");
+  return residual_jacobian(m, d_x, d_R, d_K, stream, m->prm.block_layout == BIOFEM_BLOCK_COL_MAJOR);
 }
 
-/* k_on_host: d_K is the device view of a mapped page-locked host buffer */
-static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream, bool k_on_host)
+/* colmajor: each 3x3 block stored column by column (PETSc SeqBAIJ); the
+   Newton solve's own calls always take row-major blocks */
+static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, void *d_K, void *stream, bool colmajor)
 {
   if (!m || !d_x || !d_R || !d_K) return fail(85, "null argument");
   if (!m->dm.patch) return fail(58, "host-only handle");
@@ -731,16 +718,16 @@ static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, v
     if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st, true); tmark(m, st, 2); }
     if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 3); }
     if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
-    if (!rc) { rc = launch_block_gather(m->dm, m->kp, K, st, k_on_host); tmark(m, st, 5); }
+    if (!rc) { rc = launch_row_assemble(m->dm, m->kp, K, false, colmajor, st); tmark(m, st, 5); }
     if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   } else {
-    /* FP32-bulk: residual in FP64, tangent (D, K_e, K) in FP32 */
+    /* FP32-bulk: residual in float-float, tangent (D, K) in FP32 */
     float *K = static_cast<float *>(d_K);
     if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
-    if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st); tmark(m, st, 2); }
+    if (!rc) { rc = launch_elem_residual_ff(m->dm, m->kp, st); tmark(m, st, 2); }
     if (!rc) { rc = launch_elem_tangent_f32(m->dm, m->kp, st); tmark(m, st, 3); }
     if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
-    if (!rc) { rc = launch_block_gather_f32(m->dm, m->kp, K, st, k_on_host); tmark(m, st, 5); }
+    if (!rc) { rc = launch_row_assemble(m->dm, m->kp, K, true, colmajor, st); tmark(m, st, 5); }
     if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   }
   if (rc) return fail(76, std::string("jacobian launch: ") + cudaGetErrorString((cudaError_t)rc));
@@ -804,7 +791,7 @@ int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K
   const size_t n = 3 * (size_t)(m->topo.n_v + m->topo.n_ghosts);
   const size_t kbytes = 9 * (size_t)m->nnzb * (m->prm.precision == BIOFEM_FP64 ? sizeof(double) : sizeof(float));
   /* A page-locked, device-mapped K buffer (cudaHostAlloc / cudaMallocHost /
-     cudaHostRegister) is written by the block gather itself, each value once,
+     cudaHostRegister) is written by the row assembly itself, each value once,
      so the copy-out overlaps the assembly instead of following it. */
   void *dK = m->d_K;
   cudaPointerAttributes a{};
@@ -813,7 +800,7 @@ int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *K
   else
     cudaGetLastError();
   CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, m->st));
-  int rc = residual_jacobian(m, m->d_x, m->d_R, dK, m->st, dK != m->d_K);
+  int rc = RunGpuResidualJacobianDevice(m, m->d_x, m->d_R, dK, m->st);
   if (rc) return rc;
   if (R) CUDA_TRY(cudaMemcpyAsync(R, m->d_R, n * sizeof(double), cudaMemcpyDeviceToHost, m->st));
   if (dK == m->d_K) CUDA_TRY(cudaMemcpyAsync(K, m->d_K, kbytes, cudaMemcpyDeviceToHost, m->st));
@@ -830,7 +817,7 @@ int RunGpuResidualParts(BiofemGpuMesh *m, const double *x, double *R, double *Fi
   CUDA_TRY(cudaMallocAsync((void **)&parts, 3 * n * sizeof(double), st));
   CUDA_TRY(cudaMemcpyAsync(m->d_x, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
   int rc = launch_positions(m->dm, m->kp, m->d_x, st);
-  if (!rc) rc = launch_elem_residual(m->dm, m->kp, st);
+  if (!rc) rc = launch_residual_elements(m, st);
   if (!rc) rc = launch_node_gather(m->dm, m->kp, m->d_x, m->d_R, st, parts);
   if (!rc) rc = launch_scale(m->dm, m->kp, m->d_R, st);
   if (rc) {
@@ -893,7 +880,7 @@ static int newton_residual_cb(void *ctx, const double *x, double *R, void *strea
 
 static int newton_jacobian_cb(void *ctx, const double *x, double *R, void *K, void *stream)
 {
-  return RunGpuResidualJacobianDevice(static_cast<BiofemGpuMesh *>(ctx), x, R, K, stream);
+  return residual_jacobian(static_cast<BiofemGpuMesh *>(ctx), x, R, K, stream, false);
 }
 
 int RunGpuNewtonSolveDevice(BiofemGpuMesh *m, double *d_x, const BiofemNewtonOptions *opt, BiofemNewtonStats *stats,
@@ -960,11 +947,11 @@ int SetGpuDynamics(BiofemGpuMesh *m, const BiofemDynParams *d)
     return fail(62, "dynamic parameters out of range");
   const size_t n = 3 * (size_t)kp.nt;
   if (!m->dm.xn) {
-    /* lumped mass over every triangle (FDynamic's serial loop runs over
-       n_elmt + 2 n_ghosts): flat reference areas and, per node, its corner
-       triangles in triangle order */
+    /* lumped mass over the real triangles (FDynamic with the DMPlex context
+       of an active-strain run, main.c:1178-1270): flat reference areas and,
+       per node, its corner triangles in triangle order */
     const HostTopo &T = m->topo;
-    const int ntri = T.n_elmt + 2 * T.n_ghosts, nt = kp.nt;
+    const int ntri = T.n_elmt, nt = kp.nt;
     std::vector<double> area(ntri);
     for (int t = 0; t < ntri; t++) area[t] = tri_area0(T, t);
     std::vector<int> dptr(nt + 1, 0), didx(3 * (size_t)ntri);
@@ -1049,6 +1036,7 @@ int SetGpuElementGamma(BiofemGpuMesh *m, const double *gamma_e)
   if (!rc) rc = launch_ref_prep(m->dm, kp, m->d_fib, m->d_gam, const_cast<double *>(m->dm.eref), m->st);
   const size_t nref = (size_t)(kRefPerQp * kp.nq + kRefPerElem) * ne;
   if (!rc && m->dm.erefF) rc = launch_to_float(m->dm.eref, const_cast<float *>(m->dm.erefF), (long long)nref, m->st);
+  if (!rc && m->dm.erefFF) rc = launch_to_ff(m->dm.eref, const_cast<void *>(m->dm.erefFF), (long long)nref, m->st);
   if (rc) return fail(76, std::string("activation update launch: ") + cudaGetErrorString((cudaError_t)rc));
   CUDA_TRY(cudaStreamSynchronize(m->st));
   return 0;

@@ -40,6 +40,7 @@
 #define BIOFEM_ELEMENT_CUH
 
 #include "biofem_host.h"
+#include "ff.cuh"
 
 namespace biofem {
 
@@ -197,6 +198,14 @@ template <> __host__ __device__ __forceinline__ EPar<double> epar<double>(const 
   EPar<double> e;
   e.mu = p.mu; e.K = p.K; e.hhalf = p.hhalf; e.nq = p.nq; e.iters = p.iters; e.tnormal = p.tnormal;
   for (int q = 0; q < kMaxQp; q++) { e.theta[q] = p.theta[q]; e.w[q] = p.w[q]; }
+  return e;
+}
+/* Float-float parameters (the FP32-bulk residual) */
+template <> __host__ __device__ __forceinline__ EPar<FF> epar<FF>(const KParams &p)
+{
+  EPar<FF> e;
+  e.mu = FF(p.mu); e.K = FF(p.K); e.hhalf = FF(p.hhalf); e.nq = p.nq; e.iters = p.iters; e.tnormal = p.tnormal;
+  for (int q = 0; q < kMaxQp; q++) { e.theta[q] = FF(p.theta[q]); e.w[q] = FF(p.w[q]); }
   return e;
 }
 /* FP32 parameters were converted on the host: no FP64 work in FP32 kernels */
@@ -883,8 +892,33 @@ __device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R
   df[12] = -dm2.x; df[13] = -dm2.y; df[14] = -dm2.z;
 }
 
-/* ---------------- element contraction ---------------- */
-constexpr int kKRounds = (9 * 16 + 15) / 16;   /* offsets per lane of a 9 nen block row, nen <= 16 */
+/* ---------------- tangent contraction (row assembly) ---------------- */
+/* The element stiffness is K_e = N^T D N with D = df/dy (15 x 15) and N the
+   5 x nen basis table acting on each Cartesian component.  The row assembly
+   forms it one block row a at a time:
+     w = (N[:,a] (x) I3)^T D          (3 x 15, w[15 i + k] = sum_r N[r][a] D[3r+i][k]),
+     K_ab[i][j] = sum_s N[s][b] w[15 i + 3 s + j],
+   plus, when a and b are corner slots of the triangle, the follower-pressure
+   block: the cross-product matrix of sc v_b, v_b the corner's vector. */
+template <class R>
+__host__ __device__ __forceinline__ R row_w_entry(const R *D, const R *tab, int a, int t)
+{
+  const int i = t / 15, k = t - 15 * i;
+  R acc = R(0);
+#pragma unroll
+  for (int r = 0; r < 5; r++) acc = fma(tab[r * 16 + a], D[(3 * r + i) * 15 + k], acc);
+  return acc;
+}
+
+template <class R>
+__host__ __device__ __forceinline__ R row_block_entry(const R *w, const R *tab, int b, int q)
+{
+  const int i = q / 3, j = q - 3 * i;
+  R acc = R(0);
+#pragma unroll
+  for (int s = 0; s < 5; s++) acc = fma(tab[s * 16 + b], w[15 * i + 3 * s + j], acc);
+  return acc;
+}
 
 /* Entry (i, j) of the follower-pressure block d c / d x_k = [s v]x (the cross
    product matrix of s v), for runtime i, j. */
@@ -896,64 +930,6 @@ __host__ __device__ __forceinline__ R skew_entry(int i, int j, const R v[3], R s
   const R vm = m3 == 0 ? v[0] : (m3 == 1 ? v[1] : v[2]);
   const R t = s * vm;
   return (j - i + 3) % 3 == 1 ? -t : t;
-}
-
-/* K_e = N^T D N of one element in its 16 lanes, T = D N kept in registers.
-   Lane l owns the offsets o = l + 16k (k < kKRounds, o < 9 nen) of a block
-   row, o = 9b + 3i + j, and forms T[(r,i)][(b,j)] = sum_s D[3r+i][3s+j] N[s][b]
-   (r < 5) for them once; then for every row node a it writes
-   K[(a,i)][(b,j)] = sum_r N[r][a] T[(r,i)][(b,j)], plus the follower-pressure
-   block when a and b are corner slots, to ke[9 nen a + o] (block layout
-   (a nen + b) 9 + 3i + j): consecutive lanes write consecutive values.  The
-   summation order of every entry is that of the two-pass form (T, then K).
-   D: this element's D = df/dy, row stride drow.  vv, sc: the pressure block
-   of corner k is the cross-product matrix of sc vv[k]. */
-template <class R>
-__host__ __device__ __forceinline__ void contract_element(const R *D, int drow, const R *tab, int nen, int lane,
-                                                 const int cslot[3], bool pressure, const R vv[3][3], R sc, R *ke)
-{
-  const int lim = 9 * nen;
-  R T[kKRounds][5], P[kKRounds];
-#pragma unroll
-  for (int k = 0; k < kKRounds; k++) {
-    if (16 * k < lim) {   /* the same for the 16 lanes of the element */
-      const int o = lane + 16 * k;
-      const int oc = o < lim ? o : 0;
-      const int b = oc / 9, w = oc - 9 * b, i = w / 3, j = w - 3 * i;
-#pragma unroll
-      for (int r = 0; r < 5; r++) {
-        R acc = R(0);
-#pragma unroll
-        for (int sr = 0; sr < 5; sr++) acc = fma(D[(3 * r + i) * drow + 3 * sr + j], tab[sr * 16 + b], acc);
-        T[k][r] = acc;
-      }
-      R pk = R(0);
-      if (pressure) {
-#pragma unroll
-        for (int c = 0; c < 3; c++)
-          if (b == cslot[c]) pk = pk + skew_entry(i, j, vv[c], sc);
-      }
-      P[k] = pk;
-    }
-  }
-  for (int a = 0; a < nen; a++) {
-    R Na[5];
-#pragma unroll
-    for (int r = 0; r < 5; r++) Na[r] = tab[r * 16 + a];
-    const bool corner = pressure && (a == cslot[0] || a == cslot[1] || a == cslot[2]);
-    R *row = ke + (size_t)a * lim;
-#pragma unroll
-    for (int k = 0; k < kKRounds; k++) {
-      if (16 * k < lim) {
-        const int o = lane + 16 * k;
-        R acc = R(0);
-#pragma unroll
-        for (int r = 0; r < 5; r++) acc = fma(Na[r], T[k][r], acc);
-        if (corner) acc += P[k];
-        if (o < lim) row[o] = acc;
-      }
-    }
-  }
 }
 
 } /* namespace biofem */

@@ -14,24 +14,28 @@
  *   k_elem_tangent   16 lanes per element: the stress is differentiated along
  *                    the metric components of each thickness point (one job
  *                    per lane), then lane j carries d/dy_j through the
- *                    geometry and the chain rule, giving column j of df/dy;
- *                    the half-warp then forms K_e = N^T (df/dy) N
- *                    (contract_element: T = (df/dy) N held in registers)
+ *                    geometry and the chain rule, giving column j of
+ *                    D = df/dy, stored per element (kDeStride values, with the
+ *                    follower-pressure corner vectors) for the row assembly
+ *   k_elem_residual_ff  the FP32-bulk residual: k_elem_residual's element math
+ *                    in float-float numbers on the FP32 pipe
  *   k_node_gather    one thread per node: Fint / Fext (and FDynamic's Fdyn)
  *                    summed over the node's element contributions in element
  *                    order (the order FInternalAct's VecSetValues loop adds
  *                    them), R = Fint - Fext + Fdyn, clamp rows R = x - X,
  *                    ghost rows 0 (main.c:844-1016)
- *   k_block_gather   one thread per tangent value: sum of the element-matrix
- *                    entries mapped to that 3x3 block, in element order
- *   k_scale          R *= 1 / max(|Fext|_inf, 1) (main.c:1020-1026); the block
- *                    gathers apply the same factor to K as they write it
+ *   k_row_assemble   one warp per row node: for every element holding the
+ *                    node, K_e's block row N_a^T D N (and the pressure blocks)
+ *                    added into the row's blocks in shared memory in a fixed
+ *                    order, then the row written once
+ *   k_scale          R *= 1 / max(|Fext|_inf, 1) (main.c:1020-1026); the row
+ *                    assembly applies the same factor to K as it writes it
  *   k_elem_thickness UpdateElementThickness (output); k_dyn_diag / k_dyn_update
  *                    the dynamic term's tangent diagonal and xAccVel
  *
  * Assembly is deterministic: every sum runs in a fixed order given by the
- * precomputed element-to-node / element-to-block maps, independent of the
- * launch configuration.
+ * precomputed node-to-element lists, independent of the launch
+ * configuration; nothing is accumulated with atomics.
  */
 #include <cuda_runtime.h>
 
@@ -158,11 +162,26 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
     a31 = a31 - scl(dot(a31, n), n);
     a32 = a32 - scl(dot(a32, n), n);
   }
-  const V3<double> f = {fib[3 * (size_t)e], fib[3 * (size_t)e + 1], fib[3 * (size_t)e + 2]};
-  const double gam = p.gamma * gscale[e];
+  /* Fa_cart = afac (I - gam f f^T): the fibre activation (-cart_fib_act 1)
+     has afac = 1; the isotropic one (-cart_fib_act 0,
+     active_strain.c:1238-1255), diag(a, a, 1/a^2) with a = 1 - gamma, is
+     a (I - (1 - 1/a^3) e3 e3^T).  The scale afac divides the mu part of the
+     stress by afac^2 and rho by afac^6 (det Fa_cart = afac^3 (1 - gam phi));
+     Ci + A Ci H, CC3333 and the quadratic forms do not depend on it. */
+  double afac = 1.0, gam;
+  V3<double> f;
+  if (!p.iso_act) {
+    f = {fib[3 * (size_t)e], fib[3 * (size_t)e + 1], fib[3 * (size_t)e + 2]};
+    gam = p.gamma * gscale[e];
+  } else {
+    afac = 1.0 - p.gamma * gscale[e];
+    f = {0.0, 0.0, 1.0};
+    gam = 1.0 - 1.0 / (afac * afac * afac);
+  }
+  const double ia2 = 1.0 / (afac * afac);
   const double phi = dot(f, f);
   const double gamp = gam / (1.0 - gam * phi);
-  const double c1 = 2.0 * gamp + gamp * gamp * phi;
+  const double c1 = (2.0 * gamp + gamp * gamp * phi) * ia2;
   /* flat reference triangle area (AreaNormal, io.c:1646-1669) */
   double X[3][3];
   for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
@@ -181,7 +200,8 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
     for (int i = 0; i < 3; i++) t[i] = dot(g[i], f);
     for (int i = 0; i < 3; i++) s[i] = Gi[i][0] * t[0] + Gi[i][1] * t[1] + Gi[i][2] * t[2];
     const double omg = 1.0 - gam * phi;
-    const double rho = 1.0 / (det3(G) * omg * omg);
+    const double a3 = afac * afac * afac;
+    const double rho = 1.0 / (det3(G) * omg * omg * (a3 * a3));
     /* v = Fa_inv.Cov G^-1 e3, w = Fa_inv.Cov G^-1 v, A^T x = G (Fa.Cont x) */
     double u[3] = {Gi[0][2], Gi[1][2], Gi[2][2]};
     double v[3], gv[3], w[3];
@@ -200,7 +220,8 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
     const double e3[3] = {0.0, 0.0, 1.0};
     aT(v, av); aT(w, aw); aT(e3, ae);
     double *o = eref + (size_t)kRefPerQp * q * ne + e;
-    o[0] = Gi[0][0]; o[1 * ne] = Gi[1][1]; o[2 * ne] = 0.5 * (Gi[0][1] + Gi[1][0]); o[3 * ne] = Gi[2][2];
+    o[0] = Gi[0][0] * ia2; o[1 * ne] = Gi[1][1] * ia2; o[2 * ne] = 0.5 * (Gi[0][1] + Gi[1][0]) * ia2;
+    o[3 * ne] = Gi[2][2] * ia2;
     for (int k = 0; k < 3; k++) {
       o[(4 + k) * ne] = s[k]; o[(7 + k) * ne] = t[k];
       o[(11 + k) * ne] = av[k]; o[(14 + k) * ne] = aw[k]; o[(17 + k) * ne] = ae[k];
@@ -212,6 +233,29 @@ __global__ void k_ref_prep(DevMesh m, KParams p, const double *__restrict__ fib,
 }
 
 /* ---------------- residual element kernel ---------------- */
+/* Pressure corner force of element e: each corner receives n P dA / 3 =
+   P (x2-x1)x(x3-x1) / 6 (SurfaceNormalPressure, external.c:589-624); the dead
+   load takes the same expression on the reference corners
+   (SurfaceConstNormalPressure, Nf and dA0 of Init, external.c:699-730). */
+__device__ __forceinline__ void elem_pressure_force(const DevMesh &m, const KParams &p, int e)
+{
+  const size_t ne = p.ne;
+  double X[3][3];
+  for (int k = 0; k < 3; k++) {
+    const size_t c = (size_t)m.etri[3 * (size_t)e + k];
+    if (p.pres_dead) { X[k][0] = m.X[3 * c]; X[k][1] = m.X[3 * c + 1]; X[k][2] = m.X[3 * c + 2]; }
+    else load_node(m.pos, (int)c, X[k][0], X[k][1], X[k][2]);
+  }
+  const V3<double> d21 = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
+  const V3<double> d31 = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
+  const V3<double> ca = cross(d21, d31);
+  const double nrm = sqrt(ca.x * ca.x + ca.y * ca.y + ca.z * ca.z);
+  const double dA = 0.5 * nrm;
+  m.fp[e] = (ca.x / nrm) * p.pressure * dA / 3.;
+  m.fp[ne + e] = (ca.y / nrm) * p.pressure * dA / 3.;
+  m.fp[2 * ne + e] = (ca.z / nrm) * p.pressure * dA / 3.;
+}
+
 __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, double *__restrict__ gm_out,
                                                        double *__restrict__ gp_out, double *__restrict__ tape_out)
 {
@@ -245,31 +289,99 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
     m.fb[(3 * a + 1) * ne + e] = fy;
     m.fb[(3 * a + 2) * ne + e] = fz;
   }
-  /* follower pressure: each corner receives n P dA / 3 = P (x2-x1)x(x3-x1) / 6 */
-  if (p.pressure != 0.0) {
-    double X[3][3];
-    for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
-    const V3<double> d21 = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
-    const V3<double> d31 = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
-    const V3<double> ca = cross(d21, d31);
-    const double nrm = sqrt(ca.x * ca.x + ca.y * ca.y + ca.z * ca.z);
-    const double dA = 0.5 * nrm;
-    m.fp[e] = (ca.x / nrm) * p.pressure * dA / 3.;
-    m.fp[ne + e] = (ca.y / nrm) * p.pressure * dA / 3.;
-    m.fp[2 * ne + e] = (ca.z / nrm) * p.pressure * dA / 3.;
+  if (p.pressure != 0.0) elem_pressure_force(m, p, e);
+}
+
+/* ---------------- FP32-bulk residual (float-float) ---------------- */
+/* The residual of the FP32-bulk form, on the FP32 pipe with float-float
+   numbers (ff.cuh, about 48 significant bits): one thread per element, the
+   element math of k_elem_residual.  Plain FP32 does not keep the residual's
+   1e-6 budget on these meshes: rounding y = N x alone to FP32 moves R by
+   ~1e-6 relative (C1, C2) and the FP32 stress by ~5e-6, so the residual takes
+   float-float, whose error sits near 1e-13.  Node positions are taken
+   relative to the element's first corner in FP64 before the split, the shift
+   is put back through (sum_i N_r[i]) x_c; the element forces leave as
+   doubles (hi + lo is exact in FP64) for the FP64 node sums. */
+__global__ void __launch_bounds__(128) k_elem_residual_ff(DevMesh m, KParams p)
+{
+  __shared__ FF tabs[kNumTables * 85];   /* tables, then their row sums */
+  const FF *ntab = static_cast<const FF *>(m.ntabFF);
+  for (int i = threadIdx.x; i < kNumTables * 85; i += blockDim.x) tabs[i] = ntab[i];
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.ne) return;
+  const int info = m.einfo[e];
+  const int nen = info & 0xff, tabi = info >> 8;
+  const FF *tab = tabs + tabi * 80, *tsum = tabs + kNumTables * 80 + tabi * 5;
+  double xc[3];
+  load_node(m.pos, m.etri[3 * (size_t)e], xc[0], xc[1], xc[2]);
+  FF y[15];
+  {
+    const FF c[3] = {FF(xc[0]), FF(xc[1]), FF(xc[2])};
+#pragma unroll
+    for (int r = 0; r < 5; r++)
+#pragma unroll
+      for (int d = 0; d < 3; d++) y[3 * r + d] = tsum[r] * c[d];
   }
+  const int *pe = m.patch + 16 * (size_t)e;
+  for (int i = 0; i < nen; i++) {
+    double X, Y, Z;
+    load_node(m.pos, __ldg(pe + i), X, Y, Z);
+    const FF d[3] = {FF(X - xc[0]), FF(Y - xc[1]), FF(Z - xc[2])};
+#pragma unroll
+    for (int r = 0; r < 5; r++) {
+      const FF c = tab[r * 16 + i];
+#pragma unroll
+      for (int k = 0; k < 3; k++) y[3 * r + k] = y[3 * r + k] + c * d[k];
+    }
+  }
+  FF f[15];
+  int st = 0;
+  const EPar<FF> ep = epar<FF>(p);
+  elem_forces<FF, FF>(y, ep, static_cast<const FF *>(m.erefFF) + e, p.ne, f, st);
+  set_status(m.status, st);
+  const size_t ne = p.ne;
+  for (int a = 0; a < nen; a++) {
+    FF fx = FF(0.f, 0.f), fy = FF(0.f, 0.f), fz = FF(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < 5; r++) {
+      const FF c = tab[r * 16 + a];
+      fx = fx + c * f[3 * r]; fy = fy + c * f[3 * r + 1]; fz = fz + c * f[3 * r + 2];
+    }
+    m.fb[(3 * a) * ne + e] = ff_to_double(fx);
+    m.fb[(3 * a + 1) * ne + e] = ff_to_double(fy);
+    m.fb[(3 * a + 2) * ne + e] = ff_to_double(fz);
+  }
+  if (p.pressure != 0.0) elem_pressure_force(m, p, e);
+}
+
+__global__ void k_to_ff(const double *__restrict__ a, FF *__restrict__ b, long long n)
+{
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) b[t] = FF(a[t]);
 }
 
 /* ---------------- tangent element kernel ---------------- */
 constexpr int kTanElemsPerCta = 8;   /* 16 lanes per element, 128 threads */
 
+/* The pressure block vectors of one element (follower-pressure load
+   stiffness): every corner carries P/6 (x2-x1)x(x3-x1), so d/dx1 = [b-a]x,
+   d/dx2 = -[b]x, d/dx3 = [a]x with a = x2-x1, b = x3-x1; stored after D in
+   the element's block for the row assembly. */
+template <class R>
+__device__ __forceinline__ void store_pressure_vectors(const R av[3], const R bv[3], R *dst)
+{
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    dst[d] = bv[d] - av[d];
+    dst[3 + d] = -bv[d];
+    dst[6 + d] = av[d];
+  }
+}
+
 __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
 {
   __shared__ double tabs[kNumTables * 80];
-  /* D = df/dy per element, row stride 19 (3 mod 16 eight-byte banks: the 9
-     (i, j) rows and columns the lanes read fall in distinct banks) */
-  constexpr int kDRow = 19, kDSlot = 15 * kDRow;
-  __shared__ double Dsh[kTanElemsPerCta * kDSlot];
   __shared__ double Jsh[kTanElemsPerCta][kMaxQp * 21]; /* constitutive derivatives per thickness point */
   for (int i = threadIdx.x; i < kNumTables * 80; i += blockDim.x) tabs[i] = m.ntab[i];
   __syncthreads();
@@ -289,27 +401,19 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
      primal C33 sub-iteration values come from k_elem_residual, launched
      before this kernel (which also performs the CC3333 checks) */
   elem_forces_split_tl<double>(y, ep, m.eref + ee, p.ne, m.gpr + ee, lane, Jsh[slot], fd, m.gmq + ee, m.gtape + ee);
-  /* column `lane` of D = df/dy */
-  double *D = Dsh + slot * kDSlot;
+  if (!live) return;
+  /* column `lane` of D = df/dy, row-major in the element's block */
+  double *De = m.De + (size_t)kDeStride * e;
   if (lane < 15) {
 #pragma unroll
-    for (int r = 0; r < 15; r++) D[r * kDRow + lane] = fd[r];
+    for (int r = 0; r < 15; r++) De[r * 15 + lane] = fd[r];
+  } else if (p.pressure != 0.0 && !p.pres_dead) {
+    double X[3][3];
+    for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
+    const double av[3] = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
+    const double bv[3] = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
+    store_pressure_vectors<double>(av, bv, De + kDePres);
   }
-  /* the element forces come from k_elem_residual, launched before this kernel */
-  __syncwarp();
-  if (!live) return;
-  /* Follower-pressure load stiffness: every corner carries P/6 (x2-x1)x(x3-x1),
-     so d/dx1 = [b-a]x, d/dx2 = -[b]x, d/dx3 = [a]x with a = x2-x1, b = x3-x1,
-     entering K = dR/dx with a minus sign at the corner rows. */
-  const int cs = m.ecorner[e];
-  const int cslot[3] = {cs & 31, (cs >> 5) & 31, (cs >> 10) & 31};
-  double X[3][3];
-  for (int k = 0; k < 3; k++) load_node(m.pos, m.etri[3 * (size_t)e + k], X[k][0], X[k][1], X[k][2]);
-  const double av[3] = {X[1][0] - X[0][0], X[1][1] - X[0][1], X[1][2] - X[0][2]};
-  const double bv[3] = {X[2][0] - X[0][0], X[2][1] - X[0][1], X[2][2] - X[0][2]};
-  const double vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
-  contract_element<double>(D, kDRow, tab, nen, lane, cslot, p.pressure != 0.0, vv, -p.pressure / 6.0,
-                           m.ke + (size_t)m.kofs[e] * 9);
 }
 
 /* ---------------- FP32-bulk tangent ---------------- */
@@ -318,15 +422,11 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
    shared by shuffles) and rounded to FP32, so the FP32 values carry the
    element-size digits; the shift is put back through (sum_i N_r[i]) * x_c,
    which is not zero for the truncated second-derivative rows (their rows sum
-   to -1e-4 / -1e-4 / +2e-4).  Element matrices are written in FP32. */
-__global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams p)
+   to -1e-4 / -1e-4 / +2e-4).  D = df/dy is written in FP32 for the row assembly. */
+__global__ void __launch_bounds__(128) k_elem_tangent_f32(DevMesh m, KParams p)
 {
   __shared__ float tabs[kNumTables * 80];
   __shared__ float tsum[kNumTables * 5];
-  /* D = df/dy per element: row stride 20 and element stride 323 (3 mod 32
-     banks) keep the 9 (i, j) rows and columns the lanes read in distinct banks */
-  constexpr int kDRow = 20, kDSlot = 323;
-  __shared__ float Dsh[kTanElemsPerCta * kDSlot];
   __shared__ float JshF[kTanElemsPerCta][kMaxQp * 21];
   for (int i = threadIdx.x; i < kNumTables * 85; i += blockDim.x) {
     if (i < kNumTables * 80) tabs[i] = m.ntabF[i]; else tsum[i - kNumTables * 80] = m.ntabF[i];
@@ -373,12 +473,7 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
   const EPar<float> ep = epar<float>(p);
   elem_forces_split<float>(y, ep, m.erefF + ee, p.ne, lane, JshF[slot], fd, st);
   if (live) set_status(m.status, st);
-  float *D = Dsh + slot * kDSlot;
-  if (lane < 15) {
-#pragma unroll
-    for (int r = 0; r < 15; r++) D[r * kDRow + lane] = fd[r].d;
-  }
-  /* pressure stiffness from the shifted corner coordinates */
+  /* pressure vectors from the shifted corner coordinates */
   const int cs = m.ecorner[ee];
   const int cslot[3] = {cs & 31, (cs >> 5) & 31, (cs >> 10) & 31};
   float xk[3][3];
@@ -387,68 +482,16 @@ __global__ void __launch_bounds__(128, 4) k_elem_tangent_f32(DevMesh m, KParams 
     xk[k][1] = __shfl_sync(hmask, dy, cslot[k], 16);
     xk[k][2] = __shfl_sync(hmask, dz, cslot[k], 16);
   }
-  __syncwarp();
   if (!live) return;
-  const float av[3] = {xk[1][0] - xk[0][0], xk[1][1] - xk[0][1], xk[1][2] - xk[0][2]};
-  const float bv[3] = {xk[2][0] - xk[0][0], xk[2][1] - xk[0][1], xk[2][2] - xk[0][2]};
-  const float vv[3][3] = {{bv[0] - av[0], bv[1] - av[1], bv[2] - av[2]}, {-bv[0], -bv[1], -bv[2]}, {av[0], av[1], av[2]}};
-  contract_element<float>(D, kDRow, tab, nen, lane, cslot, p.pres6f != 0.f, vv, -p.pres6f,
-                          m.keF + (size_t)m.kofs[e] * 9);
-}
-
-/* FP32 block gather with compensated (Kahan) summation in element order. */
-__global__ void k_block_gather_f32(DevMesh m, KParams p, float *__restrict__ K, const int *__restrict__ perm)
-{
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 9 * m.nnzb) return;
-  const long long kk = t / 9;
-  const int w = (int)(t - 9 * kk);
-  const long long k = perm ? perm[kk] : kk;
-  const double fmax = __longlong_as_double((long long)*m.fmax);   /* read early: its latency hides under the sum */
-  const int row = m.blkrow[k];
-  const int kind = m.rowkind[row];
-  float s = 0.f;
-  if (kind != 0) {
-    s = (m.colind[k] == row && (w == 0 || w == 4 || w == 8)) ? 1.f : 0.f;
-  } else {
-    float comp = 0.f;
-    long long c = m.cptr[k];
-    const long long cend = m.cptr[k + 1];
-    /* four gathered loads in flight per step; the compensated sum keeps the list order */
-    for (; c + 4 <= cend; c += 4) {
-      float v[4];
+  float *De = m.DeF + (size_t)kDeStride * e;
+  if (lane < 15) {
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int id = m.cidx[c + u];
-        const int neg = (int)((unsigned)(id < 0) << 31);
-        v[u] = __int_as_float(__float_as_int(m.keF[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]) ^ neg);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const float yv = v[u] - comp;
-        const float tt = s + yv;
-        comp = (tt - s) - yv;
-        s = tt;
-      }
-    }
-    for (; c < cend; c++) {
-      const int id = m.cidx[c];
-      const int neg = (int)((unsigned)(id < 0) << 31);   /* sign flip of a chain-rule contribution, integer pipe */
-      const float v = __int_as_float(__float_as_int(m.keF[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]) ^ neg);
-      const float yv = v - comp;
-      const float tt = s + yv;
-      comp = (tt - s) - yv;
-      s = tt;
-    }
-    if (p.dyn && m.colind[k] == row && (w == 0 || w == 4 || w == 8)) s += (float)m.dyn_diag[row];
+    for (int r = 0; r < 15; r++) De[r * 15 + lane] = fd[r].d;
+  } else if (p.pres6f != 0.f && !p.pres_dead) {
+    const float av[3] = {xk[1][0] - xk[0][0], xk[1][1] - xk[0][1], xk[1][2] - xk[0][2]};
+    const float bv[3] = {xk[2][0] - xk[0][0], xk[2][1] - xk[0][1], xk[2][2] - xk[0][2]};
+    store_pressure_vectors<float>(av, bv, De + kDePres);
   }
-  /* R and K scale by 1/max(|Fext|_inf, 1) (main.c:1020-1026; k_node_gather
-     found the max); ghost rows stay identity */
-  if (fmax > 1.0 && kind != 2) {
-    const double sc = 1.0 / fmax;
-    s = (float)(s * sc);
-  }
-  K[9 * k + w] = s;
 }
 
 /* ---------------- node gather (residual assembly) ---------------- */
@@ -475,9 +518,9 @@ __global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x
         fe[0] += m.fp[e]; fe[1] += m.fp[ne + e]; fe[2] += m.fp[2 * ne + e];
       }
     const int kind = m.rowkind[i];
-    /* FDynamic (main.c:1293-1360, the serial path): triangle-order sum of the
-       node's inertial (and damping) force over every triangle with this
-       corner, ghost and bridging triangles included */
+    /* FDynamic (main.c:1178-1270, the path of an active-strain run):
+       triangle-order sum of the node's inertial (and damping) force over the
+       real triangles with this corner */
     double fd[3] = {0.0, 0.0, 0.0};
     if (p.dyn && (kind == 0 || (parts && i < p.nv))) {
       for (int c = m.dptr[i]; c < m.dptr[i + 1]; c++) {
@@ -523,54 +566,172 @@ __global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x
   if ((threadIdx.x & 31) == 0 && lmax) atomicMax(m.fmax, lmax);
 }
 
-/* ---------------- block gather (tangent assembly) ---------------- */
-__global__ void k_block_gather(DevMesh m, KParams p, double *__restrict__ K, const int *__restrict__ perm)
+/* ---------------- row assembly (tangent) ---------------- */
+/* One warp per row node i.  For every element e whose patch holds i at slot a
+   (the row's contribution list, element order) and every slot b of that
+   patch, K_ib += (N[:,a] (x) I3)^T D_e (N[:,b] (x) I3), with D_e = df/dy the
+   element kernel stored, plus the follower-pressure block when a and b are
+   corner slots; a ghost slot b adds to the blocks of its parents with signs
+   +, +, - (x_g = x_nv2 + x_nv1 - x_nv3).  The row's blocks accumulate in
+   shared memory in a fixed order (contributions in element order; within an
+   element the real slots, then the ghost slots in slot order), so K is
+   deterministic; FP32 sums are compensated (Kahan).  Clamped and ghost rows
+   are identity rows.  K is scaled by 1/max(|Fext|_inf, 1) as it is written
+   (main.c:1020-1026; k_node_gather, launched before, found the max); with
+   colmajor each 3x3 block is stored column by column. */
+constexpr int kRowWarps = 4;
+constexpr unsigned kSlotGhost = 1u << 31;
+
+__device__ __forceinline__ int row_find(const int *cols, int nb, int node)
 {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 9 * m.nnzb) return;
-  const long long kk = t / 9;
-  const int w = (int)(t - 9 * kk);
-  const long long k = perm ? perm[kk] : kk;   /* blocks of one row by decreasing contribution count */
-  const double fmax = __longlong_as_double((long long)*m.fmax);   /* read early: its latency hides under the sum */
-  const int row = m.blkrow[k];
-  const int kind = m.rowkind[row];
-  double s = 0.0;
-  if (kind != 0) {
-    s = (m.colind[k] == row && (w == 0 || w == 4 || w == 8)) ? 1.0 : 0.0;
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (cols[mid] < node) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+template <class R> struct RowAsmBuf {
+  R *acc, *comp, *w, *gv;
+  int *cols;
+  unsigned *slot;
+};
+
+template <class R>
+__device__ __forceinline__ RowAsmBuf<R> row_buf(unsigned char *base, int maxblk)
+{
+  RowAsmBuf<R> b;
+  b.acc = reinterpret_cast<R *>(base);
+  b.comp = b.acc + 9 * maxblk;
+  b.w = b.comp + (sizeof(R) == 4 ? 9 * maxblk : 0);
+  b.gv = b.w + 48;
+  b.cols = reinterpret_cast<int *>(b.gv + 144);
+  b.slot = reinterpret_cast<unsigned *>(b.cols + maxblk);
+  return b;
+}
+
+/* bytes of one warp's buffers (kept a multiple of 16) */
+__host__ __device__ __forceinline__ size_t row_buf_bytes(int maxblk, size_t rsize)
+{
+  const size_t nr = 9 * (size_t)maxblk * (rsize == 4 ? 2 : 1) + 48 + 144;
+  return ((nr * rsize + 4 * (size_t)maxblk + 64) + 15) & ~(size_t)15;
+}
+
+template <class R>
+__device__ __forceinline__ void row_add(R *acc, R *comp, int idx, R v)
+{
+  if constexpr (sizeof(R) == 4) {
+    const R s = acc[idx], yv = v - comp[idx];
+    const R t = s + yv;
+    comp[idx] = (t - s) - yv;
+    acc[idx] = t;
   } else {
-    long long c = m.cptr[k];
-    const long long cend = m.cptr[k + 1];
-    /* four gathered loads in flight per step; the sum keeps the list order
-       (s - v and s + (-v) round alike) */
-    /* the sign of a chain-rule contribution is flipped on the integer pipe
-       (the FP64 pipe, which bounds this kernel, then sees one add each) */
-    for (; c + 4 <= cend; c += 4) {
-      double v[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int id = m.cidx[c + u];
-        const long long neg = (long long)(id < 0) << 63;
-        const long long bits = __double_as_longlong(m.ke[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]);
-        v[u] = __longlong_as_double(bits ^ neg);
+    acc[idx] += v;
+  }
+}
+
+template <class R>
+__global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KParams p, const R *__restrict__ De,
+                                                                 const R *__restrict__ ntab, R psc, R *__restrict__ K,
+                                                                 int maxblk, int colmajor)
+{
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  R *tabs = reinterpret_cast<R *>(row_smem);
+  for (int t = threadIdx.x; t < kNumTables * 80; t += blockDim.x) tabs[t] = ntab[t];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int i = blockIdx.x * kRowWarps + wid;
+  if (i >= p.nt) return;
+  RowAsmBuf<R> B = row_buf<R>(row_smem + ((kNumTables * 80 * sizeof(R) + 15) & ~(size_t)15) +
+                              (size_t)wid * row_buf_bytes(maxblk, sizeof(R)), maxblk);
+  const int k0 = m.rowptr[i], nb = m.rowptr[i + 1] - k0;
+  const int kind = m.rowkind[i];
+  R *Kr = K + 9 * (size_t)k0;
+  if (kind != 0) {   /* clamped (R = x - X) and ghost (R = 0) rows: identity */
+    for (int t = lane; t < 9 * nb; t += 32) {
+      const int q = t % 9;
+      Kr[t] = (m.colind[k0 + t / 9] == i && (q == 0 || q == 4 || q == 8)) ? R(1) : R(0);
+    }
+    return;
+  }
+  for (int t = lane; t < nb; t += 32) B.cols[t] = m.colind[k0 + t];
+  for (int t = lane; t < 9 * nb; t += 32) {
+    B.acc[t] = R(0);
+    if constexpr (sizeof(R) == 4) B.comp[t] = R(0);
+  }
+  __syncwarp();
+  const int c1 = m.rptr[i + 1];
+  for (int c = m.rptr[i]; c < c1; c++) {
+    const int rc = m.rcon[c];
+    const int e = rc & ((1 << 27) - 1), a = rc >> 27;
+    const int info = m.einfo[e];
+    const int nen = info & 0xff;
+    const R *tab = tabs + (info >> 8) * 80;
+    const R *D = De + (size_t)kDeStride * e;
+    /* where each patch slot lands in this row: lane b < nen */
+    bool ghost = false;
+    if (lane < nen) {
+      const int node = m.patch[16 * (size_t)e + lane];
+      unsigned s;
+      if (node < p.nv) {
+        s = (unsigned)row_find(B.cols, nb, node);
+      } else {
+        const int g = node - p.nv;
+        const int q2 = row_find(B.cols, nb, m.ghost3[3 * g + 1]), q1 = row_find(B.cols, nb, m.ghost3[3 * g]);
+        const int q3 = row_find(B.cols, nb, m.ghost3[3 * g + 2]);
+        s = kSlotGhost | (unsigned)q2 | ((unsigned)q1 << 10) | ((unsigned)q3 << 20);
+        ghost = true;
       }
-#pragma unroll
-      for (int u = 0; u < 4; u++) s += v[u];
+      B.slot[lane] = s;
     }
-    for (; c < cend; c++) {
-      const int id = m.cidx[c];
-      const long long neg = (long long)(id < 0) << 63;
-      const long long bits = __double_as_longlong(m.ke[(size_t)(id < 0 ? -(id + 1) : id) * 9 + w]);
-      s += __longlong_as_double(bits ^ neg);
+    const unsigned gmask = __ballot_sync(0xffffffffu, ghost);
+    /* w = (N[:,a] (x) I3)^T D: 45 values, w[15 i + k] = sum_r N[r][a] D[3r+i][k] */
+    for (int t = lane; t < 45; t += 32) B.w[t] = row_w_entry(D, tab, a, t);
+    /* pressure blocks: rows and columns at the triangle's corner slots */
+    const int cs = m.ecorner[e];
+    const int cslot0 = cs & 31, cslot1 = (cs >> 5) & 31, cslot2 = (cs >> 10) & 31;
+    const bool acorner = p.pressure != 0.0 && !p.pres_dead && (a == cslot0 || a == cslot1 || a == cslot2);
+    __syncwarp();
+    for (int t = lane; t < 9 * nen; t += 32) {
+      const int b = t / 9, q = t - 9 * b;
+      R v = row_block_entry(B.w, tab, b, q);
+      if (acorner) {
+        const int kc = b == cslot0 ? 0 : (b == cslot1 ? 1 : (b == cslot2 ? 2 : -1));
+        if (kc >= 0) v += skew_entry(q / 3, q % 3, D + kDePres + 3 * kc, psc);
+      }
+      const unsigned s = B.slot[b];
+      if (!(s & kSlotGhost)) row_add(B.acc, B.comp, 9 * (int)s + q, v);
+      else B.gv[t] = v;
     }
-    if (p.dyn && m.colind[k] == row && (w == 0 || w == 4 || w == 8)) s += m.dyn_diag[row];
+    __syncwarp();
+    /* ghost slots, in slot order: lane 9k + q adds to entry q of parent k */
+    for (unsigned gm = gmask; gm; gm &= gm - 1) {
+      const int b = __ffs(gm) - 1;
+      if (lane < 27) {
+        const int k = lane / 9, q = lane - 9 * k;
+        const unsigned s = B.slot[b];
+        const int pos = (int)((s >> (10 * k)) & 1023u);
+        const R v = B.gv[9 * b + q];
+        row_add(B.acc, B.comp, 9 * pos + q, k == 2 ? -v : v);
+      }
+      __syncwarp();
+    }
+    __syncwarp();   /* slot targets and w are rewritten by the next contribution */
   }
-  /* the scale 1/max(|Fext|_inf, 1) of R and K (main.c:1020-1026; k_node_gather
-     found the max), applied as the value is written; ghost rows stay identity */
-  if (fmax > 1.0 && kind != 2) {
-    const double sc = 1.0 / fmax;
-    s = s * sc;
+  /* dynamic term diagonal, scale, write-out */
+  const double fmax = __longlong_as_double((long long)*m.fmax);
+  const R sc = fmax > 1.0 ? R(1.0 / fmax) : R(1);
+  const int pd = row_find(B.cols, nb, i);
+  for (int t = lane; t < 9 * nb; t += 32) {
+    R v = B.acc[t];
+    const int q = t % 9;
+    if (p.dyn && t / 9 == pd && (q == 0 || q == 4 || q == 8)) v += R(m.dyn_diag[i]);
+    if (fmax > 1.0) {
+      if constexpr (sizeof(R) == 4) v = (R)((double)v * (1.0 / fmax)); else v = v * sc;
+    }
+    Kr[colmajor ? t - q + 3 * (q % 3) + q / 3 : t] = v;
   }
-  K[9 * k + w] = s;
 }
 
 /* ---------------- scaling ---------------- */
@@ -606,6 +767,18 @@ int launch_elem_residual(const DevMesh &m, const KParams &p, void *stream, bool 
   return (int)cudaGetLastError();
 }
 
+int launch_elem_residual_ff(const DevMesh &m, const KParams &p, void *stream)
+{
+  k_elem_residual_ff<<<blocks_for(p.ne, 128), 128, 0, (cudaStream_t)stream>>>(m, p);
+  return (int)cudaGetLastError();
+}
+
+int launch_to_ff(const double *a, void *b, long long n, void *stream)
+{
+  k_to_ff<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(a, static_cast<FF *>(b), n);
+  return (int)cudaGetLastError();
+}
+
 int launch_elem_tangent(const DevMesh &m, const KParams &p, void *stream)
 {
   k_elem_tangent<<<blocks_for(p.ne, kTanElemsPerCta), 128, 0, (cudaStream_t)stream>>>(m, p);
@@ -618,12 +791,6 @@ int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream)
   return (int)cudaGetLastError();
 }
 
-int launch_block_gather_f32(const DevMesh &m, const KParams &p, float *K, void *stream, bool k_on_host)
-{
-  if (m.nnzb == 0) return 0;
-  k_block_gather_f32<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K, k_on_host ? nullptr : m.gperm);
-  return (int)cudaGetLastError();
-}
 
 __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long long n)
 {
@@ -680,16 +847,18 @@ __global__ void k_dyn_diag(DevMesh m, KParams p)
   m.dyn_diag[i] = s;
 }
 
-/* xAccVel (main.c:1367-1412, the serial path over n_v + n_ghosts nodes),
-   then xnm1 <- xn, xn <- x (main.c:571-572) */
+/* xAccVel (main.c:1367-1412; with the DMPlex context the n_v real nodes),
+   then xnm1 <- xn, xn <- x over every entry (main.c:571-572) */
 __global__ void k_dyn_update(DevMesh m, KParams p, const double *__restrict__ x)
 {
   const size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (j >= 3 * (size_t)p.nt) return;
-  const double xddn = m.xdd[j];
-  const double a = p.dyn_M1 * (x[j] - m.xn[j]) - p.dyn_M2 * m.xd[j] - p.dyn_M3 * m.xdd[j];
-  m.xdd[j] = a;
-  m.xd[j] = m.xd[j] + p.dyn_U2 * xddn + p.dyn_U3 * a;
+  if (j < 3 * (size_t)p.nv) {
+    const double xddn = m.xdd[j];
+    const double a = p.dyn_M1 * (x[j] - m.xn[j]) - p.dyn_M2 * m.xd[j] - p.dyn_M3 * m.xdd[j];
+    m.xdd[j] = a;
+    m.xd[j] = m.xd[j] + p.dyn_U2 * xddn + p.dyn_U3 * a;
+  }
   m.xnm1[j] = m.xn[j];
   m.xn[j] = x[j];
 }
@@ -713,13 +882,31 @@ int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, doub
   return (int)cudaGetLastError();
 }
 
-int launch_block_gather(const DevMesh &m, const KParams &p, double *K, void *stream, bool k_on_host)
+size_t row_assemble_smem(int maxblk, bool f32)
 {
-  if (m.nnzb == 0) return 0;
-  /* K in HBM: each row's blocks by decreasing contribution count; K in mapped
-     host memory: plain block order, so the stores stream out in address order */
-  k_block_gather<<<blocks_for(9 * m.nnzb, 256), 256, 0, (cudaStream_t)stream>>>(m, p, K, k_on_host ? nullptr : m.gperm);
+  const size_t rs = f32 ? sizeof(float) : sizeof(double);
+  return ((kNumTables * 80 * rs + 15) & ~(size_t)15) + kRowWarps * row_buf_bytes(maxblk, rs);
+}
+
+int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, bool colmajor, void *stream)
+{
+  const int grid = blocks_for(p.nt, kRowWarps);
+  const size_t smem = row_assemble_smem(m.maxblk, f32);
+  if (f32)
+    k_row_assemble<float><<<grid, 32 * kRowWarps, smem, (cudaStream_t)stream>>>(
+        m, p, m.DeF, m.ntabF, -p.pres6f, static_cast<float *>(K), m.maxblk, (int)colmajor);
+  else
+    k_row_assemble<double><<<grid, 32 * kRowWarps, smem, (cudaStream_t)stream>>>(
+        m, p, m.De, m.ntab, -p.pressure / 6.0, static_cast<double *>(K), m.maxblk, (int)colmajor);
   return (int)cudaGetLastError();
+}
+
+int row_assemble_configure(int maxblk, bool f32)
+{
+  const size_t smem = row_assemble_smem(maxblk, f32);
+  cudaError_t e = f32 ? cudaFuncSetAttribute(k_row_assemble<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                      : cudaFuncSetAttribute(k_row_assemble<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return (int)e;
 }
 
 int launch_scale(const DevMesh &m, const KParams &p, double *R, void *stream)

@@ -24,6 +24,15 @@
  * First call on a device: it looks up the array's device address with
  * cudaGetSymbolAddress (once per device, that device current) and caches
  * it.  Make that first call before any stream capture.
+ *
+ * Device: the handle's mesh arrays live on the device that was current when
+ * it was prepared; a call made with another device current is refused
+ * (error 62), so that no launch mixes one device's array with another's mesh.
+ *
+ * Errors: as for the other device variants, a vanishing CC3333 inside the
+ * element kernel (ModElemC33, active_strain.c:1676) sets the handle's status
+ * word, which BiofemGpuSync(handle, stream) turns into error 72; calls on
+ * the same handle that overlap on the GPU share that word.
  */
 #include <cuda_runtime.h>
 
@@ -43,7 +52,7 @@ static double *g_noalloc_ptr[64] = {};   /* device address per device ordinal */
 
 /* error reporting shared with bridge.cu */
 int noalloc_fail(int code, const std::string &msg);
-const DevMesh *mesh_devview(const BiofemGpuMesh *m, const KParams **kp);
+const DevMesh *mesh_devview(const BiofemGpuMesh *m, const KParams **kp, int *device);
 
 static int noalloc_scratch(double **out)
 {
@@ -71,8 +80,13 @@ extern "C" int RunGpuResidualNoAlloc(BiofemGpuMesh *m, const double *d_x, double
 {
   if (!m || !d_x || !d_R) return noalloc_fail(85, "null argument");
   const KParams *kp = nullptr;
-  const DevMesh *dm = mesh_devview(m, &kp);
+  int mdev = -1, cur = -1;
+  const DevMesh *dm = mesh_devview(m, &kp, &mdev);
   if (!dm || !kp) return noalloc_fail(58, "mesh handle has no device data (host-only handle?)");
+  if (cudaGetDevice(&cur) != cudaSuccess) return noalloc_fail(76, "cudaGetDevice failed");
+  if (cur != mdev)
+    return noalloc_fail(62, "the mesh handle lives on device " + std::to_string(mdev) + " but device " +
+                                std::to_string(cur) + " is current");
   const long long need = 4LL * kp->nt + 51LL * kp->ne + 1;
   if (need > BIOFEM_NOALLOC_SCRATCH_DOUBLES)
     return noalloc_fail(63, "mesh too large for the no-allocation residual: needs " + std::to_string(need) +

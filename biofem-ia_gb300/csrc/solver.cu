@@ -381,6 +381,7 @@ struct SolverWork {
   const void *g_K = nullptr;
   const void *g_pc = nullptr;   /* preconditioner the graph was captured with (null: block-Jacobi) */
   cudaStream_t st = nullptr;   /* allocation stream */
+  long long bytes = 0;         /* device memory allocated above */
 };
 
 /* Restarted GMRES(m) with right block-Jacobi preconditioning; the Arnoldi
@@ -512,7 +513,10 @@ SolverWork *solver_create(int n, int nb, int m, void *stream, int *rc)
   w->st = (cudaStream_t)stream;
   cudaError_t e = cudaSuccess;
   const size_t dn = sizeof(double) * (size_t)n;
-  auto A = [&](void **p, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(p, bytes, w->st); };
+  auto A = [&](void **p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMallocAsync(p, bytes, w->st);
+    if (e == cudaSuccess) w->bytes += (long long)bytes;
+  };
   A((void **)&w->V, dn * (size_t)(m + 1));
   A((void **)&w->Z, dn * (size_t)m); A((void **)&w->w, dn); A((void **)&w->dx, dn); A((void **)&w->xt, dn);
   A((void **)&w->Rt, dn); A((void **)&w->xh, dn);
@@ -555,6 +559,7 @@ void solver_destroy(SolverWork *w)
 
 double *solver_xbuf(SolverWork *w) { return w->xh; }
 int solver_m(const SolverWork *w) { return w->m; }
+long long solver_device_bytes(const SolverWork *w) { return w ? w->bytes : 0; }
 
 /* Newton on device data; x is a device vector (updated in place). */
 int newton_device(const DevMesh &dm, const KParams &kp, bool f32, void *dK, double *dR, double *x,

@@ -6,7 +6,7 @@
  * (InitCudaWorkspace / DestroyCudaWorkspace / PrepareCudaHostWorkspace /
  * Run*Kernel, all extern "C", PetscErrorCode return), but taking plain
  * arrays instead of FE* so that callers need neither PETSc nor CUDA headers.
- * A PETSc build binds these from its SNES callbacks (see INTEGRATION.md).
+ * A PETSc build binds these from its SNES callbacks.
  *
  * Conventions
  *   - Every entry point returns an int that is PetscErrorCode-compatible:
@@ -18,7 +18,8 @@
  *     node-major (x, y, z), real nodes first, then one ghost node per
  *     boundary-ring node (io.c:329-345, dmplex_geom.c:836-857).
  *   - The tangent is a 3x3-block CSR (BSR) matrix over the same node
- *     numbering.  Block values are row-major within the block.
+ *     numbering.  Block values are row-major within the block, or column-major
+ *     (PETSc SeqBAIJ storage) when BiofemParams.block_layout asks for it.
  *   - Host-side API is single-threaded per mesh handle; different handles may
  *     be driven from different host threads (error messages are per thread).
  */
@@ -63,9 +64,22 @@ typedef struct {
                                   tangential part n,alpha only.  The two agree where |a1 x a2| is uniform; on
                                   non-uniform patches (ghost-reflected boundary patches of a fine mesh) the
                                   normal part J,alpha/J n folds the thickness points once h << h0 */
+  int32_t block_layout;        /* storage of each 3x3 block of the tangent the RunGpuResidualJacobian* calls
+                                  return: BIOFEM_BLOCK_ROW_MAJOR (0, default) or BIOFEM_BLOCK_COL_MAJOR (1, the
+                                  layout of PETSc SeqBAIJ storage, so MatSeqBAIJGetArray's array can be passed) */
+  int32_t pressure_kind;       /* BIOFEM_PRESSURE_FOLLOWER (0, default): SurfaceNormalPressure, the current normal
+                                  and area (external.c:589-624), with its load stiffness in K;
+                                  BIOFEM_PRESSURE_DEAD (1): SurfaceConstNormalPressure, the reference normal and
+                                  area dA0 (external.c:699-730), no load stiffness */
+  int32_t activation_kind;     /* BIOFEM_ACTIVATION_FIBRE (0, default; -cart_fib_act 1): Fa = I - gamma f f^T;
+                                  BIOFEM_ACTIVATION_ISOTROPIC (1; -cart_fib_act 0): Fa = diag(1 - gamma,
+                                  1 - gamma, 1/(1 - gamma)^2) in the Cartesian basis (active_strain.c:1238-1255) */
 } BiofemParams;
 
 enum { BIOFEM_FP64 = 0, BIOFEM_FP32_BULK = 1 };
+enum { BIOFEM_BLOCK_ROW_MAJOR = 0, BIOFEM_BLOCK_COL_MAJOR = 1 };
+enum { BIOFEM_PRESSURE_FOLLOWER = 0, BIOFEM_PRESSURE_DEAD = 1 };
+enum { BIOFEM_ACTIVATION_FIBRE = 0, BIOFEM_ACTIVATION_ISOTROPIC = 1 };
 /* Centroid basis-derivative tables.  REFERENCE: the four-decimal values of
    active_strain.c:69-88 (parity with the reference).  EXACT (extension): the
    rationals they round; the four-decimal second-derivative rows sum to
@@ -79,7 +93,8 @@ typedef struct {
   int32_t n_irregular;         /* elements on the one-step-subdivision branch */
   int64_t nnzb;                /* 3x3 blocks in the tangent pattern */
   int64_t n_contrib;           /* element-block contributions (assembly map size) */
-  int64_t device_bytes;        /* device memory held by the handle */
+  int64_t device_bytes;        /* device memory held by the handle: mesh arrays, and once a Newton solve has
+                                  run, its GMRES work and multigrid hierarchy */
   int32_t precision;           /* BIOFEM_FP64 or BIOFEM_FP32_BULK */
 } BiofemMeshInfo;
 
@@ -124,8 +139,9 @@ int GetGpuCsrPattern(const BiofemGpuMesh *m, int32_t *rowptr, int32_t *colind);
 int RunGpuResidual(BiofemGpuMesh *m, const double *x, double *R);
 /* R(x) and the tangent K = dR/dx (new: the reference is matrix-free,
    main.c:464-466).  Kvals has 9*nnzb entries: double for a BIOFEM_FP64
-   handle, float for a BIOFEM_FP32_BULK handle (whose residual is still FP64
-   and whose tangent is formed in FP32 on patch-local shifted coordinates).
+   handle, float for a BIOFEM_FP32_BULK handle (whose residual runs in
+   float-float numbers on the FP32 pipe and whose tangent is formed in FP32
+   on patch-local shifted coordinates).
    R may be NULL. */
 int RunGpuResidualJacobian(BiofemGpuMesh *m, const double *x, double *R, void *Kvals);
 
@@ -148,7 +164,9 @@ int BiofemGpuSync(BiofemGpuMesh *m, void *stream);
    19,000 triangles) are rejected with error 63.  All calls share that array:
    calls that overlap on the GPU race and must be serialised.  The first call
    on a device looks up the array's address (once per device); make it before
-   any stream capture. */
+   any stream capture.  The handle's device must be current (else error 62).
+   Element errors (a vanishing CC3333) come back, as for the other device
+   variants, through BiofemGpuSync(handle, stream) as error 72. */
 int RunGpuResidualNoAlloc(BiofemGpuMesh *m, const double *d_x, double *d_R, void *stream);
 
 /* One quasi-static load step: Newton on R(x) = 0 with the assembled tangent
@@ -295,7 +313,7 @@ int FormJacobianFEMGpu(void *snes, const double *x, void *Kvals, void *ctx);
 /* Per-kernel CUDA-event timing of the device calls (off by default): slot i
    is the i-th launch of the call (residual: positions, element residual,
    node gather, scale; jacobian: positions, element tangent, node gather,
-   block gather, scale).  Times accumulate over calls until re-enabled. */
+   row assembly, scale).  Times accumulate over calls until re-enabled. */
 int EnableGpuKernelTiming(BiofemGpuMesh *m, int on);
 int GetGpuKernelTimes(const BiofemGpuMesh *m, double *ms, int32_t nslots, int32_t *calls);
 

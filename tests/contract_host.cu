@@ -1,9 +1,11 @@
-/* Host driver of contract_element (element.cuh) for tests/test_contraction_host.py:
-   reads one case (nen, corner slots, pressure flag, D 15x15, the 5x16 basis
-   table, the three corner vectors and the scale) from argv[1], runs the 16
-   lanes one after another in double and in float, and writes both element
-   matrices (9 nen^2 values each, as double; entries never written keep NaN)
-   to argv[2]. */
+/* Host driver of the tangent contraction of the row assembly (row_w_entry,
+   row_block_entry and skew_entry in element.cuh) for
+   tests/test_contraction_host.py: reads one case (nen, corner slots, pressure
+   flag, D 15x15, the 5x16 basis table, the three corner vectors and the
+   scale) from argv[1], forms every block (a, b) of the element matrix the way
+   the row assembly does, row a after row a, in double and in float, and
+   writes both element matrices (9 nen^2 values each, block layout
+   (a nen + b) 9 + 3i + j, as double) to argv[2]. */
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -16,16 +18,24 @@ template <class R>
 static void run(const double *Din, const double *tabin, int nen, const int cs[3], bool pres, const double *vvin,
                 double sc, double *out)
 {
-  const int drow = 20;
-  std::vector<R> D(15 * drow, R(0)), tab(80, R(0)), ke((size_t)9 * nen * nen, R(NAN));
-  for (int r = 0; r < 15; r++)
-    for (int c = 0; c < 15; c++) D[r * drow + c] = (R)Din[15 * r + c];
+  std::vector<R> D(225), tab(80), w(45), ke((size_t)9 * nen * nen, R(NAN));
+  for (int i = 0; i < 225; i++) D[i] = (R)Din[i];
   for (int i = 0; i < 80; i++) tab[i] = (R)tabin[i];
   R vv[3][3];
   for (int k = 0; k < 3; k++)
     for (int d = 0; d < 3; d++) vv[k][d] = (R)vvin[3 * k + d];
-  for (int lane = 0; lane < 16; lane++)
-    contract_element<R>(D.data(), drow, tab.data(), nen, lane, cs, pres, vv, (R)sc, ke.data());
+  for (int a = 0; a < nen; a++) {
+    for (int t = 0; t < 45; t++) w[t] = row_w_entry(D.data(), tab.data(), a, t);
+    const bool acorner = pres && (a == cs[0] || a == cs[1] || a == cs[2]);
+    for (int b = 0; b < nen; b++)
+      for (int q = 0; q < 9; q++) {
+        R v = row_block_entry(w.data(), tab.data(), b, q);
+        if (acorner)
+          for (int k = 0; k < 3; k++)
+            if (b == cs[k]) v += skew_entry(q / 3, q % 3, vv[k], (R)sc);
+        ke[((size_t)a * nen + b) * 9 + q] = v;
+      }
+  }
   for (size_t i = 0; i < ke.size(); i++) out[i] = (double)ke[i];
 }
 

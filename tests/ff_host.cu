@@ -1,0 +1,50 @@
+/* Host check of the float-float arithmetic (biofem-ia_gb300/csrc/ff.cuh) for
+   tests/test_ff_host.py: for seeded operand pairs spanning 1e-12 .. 1e12 (and
+   nearly cancelling pairs for the sum), prints the largest error of +, -, *,
+   /, sqrt against long double, relative to the result (sum: to the larger
+   operand, the bound a double-word sum guarantees under cancellation). */
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+
+#include "../biofem-ia_gb300/csrc/ff.cuh"
+
+using namespace biofem;
+
+static uint64_t g_state = 0x9e3779b97f4a7c15ull;
+static double urand()
+{
+  g_state = g_state * 6364136223846793005ull + 1442695040888963407ull;
+  return (double)(g_state >> 11) * (1.0 / 9007199254740992.0);
+}
+static double operand()
+{
+  const double mag = std::pow(10.0, -12.0 + 24.0 * urand());
+  return (urand() < 0.5 ? -1.0 : 1.0) * mag * (1.0 + urand());
+}
+static long double ld(FF a) { return (long double)a.hi + (long double)a.lo; }
+/* the operand as the float-float value it becomes, exactly */
+static long double ldv(double d) { return ld(FF(d)); }
+
+int main()
+{
+  double e_add = 0, e_cancel = 0, e_mul = 0, e_div = 0, e_sqrt = 0;
+  for (int k = 0; k < 200000; k++) {
+    const double a = operand(), b = operand();
+    const FF A(a), B(b);
+    const long double la = ldv(a), lb = ldv(b);
+    const long double s = la + lb;
+    e_add = std::fmax(e_add, (double)(std::fabs(ld(A + B) - s) / std::fmax(std::fabs(la), std::fabs(lb))));
+    const double c = -a * (1.0 + 1e-9 * (urand() - 0.5));   /* nearly cancelling */
+    const FF C(c);
+    const long double lc = ldv(c);
+    e_cancel = std::fmax(e_cancel, (double)(std::fabs(ld(A + C) - (la + lc)) / std::fabs(la)));
+    e_mul = std::fmax(e_mul, (double)(std::fabs(ld(A * B) - la * lb) / std::fabs(la * lb)));
+    e_div = std::fmax(e_div, (double)(std::fabs(ld(A / B) - la / lb) / std::fabs(la / lb)));
+    const double p = std::fabs(a);
+    const long double lp = ldv(p);
+    e_sqrt = std::fmax(e_sqrt, (double)(std::fabs(ld(dsqrt(FF(p))) - std::sqrt(lp)) / std::sqrt(lp)));
+  }
+  std::printf("%.3e %.3e %.3e %.3e %.3e\n", e_add, e_cancel, e_mul, e_div, e_sqrt);
+  return 0;
+}

@@ -1,8 +1,8 @@
-"""The element contraction K_e = N^T D N of both tangent kernels
-(contract_element in element.cuh), run on the host for every patch size
-1-step subdivision gives (nen = 10..16, so every register round of a lane,
-including the ones no test mesh reaches on the device), with and without the
-follower-pressure blocks, against numpy.  Every entry must be written."""
+"""The element contraction K_e = N^T D N of the row assembly (row_w_entry,
+row_block_entry and skew_entry in element.cuh), run on the host for every
+patch size 1-step subdivision gives (nen = 10..16, including the ones no test
+mesh reaches on the device), with and without the follower-pressure blocks,
+against numpy.  Every entry must be written."""
 import os
 import shutil
 import subprocess

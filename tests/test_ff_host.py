@@ -1,0 +1,25 @@
+"""The float-float arithmetic of the FP32-bulk residual (ff.cuh), on the
+host: sums (including nearly cancelling ones), products, quotients and square
+roots of seeded operands over 24 decades against long double.  Bound: 2^-44
+(5.7e-14) relative, against the 2^-24 (6e-8) of plain FP32."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_float_float_operations_hold_48_bits(tmp_path):
+    nvcc = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if Path("/usr/local/cuda/bin/nvcc").exists() else None)
+    if nvcc is None:
+        pytest.skip("nvcc not available")
+    exe = tmp_path / "ff_host"
+    subprocess.run([nvcc, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+                    str(ROOT / "tests" / "ff_host.cu"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    e_add, e_cancel, e_mul, e_div, e_sqrt = map(float, out)
+    bound = 2.0 ** -44
+    assert e_add <= bound and e_cancel <= bound, (e_add, e_cancel)
+    assert e_mul <= bound and e_div <= bound and e_sqrt <= bound, (e_mul, e_div, e_sqrt)
