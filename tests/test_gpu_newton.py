@@ -88,3 +88,36 @@ def test_eisenstat_walker_forcing_reaches_the_same_root():
     assert np.linalg.norm(xe - xf) <= 1e-7 * np.linalg.norm(xf - x0)
     assert se["gmres_its_total"] < sf["gmres_its_total"], (se["gmres_its_total"], sf["gmres_its_total"])
     sh.close()
+
+
+@pytest.mark.parametrize("pc", [0, 1], ids=["multigrid", "bjacobi"])
+def test_device_gmres_step_matches_scipy_gmres(pc):
+    """The device Krylov solve against scipy's gmres, the stand-in for PETSc
+    KSP: one Newton step without line search, linear tolerance 1e-11, solves
+    the system scipy's gmres (block-Jacobi(3x3) preconditioned, same
+    tolerance) solves on the same assembled tangent and residual."""
+    import scipy.sparse.linalg as spla
+    from biofem.gpu import GpuShell
+    w = configs.Workload("flat_40x30", 40, 30, z_sigma=1e-3, activation="smooth", index=83, pressure=3e-4)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+    R, K = sh.form_jacobian(x0)
+    A = sh.to_scipy(K).tocsr()
+    nb = A.shape[0] // 3
+    blocks = np.array([np.linalg.inv(A[3 * i:3 * i + 3, 3 * i:3 * i + 3].toarray()) for i in range(nb)])
+    M = spla.LinearOperator(A.shape, matvec=lambda v: np.einsum("bij,bj->bi", blocks, v.reshape(-1, 3)).ravel())
+    try:
+        dx_ref, info = spla.gmres(A, -R, rtol=1e-11, atol=0.0, restart=30, maxiter=3000, M=M)
+    except TypeError:   # scipy before 1.12 names the tolerance tol
+        dx_ref, info = spla.gmres(A, -R, tol=1e-11, atol=0.0, restart=30, maxiter=3000, M=M)
+    assert info == 0
+    x1, st = sh.newton(x0, max_newton=1, rtol=1e-30, gmres_rtol=1e-11, line_search=0, preconditioner=pc)
+    dx = x1 - x0
+    assert st["gmres_relres_last"] <= 1.0001e-11, st
+    # both solve the same system: true residuals in the assembled operator, and the two solutions
+    rn = np.linalg.norm(R)
+    assert np.linalg.norm(A @ dx + R) <= 1e-10 * rn, np.linalg.norm(A @ dx + R) / rn
+    assert np.linalg.norm(A @ dx_ref + R) <= 1e-10 * rn
+    assert np.linalg.norm(dx - dx_ref) <= 1e-6 * np.linalg.norm(dx_ref), np.linalg.norm(dx - dx_ref) / np.linalg.norm(dx_ref)
+    sh.close()

@@ -67,8 +67,12 @@ def test_residual_is_deterministic():
                                 configs.small(11, 8, activation="random", index=45, n_qp=6, basis=1),
                                 configs.small(12, 9, index=46, basis=1, tnormal=1, pressure=1e-3),
                                 configs.LVWorkload("lv_f4", 4, index=47),
+                                configs.small(8, 7, index=48, pressure=2e-3, dead_load=1),
+                                configs.small(9, 6, activation="random", index=49, iso_act=1),
+                                configs.LVWorkload("lv_f3", 3, index=50, iso_act=1, dead_load=1),
                                 configs.C1],
-                         ids=lambda w: w.name + ("_exact" if w.basis else "") + ("_tnormal" if w.tnormal else ""))
+                         ids=lambda w: w.name + ("_exact" if w.basis else "") + ("_tnormal" if w.tnormal else "")
+                         + ("_dead" if w.dead_load else "") + ("_iso" if w.iso_act else ""))
 def test_tangent_matches_oracle_directional_derivative(wl, oracle_lib):
     m = wl.build_mesh()
     o = oracle_lib.setup(m, wl, configs.MU, configs.BULK, configs.H0)
@@ -148,7 +152,7 @@ def test_kinematic_checks_C1():
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32_bulk"])
 def test_host_call_into_pinned_buffers(precision):
-    """RunGpuResidualJacobian with page-locked host buffers: the block gather
+    """RunGpuResidualJacobian with page-locked host buffers: the row assembly
     writes K straight into the mapped buffer; R and K equal the pageable-buffer
     call bitwise."""
     import torch

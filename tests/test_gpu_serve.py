@@ -71,3 +71,25 @@ def test_serve_admission_respects_budget():
         srv.submit(mb, big, configs.MU, configs.BULK, configs.H0, np.zeros(mb.n_dof))
     assert e.value.code == 55
     srv.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32_bulk"])
+def test_serve_estimate_covers_what_a_request_allocates(precision):
+    """The admission estimate BiofemServeEstimateBytes must not undercount:
+    for requests across the stream's size range, the device memory a handle
+    holds after its load step (mesh arrays, GMRES work, multigrid hierarchy;
+    GetGpuMeshInfo.device_bytes) stays below the estimate."""
+    import ctypes
+    from biofem.gpu import GpuShell, MeshInfo, estimate_bytes
+    for i, (lo, hi) in enumerate([(16, 17), (40, 41), (96, 97), (200, 201)]):
+        w = configs.serve_request(300 + i, lo, hi)
+        m = w.build_mesh()
+        sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=precision)
+        x0 = w.initial_x(m, sh.topology()["xyz0_full"])
+        sh.newton(x0, max_newton=2, rtol=1e-10)
+        info = MeshInfo()
+        assert sh.lib.GetGpuMeshInfo(sh.handle, ctypes.byref(info)) == 0
+        est = estimate_bytes(m.n_v, m.n_elmt, m.n_ghosts, precision)
+        print(f"{w.name} prec {precision}: device {info.device_bytes / 2**20:.1f} MiB, estimate {est / 2**20:.1f} MiB")
+        assert info.device_bytes <= est, (w.name, info.device_bytes, est)
+        sh.close()

@@ -75,3 +75,31 @@ def test_no_alloc_rejects_meshes_beyond_the_fixed_array():
         sh.residual_device_noalloc(dx.data_ptr(), dx.data_ptr(), 0)
     assert ei.value.code == 63 and "too large" in str(ei.value)
     sh.close()
+
+
+def test_no_alloc_residual_reports_element_errors_through_sync():
+    """A NaN coordinate makes CC3333 fail inside the element kernel; the
+    no-allocation call reports it like the other device variants, through
+    BiofemGpuSync (error 72), and the handle then gives the clean result."""
+    torch = pytest.importorskip("torch")
+    from biofem.gpu import BiofemError
+    w = configs.small(8, 6, activation="random", index=62, pressure=1e-3)
+    m, sh = _shell(w)
+    x = w.initial_x(m, sh.topology()["xyz0_full"])
+    dx = torch.tensor(x, device="cuda")
+    ref = torch.empty_like(dx)
+    sh.residual_device(dx.data_ptr(), ref.data_ptr(), 0)
+    sh.sync(0)
+    bad = x.copy()
+    bad[3 * (m.n_v // 2) + 2] = np.nan
+    dbad = torch.tensor(bad, device="cuda")
+    out = torch.empty_like(dx)
+    sh.residual_device_noalloc(dbad.data_ptr(), out.data_ptr(), 0)
+    with pytest.raises(BiofemError) as ei:
+        sh.sync(0)
+    assert ei.value.code == 72
+    sh.residual_device_noalloc(dx.data_ptr(), out.data_ptr(), 0)
+    sh.sync(0)
+    Rref = ref.cpu().numpy()
+    assert np.linalg.norm(out.cpu().numpy() - Rref) <= 1e-10 * np.linalg.norm(Rref)
+    sh.close()
