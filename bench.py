@@ -36,14 +36,21 @@ for _p in (ROOT, ROOT / "biofem-ia_gb300"):
         sys.path.insert(0, str(_p))
 
 METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_elem_tangent launch on
-# the 256x192 workload (ncu --set full; 239.8 MB read, 964.2 MB written)
-TANGENT_DRAM_BYTES_C2 = 239.822e6 + 964.227e6
-# sm__pipe_fp64_cycles_active (of peak sustained active) of the same capture
-FP64_PIPE_ACTIVE_C2 = 0.892
+# dram__bytes_read.sum + dram__bytes_write.sum per launch on the 256x192
+# workload, from one ncu capture of each kernel (None: not captured)
+DRAM_BYTES_C2 = {"elem_tangent": None, "row_assemble": None, "elem_residual": None}
+# sm__pipe_fp64_cycles_active (of peak sustained active) of k_elem_tangent on
+# the same workload (None: not captured)
+FP64_PIPE_ACTIVE_C2 = None
+# FP64 FMA throughput of this GB300, measured by the DFMA loop of the FP64 pipe
+# probe (biofem-ia_gb300/csrc/probe_fp64.cu): TFLOP/s
+FP64_DFMA_TFLOPS = 1.057
+KERNELS_FP64 = ["positions", "elem_residual", "elem_tangent", "node_gather", "row_assemble", "scale"]
+KERNELS_FP32 = ["positions", "elem_residual_ff", "elem_tangent_fp32", "node_gather", "row_assemble_fp32", "scale"]
 UNIT = "elems/s"
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_ELEMS = 2048
+REF_SAMPLE_ELEMS = 4096
 
 
 def parse():
@@ -126,22 +133,33 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_rk(w, mesh, topo, x_full, n_elems, threads, steps=1, warmup=0, residual_only=False):
-    """The reference's element algorithm on the host: R and element tangents
-    (or, with residual_only, R alone) for a bounded element sample; returns
-    elems/s.  The subdivision tables come from the library's host builder
-    (bitwise equal to the reference's)."""
+def cpu_oracle(w, mesh):
+    """The oracle set up on `mesh` by the reference's own table builders
+    (GlobalGhostInit, IrrVer, Patch restated; corner-incident scans, the same
+    tables as the reference's full scans) -- no GPU library involved."""
     from oracle.pyoracle import Oracle
     from biofem import configs
-    o = Oracle().setup_given_topology(mesh, w, topo, configs.MU, configs.BULK, configs.H0)
+    o = Oracle().set_fast_topology(True)
+    try:
+        o.setup(mesh, w, configs.MU, configs.BULK, configs.H0)
+    finally:
+        o.set_fast_topology(False)
+    return o
+
+
+def cpu_rk(o, n_elmt, x_full, n_elems, threads, steps=1, warmup=0, residual_only=False):
+    """The reference's element algorithm on the host (oracle `o`): R and the
+    element tangents (or, with residual_only, R alone) of a bounded window of
+    n_elems consecutive elements; each step takes the next window, spread over
+    the mesh.  Returns (elems/s, seconds, n_elems)."""
     x = np.ascontiguousarray(x_full)
     chk = ctypes.c_double()
-    n_elems = min(n_elems, mesh.n_elmt)
-    # spread the sample over the mesh: a strided window of consecutive elements
-    e0 = max(0, mesh.n_elmt // 2 - n_elems // 2)
+    n_elems = min(n_elems, n_elmt)
+    span = max(1, n_elmt - n_elems + 1)
     fn = o.lib.oracle_r_sample if residual_only else o.lib.oracle_rk_sample
     times = []
     for s in range(warmup + steps):
+        e0 = (n_elmt // 2 + s * 7919 * n_elems) % span
         t0 = time.perf_counter()
         rc = fn(x.ctypes.data_as(ctypes.c_void_p), e0, e0 + n_elems, threads, ctypes.byref(chk))
         dt = time.perf_counter() - t0
@@ -157,22 +175,48 @@ def cpu_jfnk_step(threads):
     Newton, unpreconditioned GMRES(30) on finite-difference J v) on C1, on
     the oracle residual with `threads` OpenMP threads: its wall time and how
     many residual evaluations it took."""
-    from oracle.pyoracle import Oracle
     from biofem import configs
-    from biofem.gpu import GpuShell
     w = configs.C1
     mesh = w.build_mesh()
-    host = GpuShell(mesh, w, configs.MU, configs.BULK, configs.H0, host_only=True)
-    topo = host.topology()
-    host.close()
-    o = Oracle().setup_given_topology(mesh, w, topo, configs.MU, configs.BULK, configs.H0)
+    o = cpu_oracle(w, mesh)
     o.set_threads(threads)
-    x0 = w.initial_x(mesh, topo["xyz0_full"])
+    x0 = w.initial_x(mesh, o.topology().xyz0_full)
     _, _, st = o.jfnk_newton_step(x0)
     return {"workload": f"{w.name} ({mesh.n_elmt} triangles), first Newton step from the reference state",
             "seconds": st["seconds"], "residual_evaluations": st["residual_evaluations"],
             "gmres_its": st["gmres_its"], "lin_converged": bool(st["lin_converged"]), "cores": threads,
             "kind": "port"}
+
+
+def bench_config(w, mesh, world):
+    """The workload description both arms print."""
+    return {"workload": f"{w.name} R+K FP64: {mesh.n_elmt} triangles, {mesh.n_v} nodes, {mesh.n_ghosts} ghosts, "
+                        f"{w.n_qp} thickness points, {w.c33_iters} C33 sub-iterations, P={w.pressure}, clamped ring",
+            "l2": "GPU arm: flushed between timed steps (256 MiB device write outside the events)",
+            "parallelism": f"replicas x{world}"}
+
+
+SAMPLE_NOTE = ("reference element algorithm (oracle/oracle.cpp, bitwise equal to the reference build) + exact "
+               "element tangent by Dual<48> forward mode, OpenMP over elements")
+
+
+def cpu_baseline_block(w, mesh, o, x, threads, n_sample, steps=1, warmup=0):
+    """cpu_baseline: R+K of a bounded element sample on all host threads, the
+    residual alone (what the reference evaluates: its Newton is Jacobian-free)
+    on all threads and on one, and one reference JFNK Newton step on C1."""
+    val, tot, n = cpu_rk(o, mesh.n_elmt, x, n_sample, threads, steps=steps, warmup=warmup)
+    cpu = {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{steps} x {n} consecutive elements of {w.name} (moving windows): {SAMPLE_NOTE}, {tot:.1f} s"}
+    rval, rtot, rn = cpu_rk(o, mesh.n_elmt, x, 4 * n_sample, threads, residual_only=True)
+    r1val, r1tot, r1n = cpu_rk(o, mesh.n_elmt, x, 4 * n_sample, 1, residual_only=True)
+    cpu["residual_only"] = {"value": rval, "unit": UNIT, "cores": threads, "one_core_value": r1val,
+                            "sample": f"{rn} elements on {threads} threads ({rtot:.2f} s), {r1n} on one "
+                                      f"({r1tot:.2f} s): element forces only"}
+    try:   # the reference's solver step, for scale beside the device Newton load step
+        cpu["jfnk_newton_step"] = cpu_jfnk_step(threads)
+    except Exception as exc:   # reported, never fatal to the line
+        cpu["jfnk_newton_step"] = {"error": f"{type(exc).__name__}: {exc}"}
+    return cpu
 
 
 def max_over_ranks(x: float, dist, device) -> float:
@@ -306,11 +350,16 @@ def case_bench(w, steps=5, warmup=2):
     K64, R64, u64 = keep["fp64"]
     K32, R32, u32 = keep["fp32_bulk"]
     out["K_frobenius_rel_err_fp32_vs_fp64"] = float(torch.linalg.norm(K32 - K64) / torch.linalg.norm(K64))
-    out["R_bit_identical"] = bool(torch.equal(R32, R64))
+    out["R_rel_err_fp32_vs_fp64"] = float(torch.linalg.norm(R32 - R64) / torch.linalg.norm(R64))
     out["displacement_rel_err_fp32_vs_fp64"] = float(torch.linalg.norm(u32 - u64) / torch.linalg.norm(u64))
     out["workload"] = (f"{w.name}: {m.n_elmt} triangles, {m.n_v} nodes, {m.n_ghosts} ghosts, q={w.n_qp}, "
                        f"basis tables {'exact' if w.basis else 'reference'}, thickness metric "
                        f"{'n,alpha' if w.tnormal else 'reference'}")
+    if w.basis or w.tnormal:
+        out["formulation"] = ("builder formulation (exact tables, tangential thickness metric): the reference's "
+                              "four-decimal tables and a3,alpha thickness metric are ill-posed at this h")
+    else:
+        out["formulation"] = "reference algebra (one-step subdivision tables on irregular patches)"
     out["irregular_elements"] = n_irregular
     del keep, K64, K32
     torch.cuda.empty_cache()
@@ -405,35 +454,30 @@ def serve_bench(n_req=512, slots=16, budget=40 << 30, load=0.8):
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path on this host's cores:
+    the oracle (a restatement of the reference's element algorithm, pinned
+    bitwise to the reference build) set up by its own table builders, R and
+    exact element tangents of a bounded element sample per step.  Loads no
+    GPU library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from biofem import configs
     w = workload(args.workload)
     mesh = w.build_mesh()
-    from biofem.gpu import GpuShell
-    host = GpuShell(mesh, w, configs.MU, configs.BULK, configs.H0, host_only=True)
-    topo = host.topology()
-    host.close()
-    x = w.initial_x(mesh, topo["xyz0_full"])
+    o = cpu_oracle(w, mesh)
+    x = w.initial_x(mesh, o.topology().xyz0_full)
     threads = os.cpu_count() or 1
-    sample = 1024
-    val, tot, n = cpu_rk(w, mesh, topo, x, sample, threads, steps=args.steps, warmup=args.warmup)
-    rval, rtot, rn = cpu_rk(w, mesh, topo, x, 8 * sample, threads, residual_only=True)
+    cpu = cpu_baseline_block(w, mesh, o, x, threads, REF_SAMPLE_ELEMS, steps=args.steps, warmup=args.warmup)
+    val = cpu["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * REF_SAMPLE_ELEMS / val,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded flat membrane)",
-        "config": {"workload": f"{w.name} R+K FP64 ({mesh.n_elmt} triangles, {w.n_qp} thickness points, "
-                               f"{w.c33_iters} C33 sub-iterations)", "sample_elements_per_step": n},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} consecutive elements of {w.name} per step: reference element algorithm "
-                                   f"(oracle/oracle.cpp, bitwise equal to the reference build) + exact element "
-                                   f"tangent by Dual<48> forward mode, OpenMP over elements",
-                         "residual_only": {"value": rval, "unit": UNIT, "cores": threads,
-                                           "sample": f"{rn} elements, element forces only ({rtot:.2f} s)"}},
+        "data": "synthetic (seeded flat membrane, row-alternating diagonals)",
+        "config": dict(bench_config(w, mesh, args.gpus), sample_elements_per_step=min(REF_SAMPLE_ELEMS, mesh.n_elmt)),
+        "cpu_baseline": cpu,
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "ms_per_step is the time of one sample window; the rate is the reference algorithm's elements/s",
     }
     print(json.dumps(line), flush=True)
 
@@ -545,7 +589,8 @@ def run_ours(args):
     K64h = dK.cpu().numpy()
     K32h = dK32.cpu().numpy().astype(np.float64)
     fp32_frob = float(np.linalg.norm(K32h - K64h) / np.linalg.norm(K64h))
-    fp32_rdiff = float(np.abs(dR32.cpu().numpy() - dR.cpu().numpy()).max())
+    R64h = dR.cpu().numpy()
+    fp32_rrel = float(np.linalg.norm(dR32.cpu().numpy() - R64h) / np.linalg.norm(R64h))
     f32_step = sum(f_ms) / len(f_ms)
     hx = torch.tensor(x_host).pin_memory()
     # the FP32-bulk form end to end through the public host call (FP32 K out);
@@ -611,65 +656,50 @@ def run_ours(args):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     step_gbs = b_alg / (ms * 1e-3) / 1e9
-    kern_gbs = b_alg / (kms[2] * 1e-3) / 1e9
-    names = ["positions", "elem_residual", "elem_tangent", "node_gather", "block_gather", "scale"]
+    dom = int(np.argmax(kms))
+    dom_name = KERNELS_FP64[dom]
+    kern_gbs = b_alg / (kms[dom] * 1e-3) / 1e9
     k_tan = kms[2]
     f_alg = canonical_flops(ne, w.n_qp)
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        threads = os.cpu_count() or 1
-        cval, ctot, cn = cpu_rk(w, mesh, topo, x_host, CPU_SAMPLE_ELEMS, threads, steps=1, warmup=0)
-        cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{cn} consecutive elements of {w.name}: reference element algorithm (oracle/oracle.cpp, "
-                         f"bitwise equal to the reference build) + exact element tangent by Dual<48> forward mode, "
-                         f"{ctot:.1f} s"}
-        # the residual alone, what the reference evaluates (its Newton is Jacobian-free): all cores and one
-        rval, rtot, rn = cpu_rk(w, mesh, topo, x_host, 4 * CPU_SAMPLE_ELEMS, threads, residual_only=True)
-        r1val, r1tot, r1n = cpu_rk(w, mesh, topo, x_host, 4 * CPU_SAMPLE_ELEMS, 1, residual_only=True)
-        cpu["residual_only"] = {"value": rval, "unit": UNIT, "cores": threads, "one_core_value": r1val,
-                                "sample": f"{rn} elements on {threads} threads ({rtot:.2f} s), {r1n} on one "
-                                          f"({r1tot:.2f} s): element forces only"}
-        try:   # the reference's solver step, for scale beside the device Newton load step
-            cpu["jfnk_newton_step"] = cpu_jfnk_step(threads)
-        except Exception as exc:   # reported, never fatal to the line
-            cpu["jfnk_newton_step"] = {"error": f"{type(exc).__name__}: {exc}"}
+        cpu = cpu_baseline_block(w, mesh, cpu_oracle(w, mesh), x_host, os.cpu_count() or 1, CPU_SAMPLE_ELEMS)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flat membrane, row-alternating diagonals)",
-        "config": {"workload": f"{w.name} R+K FP64: {ne} triangles, {info.n_v} nodes, {info.n_ghosts} ghosts, "
-                               f"{w.n_qp} thickness points, {w.c33_iters} C33 sub-iterations, P={w.pressure}, "
-                               f"clamped ring; tangent 3x3-block CSR nnzb={sh.nnzb}",
-                   "l2": "flushed between timed steps (256 MiB device write outside the events)",
-                   "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "k_elem_tangent", "achieved": kern_gbs, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": kern_gbs / hbm_peak, "traffic": TANGENT_DRAM_BYTES_C2,
+        "config": dict(bench_config(w, mesh, world),
+                       tangent={"format": "3x3-block CSR, row-major blocks, FP64 values", "nnzb": sh.nnzb}),
+        "roofline": {"bound": "hbm", "kernel": f"k_{dom_name}", "achieved": kern_gbs, "peak": hbm_peak,
+                     "unit": "GB/s", "frac": kern_gbs / hbm_peak, "traffic": DRAM_BYTES_C2.get(dom_name),
                      "peak_source": peak_src, "step_achieved_gbs": step_gbs,
-                     "note": "achieved = canonical algorithmic bytes of the R+K step (the dominant kernel's "
-                             "inputs and the assembled outputs) / k_elem_tangent's live launch time; traffic = "
-                             "dram read + write of one k_elem_tangent launch on C2 from an ncu capture (writes: element-"
-                             "matrix scratch; reads: mesh, positions and the primal values k_elem_residual stores); "
-                             "the kernel is FP64-pipe bound, see compute_roofline"},
+                     "note": "of measured HBM copy bandwidth; achieved = canonical algorithmic bytes of one R+K "
+                             "evaluation (patch ids, x and X, fibre and activation, R, K values once) / the dominant "
+                             "kernel's live launch time (CUDA events on the launch stream); traffic = dram read + "
+                             "write of one launch of that kernel on C2 from an ncu capture; the step is FP64-pipe "
+                             "bound, see compute_roofline"},
         "compute_roofline": {"kernel": "k_elem_tangent", "bound": "fp64", "kernel_ms": k_tan,
                              "canonical_flops_per_step": f_alg,
                              "achieved_tflops_canonical": f_alg / (k_tan * 1e-3) / 1e12,
-                             "peak_tflops": 1.25, "peak_source": "nominal GB300 FP64 (not measured)",
+                             "peak_tflops": FP64_DFMA_TFLOPS,
+                             "frac": f_alg / (k_tan * 1e-3) / 1e12 / FP64_DFMA_TFLOPS,
+                             "peak_source": "measured DFMA loop on this GB300 (FP64 pipe probe)",
                              "fp64_pipe_active_frac": FP64_PIPE_ACTIVE_C2,
                              "note": "the canonical count leaves out geometry, the C33 sub-iterations and their "
                                      "derivatives; fp64_pipe_active_frac is sm__pipe_fp64_cycles_active of one "
-                                     "k_elem_tangent launch on C2 (ncu --set full)"},
-        "kernels_ms": dict(zip(names, kms)),
+                                     "k_elem_tangent launch on C2 (ncu)"},
+        "kernels_ms": dict(zip(KERNELS_FP64, kms)),
         "residual_only": {"ms_per_step": sum(r_ms) / len(r_ms), "elems_per_s": ne / (sum(r_ms) / len(r_ms) * 1e-3)},
         "e2e": {"value": whole_job_rate(world, ne, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 8 * sh.n_dof,
                 "d2h_bytes_per_step": 8 * sh.n_dof + 72 * sh.nnzb, "host_equals_device_R": same},
         "fp32_bulk": {"ms_per_step": f32_step, "elems_per_s": world * ne / (f32_step * 1e-3),
                       "speedup_vs_fp64": ms / f32_step,
-                      "K_frobenius_rel_err_vs_fp64": fp32_frob, "R_max_abs_diff_vs_fp64": fp32_rdiff,
-                      "kernels_ms": dict(zip(["positions", "elem_residual_fp64", "elem_tangent_fp32", "node_gather",
-                                              "block_gather_fp32", "scale"], (k32 / max(c32, 1)).tolist())),
+                      "K_frobenius_rel_err_vs_fp64": fp32_frob, "R_rel_err_vs_fp64": fp32_rrel,
+                      "kernels_ms": dict(zip(KERNELS_FP32, (k32 / max(c32, 1)).tolist())),
                       "roofline_hbm_frac": (b_alg - 36 * sh.nnzb) / (f32_step * 1e-3) / 1e9 / hbm_peak,
                       "e2e": e2e32,
-                      "note": "residual FP64, tangent FP32 on patch-local shifted coordinates, K values FP32"},
+                      "note": "residual in float-float arithmetic on the FP32 pipe (about 48 bits), node sums FP64; "
+                              "tangent FP32 on patch-local shifted coordinates; K values FP32"},
         "gpu_launches": n_launch_jac * args.steps,
         "clocks": clk,
     }
