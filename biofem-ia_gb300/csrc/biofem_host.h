@@ -24,6 +24,8 @@ constexpr int kNumTables = 11;    /* 0 = regular 12-node patch, v = 3..10 irregu
 constexpr int kDeStride = 240;    /* per-element tangent block: D = df/dy (15 x 15, row-major), */
 constexpr int kDePres = 225;      /* then the three follower-pressure corner vectors (9) */
 constexpr int kMaxRowBlocks = 1023;   /* tangent blocks per row the row assembly handles (10-bit slot targets) */
+constexpr int kRowRec = 20;           /* ints per row-assembly record (80 bytes, 16-byte aligned) */
+constexpr unsigned kRowSlotGhost = 1u << 31;   /* record slot target of a ghost slot: three packed parents */
 
 /* Topology in IBMNodes layout (see topology.cpp). */
 struct HostTopo {
@@ -74,6 +76,7 @@ struct DevMesh {
   /* residual gather lists */
   const int *rptr, *ridx;    /* nt+1, into fb scratch (slot*3*ne + e) */
   const int *rcon;           /* the same contributions as e | slot << 27 (row assembly of the tangent) */
+  const int *rrec;           /* kRowRec ints per contribution: e | slot << 27, einfo, ecorner, 0, slot targets */
   const int *pptr, *pidx;    /* nt+1, elements whose corner is the node */
   /* tangent pattern */
   const int *rowptr, *colind;   /* BSR pattern, columns sorted per row */
@@ -107,6 +110,7 @@ int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double 
 int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, bool colmajor, void *stream);
 int row_assemble_configure(int maxblk, bool f32);   /* dynamic shared memory of the row assembly */
 size_t row_assemble_smem(int maxblk, bool f32);
+int row_assemble_max_blocks(bool f32);             /* blocks per row each row assembly handles */
 int launch_scale(const DevMesh &m, const KParams &p, double *R, void *stream);
 int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);
 int launch_elem_residual_ff(const DevMesh &m, const KParams &p, void *stream);

@@ -376,6 +376,44 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   return 0;
 }
 
+/* Row-assembly records, one per contribution c of a free row i (kRowRec
+   ints): the contribution (e | a << 27), einfo[e], ecorner[e], 0, then for
+   each patch slot b < nen of e the block of row i it adds to: the block's
+   position in the row's sorted columns, or for a ghost slot the positions
+   of its parents nv2, nv1, nv3 (10 bits each) with kRowSlotGhost set.  They
+   depend on the topology only, so the row assembly reads them instead of
+   searching the row's columns on every call.  Rows with an identity block
+   (clamped, ghost) get zero records; the row assembly does not read them. */
+static void build_row_records(const BiofemGpuMesh *m, const std::vector<int> &einfo, const std::vector<int> &ecorner,
+                              const std::vector<unsigned char> &rowkind, const std::vector<int> &rptr,
+                              const std::vector<int> &rcon, std::vector<int> &rrec)
+{
+  const HostTopo &T = m->topo;
+  const int nv = T.n_v, nt = T.n_v + T.n_ghosts;
+  rrec.assign((size_t)kRowRec * rptr[nt], 0);
+  for (int i = 0; i < nt; i++) {
+    if (rowkind[i] != 0) continue;
+    const int *c0 = m->colind.data() + m->rowptr[i], *c1 = m->colind.data() + m->rowptr[i + 1];
+    auto pos = [&](int node) { return (unsigned)(std::lower_bound(c0, c1, node) - c0); };
+    for (int c = rptr[i]; c < rptr[i + 1]; c++) {
+      const int e = rcon[c] & ((1 << 27) - 1), nen = einfo[e] & 0xff;
+      int *r = &rrec[(size_t)kRowRec * c];
+      r[0] = rcon[c]; r[1] = einfo[e]; r[2] = ecorner[e]; r[3] = 0;
+      for (int b = 0; b < nen; b++) {
+        const int node = T.patch[16 * (size_t)e + b];
+        unsigned sl;
+        if (node < nv) {
+          sl = pos(node);
+        } else {
+          const int g = node - nv;
+          sl = kRowSlotGhost | pos(T.ghost_nv2[g]) | (pos(T.ghost_nv1[g]) << 10) | (pos(T.ghost_nv3[g]) << 20);
+        }
+        r[4 + b] = (int)sl;
+      }
+    }
+  }
+}
+
 static int check_params(const BiofemParams &p)
 {
   if (p.n_qp < 1 || p.n_qp > kMaxQp) return fail(63, "n_qp must be between 1 and 6");
@@ -523,9 +561,18 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3);
   UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(rcon, rcon); UP(pptr, pptr); UP(pidx, pidx);
   UP(rowptr, m->rowptr); UP(colind, m->colind);
+  {
+    std::vector<int> rrec;
+    build_row_records(m, einfo, ecorner, rowkind, rptr, rcon, rrec);
+    UP(rrec, rrec);
+  }
 #undef UP
   dm.nnzb = m->nnzb;
   dm.maxblk = m->maxblk;
+  if (m->maxblk > row_assemble_max_blocks(params->precision != BIOFEM_FP64)) {
+    free_mesh(m);
+    return fail(63, "a tangent row has more blocks than the FP32 row assembly holds in registers");
+  }
   {
     cudaError_t ce = (cudaError_t)row_assemble_configure(m->maxblk, params->precision != BIOFEM_FP64);
     if (ce != cudaSuccess) { free_mesh(m); return fail(76, std::string("row assembly configuration: ") + cudaGetErrorString(ce)); }

@@ -899,24 +899,54 @@ __device__ __forceinline__ void elem_forces_split_tl(const R y[15], const EPar<R
      w = (N[:,a] (x) I3)^T D          (3 x 15, w[15 i + k] = sum_r N[r][a] D[3r+i][k]),
      K_ab[i][j] = sum_s N[s][b] w[15 i + 3 s + j],
    plus, when a and b are corner slots of the triangle, the follower-pressure
-   block: the cross-product matrix of sc v_b, v_b the corner's vector. */
+   block: the cross-product matrix of sc v_b, v_b the corner's vector.
+   Both sums run over the five basis rows, so the operands are kept with that
+   index innermost, padded to 8, for vector loads: the table as
+   tabT[8 b + s] = N[s][b] and w as wT[8 (3 i + j) + s] = w[15 i + 3 s + j]. */
+constexpr int kRowPad = 8;
+
+/* five consecutive values from a 16-byte aligned address */
 template <class R>
-__host__ __device__ __forceinline__ R row_w_entry(const R *D, const R *tab, int a, int t)
+__host__ __device__ __forceinline__ void load5(const R *p, R v[5])
 {
-  const int i = t / 15, k = t - 15 * i;
+#ifdef __CUDA_ARCH__
+  if constexpr (sizeof(R) == 4) {
+    const float4 a = *reinterpret_cast<const float4 *>(p);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = p[4];
+  } else {
+    const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = p[4];
+  }
+#else
+  for (int k = 0; k < 5; k++) v[k] = p[k];
+#endif
+}
+
+/* Entry t < 45 of w for the row slot whose table column is tabT_a (= tabT +
+   8 a); *pos receives its place in wT. */
+template <class R>
+__host__ __device__ __forceinline__ R row_wt_entry(const R *D, const R *tabT_a, int t, int *pos)
+{
+  const int i = t / 15, k = t - 15 * i, s = k / 3, j = k - 3 * s;
+  R n[5];
+  load5(tabT_a, n);
   R acc = R(0);
 #pragma unroll
-  for (int r = 0; r < 5; r++) acc = fma(tab[r * 16 + a], D[(3 * r + i) * 15 + k], acc);
+  for (int r = 0; r < 5; r++) acc = fma(n[r], D[(3 * r + i) * 15 + k], acc);
+  *pos = kRowPad * (3 * i + j) + s;
   return acc;
 }
 
+/* acc + K_ab[i][j], q = 3 i + j, from wT_q = wT + 8 q and tabT_b = tabT + 8 b,
+   as one chain of fused multiply-adds. */
 template <class R>
-__host__ __device__ __forceinline__ R row_block_entry(const R *w, const R *tab, int b, int q)
+__host__ __device__ __forceinline__ R row_block_accum(const R *wT_q, const R *tabT_b, R acc)
 {
-  const int i = q / 3, j = q - 3 * i;
-  R acc = R(0);
+  R w[5], n[5];
+  load5(wT_q, w);
+  load5(tabT_b, n);
 #pragma unroll
-  for (int s = 0; s < 5; s++) acc = fma(tab[s * 16 + b], w[15 * i + 3 * s + j], acc);
+  for (int s = 0; s < 5; s++) acc = fma(n[s], w[s], acc);
   return acc;
 }
 

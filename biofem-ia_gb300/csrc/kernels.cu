@@ -580,7 +580,7 @@ __global__ void k_node_gather(DevMesh m, KParams p, const double *__restrict__ x
    (main.c:1020-1026; k_node_gather, launched before, found the max); with
    colmajor each 3x3 block is stored column by column. */
 constexpr int kRowWarps = 4;
-constexpr unsigned kSlotGhost = 1u << 31;
+constexpr int kRowChunk = 4;          /* contributions whose slots and w are formed together */
 
 __device__ __forceinline__ int row_find(const int *cols, int nb, int node)
 {
@@ -592,30 +592,50 @@ __device__ __forceinline__ int row_find(const int *cols, int nb, int node)
   return lo;
 }
 
+__host__ __device__ __forceinline__ size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+/* one warp's shared buffers; every part starts on 16 bytes */
 template <class R> struct RowAsmBuf {
-  R *acc, *comp, *w, *gv;
-  int *cols;
-  unsigned *slot;
+  R *acc, *comp;      /* the row's 9 nb block values (and their compensations, FP32) */
+  R *wT;              /* kRowChunk x 9 x 8: w of each contribution of the chunk */
+  R *gv;              /* 9 x 16 values of the ghost slots of one contribution */
+  int *cols;          /* the row's block columns */
+  int *rec;           /* kRowChunk row-assembly records (kRowRec ints each) */
 };
+
+__host__ __device__ __forceinline__ size_t row_buf_bytes(int maxblk, size_t rsize)
+{
+  const size_t nacc = 9 * (size_t)maxblk * (rsize == 4 ? 2 : 1);
+  return align16(nacc * rsize) + kRowChunk * 9 * kRowPad * rsize + 144 * rsize + align16(4 * (size_t)maxblk) +
+         kRowChunk * kRowRec * 4;
+}
 
 template <class R>
 __device__ __forceinline__ RowAsmBuf<R> row_buf(unsigned char *base, int maxblk)
 {
   RowAsmBuf<R> b;
+  const size_t nacc = 9 * (size_t)maxblk;
   b.acc = reinterpret_cast<R *>(base);
-  b.comp = b.acc + 9 * maxblk;
-  b.w = b.comp + (sizeof(R) == 4 ? 9 * maxblk : 0);
-  b.gv = b.w + 48;
-  b.cols = reinterpret_cast<int *>(b.gv + 144);
-  b.slot = reinterpret_cast<unsigned *>(b.cols + maxblk);
+  b.comp = b.acc + nacc;
+  unsigned char *q = base + align16(nacc * (sizeof(R) == 4 ? 2 : 1) * sizeof(R));
+  b.wT = reinterpret_cast<R *>(q);
+  q += kRowChunk * 9 * kRowPad * sizeof(R);
+  b.gv = reinterpret_cast<R *>(q);
+  q += 144 * sizeof(R);
+  b.cols = reinterpret_cast<int *>(q);
+  q += align16(4 * (size_t)maxblk);
+  b.rec = reinterpret_cast<int *>(q);
   return b;
 }
 
-/* bytes of one warp's buffers (kept a multiple of 16) */
-__host__ __device__ __forceinline__ size_t row_buf_bytes(int maxblk, size_t rsize)
+/* The records of the contributions [cb, cb + kRowChunk) of a row ending at
+   c1, one 16-byte piece per lane (lanes < 5 np); zero past the row. */
+static_assert(kRowRec % 4 == 0 && (kRowRec / 4) * kRowChunk <= 32, "a chunk's records must fit one piece per lane");
+__device__ __forceinline__ int4 row_rec_load(const int *rrec, int cb, int c1, int lane)
 {
-  const size_t nr = 9 * (size_t)maxblk * (rsize == 4 ? 2 : 1) + 48 + 144;
-  return ((nr * rsize + 4 * (size_t)maxblk + 64) + 15) & ~(size_t)15;
+  const int np = min(kRowChunk, c1 - cb);
+  if (np <= 0 || lane >= (kRowRec / 4) * np) return make_int4(0, 0, 0, 0);
+  return __ldg(reinterpret_cast<const int4 *>(rrec) + (size_t)(kRowRec / 4) * cb + lane);
 }
 
 template <class R>
@@ -631,19 +651,32 @@ __device__ __forceinline__ void row_add(R *acc, R *comp, int idx, R v)
   }
 }
 
+/* The row's contributions are taken kRowChunk at a time: one pass forms the
+   slot targets of all their patch slots (a binary search in the row's block
+   columns; a ghost slot packs its three parents' targets), one pass forms
+   all their w (45 values each, so the chunk's D loads are in flight
+   together), then the contributions are added one after another in element
+   order: lane t of 9 nen takes block b = t / 9, entry q = t % 9.  FP64
+   values are fused into the block accumulator (acc + sum_s N[s][b] wT[q][s]
+   as one FMA chain), FP32 values are formed alone and added with Kahan
+   compensation; a ghost slot's values go to its parents after the real
+   slots, in slot order. */
 template <class R>
 __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KParams p, const R *__restrict__ De,
                                                                  const R *__restrict__ ntab, R psc, R *__restrict__ K,
                                                                  int maxblk, int colmajor)
 {
   extern __shared__ __align__(16) unsigned char row_smem[];
-  R *tabs = reinterpret_cast<R *>(row_smem);
-  for (int t = threadIdx.x; t < kNumTables * 80; t += blockDim.x) tabs[t] = ntab[t];
+  R *tabsT = reinterpret_cast<R *>(row_smem);       /* kNumTables x 16 x 8: N[s][b] at 8 b + s */
+  for (int t = threadIdx.x; t < kNumTables * 16 * kRowPad; t += blockDim.x) {
+    const int tb = t / (16 * kRowPad), r = t - tb * 16 * kRowPad, b = r / kRowPad, sidx = r - b * kRowPad;
+    tabsT[t] = sidx < 5 ? ntab[tb * 80 + sidx * 16 + b] : R(0);
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int i = blockIdx.x * kRowWarps + wid;
   if (i >= p.nt) return;
-  RowAsmBuf<R> B = row_buf<R>(row_smem + ((kNumTables * 80 * sizeof(R) + 15) & ~(size_t)15) +
+  RowAsmBuf<R> B = row_buf<R>(row_smem + align16(kNumTables * 16 * kRowPad * sizeof(R)) +
                               (size_t)wid * row_buf_bytes(maxblk, sizeof(R)), maxblk);
   const int k0 = m.rowptr[i], nb = m.rowptr[i + 1] - k0;
   const int kind = m.rowkind[i];
@@ -660,65 +693,69 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
     B.acc[t] = R(0);
     if constexpr (sizeof(R) == 4) B.comp[t] = R(0);
   }
-  __syncwarp();
+  const bool pres_live = p.pressure != 0.0 && !p.pres_dead;
   const int c1 = m.rptr[i + 1];
-  for (int c = m.rptr[i]; c < c1; c++) {
-    const int rc = m.rcon[c];
-    const int e = rc & ((1 << 27) - 1), a = rc >> 27;
-    const int info = m.einfo[e];
-    const int nen = info & 0xff;
-    const R *tab = tabs + (info >> 8) * 80;
-    const R *D = De + (size_t)kDeStride * e;
-    /* where each patch slot lands in this row: lane b < nen */
-    bool ghost = false;
-    if (lane < nen) {
-      const int node = m.patch[16 * (size_t)e + lane];
-      unsigned s;
-      if (node < p.nv) {
-        s = (unsigned)row_find(B.cols, nb, node);
-      } else {
-        const int g = node - p.nv;
-        const int q2 = row_find(B.cols, nb, m.ghost3[3 * g + 1]), q1 = row_find(B.cols, nb, m.ghost3[3 * g]);
-        const int q3 = row_find(B.cols, nb, m.ghost3[3 * g + 2]);
-        s = kSlotGhost | (unsigned)q2 | ((unsigned)q1 << 10) | ((unsigned)q3 << 20);
-        ghost = true;
-      }
-      B.slot[lane] = s;
-    }
-    const unsigned gmask = __ballot_sync(0xffffffffu, ghost);
-    /* w = (N[:,a] (x) I3)^T D: 45 values, w[15 i + k] = sum_r N[r][a] D[3r+i][k] */
-    for (int t = lane; t < 45; t += 32) B.w[t] = row_w_entry(D, tab, a, t);
-    /* pressure blocks: rows and columns at the triangle's corner slots */
-    const int cs = m.ecorner[e];
-    const int cslot0 = cs & 31, cslot1 = (cs >> 5) & 31, cslot2 = (cs >> 10) & 31;
-    const bool acorner = p.pressure != 0.0 && !p.pres_dead && (a == cslot0 || a == cslot1 || a == cslot2);
-    __syncwarp();
-    for (int t = lane; t < 9 * nen; t += 32) {
-      const int b = t / 9, q = t - 9 * b;
-      R v = row_block_entry(B.w, tab, b, q);
-      if (acorner) {
-        const int kc = b == cslot0 ? 0 : (b == cslot1 ? 1 : (b == cslot2 ? 2 : -1));
-        if (kc >= 0) v += skew_entry(q / 3, q % 3, D + kDePres + 3 * kc, psc);
-      }
-      const unsigned s = B.slot[b];
-      if (!(s & kSlotGhost)) row_add(B.acc, B.comp, 9 * (int)s + q, v);
-      else B.gv[t] = v;
+  int4 nrec = row_rec_load(m.rrec, m.rptr[i], c1, lane);
+  for (int cb = m.rptr[i]; cb < c1; cb += kRowChunk) {
+    const int np = min(kRowChunk, c1 - cb);
+    if (lane < (kRowRec / 4) * np) reinterpret_cast<int4 *>(B.rec)[lane] = nrec;
+    nrec = row_rec_load(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
+    __syncwarp();   /* also orders the cols / acc set-up and the previous chunk's reads */
+    /* w of the chunk: lane u -> contribution u / 45, entry u % 45 */
+    for (int u = lane; u < 45 * np; u += 32) {
+      const int pc = u / 45, t = u - 45 * pc;
+      const int *rc = B.rec + kRowRec * pc;
+      const int e = rc[0] & ((1 << 27) - 1), a = rc[0] >> 27, info = rc[1];
+      int pos;
+      const R v = row_wt_entry(De + (size_t)kDeStride * e, tabsT + (info >> 8) * 16 * kRowPad + kRowPad * a, t, &pos);
+      B.wT[9 * kRowPad * pc + pos] = v;
     }
     __syncwarp();
-    /* ghost slots, in slot order: lane 9k + q adds to entry q of parent k */
-    for (unsigned gm = gmask; gm; gm &= gm - 1) {
-      const int b = __ffs(gm) - 1;
-      if (lane < 27) {
-        const int k = lane / 9, q = lane - 9 * k;
-        const unsigned s = B.slot[b];
-        const int pos = (int)((s >> (10 * k)) & 1023u);
-        const R v = B.gv[9 * b + q];
-        row_add(B.acc, B.comp, 9 * pos + q, k == 2 ? -v : v);
+    for (int pc = 0; pc < np; pc++) {
+      const int *rc = B.rec + kRowRec * pc;
+      const int e = rc[0] & ((1 << 27) - 1), a = rc[0] >> 27, info = rc[1], cs = rc[2];
+      const int nen = info & 0xff;
+      const R *tabT = tabsT + (info >> 8) * 16 * kRowPad;
+      const R *wT = B.wT + 9 * kRowPad * pc;
+      const unsigned *slot = reinterpret_cast<const unsigned *>(rc + 4);
+      const int cslot0 = cs & 31, cslot1 = (cs >> 5) & 31, cslot2 = (cs >> 10) & 31;
+      const bool acorner = pres_live && (a == cslot0 || a == cslot1 || a == cslot2);
+      const bool ghost_lane = lane < nen && (slot[lane] & kRowSlotGhost);
+      const unsigned gmask = __ballot_sync(0xffffffffu, ghost_lane);
+      for (int t = lane; t < 9 * nen; t += 32) {
+        const int b = t / 9, q = t - 9 * b;
+        const unsigned sl = slot[b];
+        const bool ghost = (sl & kRowSlotGhost) != 0;
+        const int idx = 9 * (int)(sl & 1023u) + q;
+        R v;
+        if constexpr (sizeof(R) == 8) v = row_block_accum(wT + kRowPad * q, tabT + kRowPad * b, ghost ? R(0) : B.acc[idx]);
+        else v = row_block_accum(wT + kRowPad * q, tabT + kRowPad * b, R(0));
+        if (acorner) {
+          const int kc = b == cslot0 ? 0 : (b == cslot1 ? 1 : (b == cslot2 ? 2 : -1));
+          if (kc >= 0) v += skew_entry(q / 3, q % 3, De + (size_t)kDeStride * e + kDePres + 3 * kc, psc);
+        }
+        if (ghost) B.gv[t] = v;
+        else if constexpr (sizeof(R) == 8) B.acc[idx] = v;
+        else row_add(B.acc, B.comp, idx, v);
+      }
+      if (gmask) {
+        __syncwarp();
+        /* ghost slots, in slot order: lane 9k + q adds to entry q of parent k */
+        for (unsigned gm = gmask; gm; gm &= gm - 1) {
+          const int b = __ffs(gm) - 1;
+          if (lane < 27) {
+            const int k = lane / 9, q = lane - 9 * k;
+            const int pos = (int)((slot[b] >> (10 * k)) & 1023u);
+            const R v = B.gv[9 * b + q];
+            row_add(B.acc, B.comp, 9 * pos + q, k == 2 ? -v : v);
+          }
+          __syncwarp();
+        }
       }
       __syncwarp();
     }
-    __syncwarp();   /* slot targets and w are rewritten by the next contribution */
   }
+  __syncwarp();
   /* dynamic term diagonal, scale, write-out */
   const double fmax = __longlong_as_double((long long)*m.fmax);
   const R sc = fmax > 1.0 ? R(1.0 / fmax) : R(1);
@@ -731,6 +768,197 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
       if constexpr (sizeof(R) == 4) v = (R)((double)v * (1.0 / fmax)); else v = v * sc;
     }
     Kr[colmajor ? t - q + 3 * (q % 3) + q / 3 : t] = v;
+  }
+}
+
+/* FP32 row assembly with the row's blocks in registers: lane k owns block
+   base + k of the row (base = 0, then 32 for the rare rows of more than 32
+   blocks, which repeat the contribution loop), holding its 9 values and
+   their Kahan compensations.  Per chunk of kRowChunk contributions: slot
+   targets and an inverse map (owned block -> real patch slot) in shared
+   memory, then w of each contribution (lane t and t + 32 of its 45 entries,
+   index arithmetic done once per row); each contribution's block values are
+   formed by the lane that owns the block (N[.][b] from the table, the 9 x 5
+   values of w read by every lane at once) and fused into a per-chunk partial
+   sum; a ghost slot's values go to the lanes owning its parents, after the
+   real slots, in slot order.  The partial sums are added into the row with
+   Kahan compensation once per chunk, in element order. */
+constexpr int kRowRegMax = 64;
+
+struct RowRegBuf {
+  float *wT;          /* kRowChunk x 9 x 8 */
+  float *stage;       /* 9 x 32 write-out staging */
+  int *cols;          /* kRowRegMax */
+  int *rec;           /* kRowChunk row-assembly records */
+  unsigned char *inv; /* kRowChunk x 32: real slot of each owned block, 255 none */
+};
+
+__host__ __device__ __forceinline__ size_t row_reg_bytes()
+{
+  return kRowChunk * 9 * kRowPad * 4 + 9 * 32 * 4 + kRowRegMax * 4 + kRowChunk * kRowRec * 4 + kRowChunk * 32;
+}
+
+__device__ __forceinline__ RowRegBuf row_reg_buf(unsigned char *q)
+{
+  RowRegBuf b;
+  b.wT = reinterpret_cast<float *>(q);
+  q += kRowChunk * 9 * kRowPad * 4;
+  b.stage = reinterpret_cast<float *>(q);
+  q += 9 * 32 * 4;
+  b.cols = reinterpret_cast<int *>(q);
+  q += kRowRegMax * 4;
+  b.rec = reinterpret_cast<int *>(q);
+  q += kRowChunk * kRowRec * 4;
+  b.inv = q;
+  return b;
+}
+
+/* tmp[q] += sum_s N[s] wT[8 q + s] for the nine entries of one block */
+__device__ __forceinline__ void row_reg_block(const float *wT, const float n[5], float tmp[9])
+{
+#pragma unroll
+  for (int q = 0; q < 9; q++) tmp[q] = row_block_accum(wT + kRowPad * q, n, tmp[q]);
+}
+
+__global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh m, KParams p, const float *__restrict__ De,
+                                                                     const float *__restrict__ ntab, float psc,
+                                                                     float *__restrict__ K, int colmajor)
+{
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  float *tabsT = reinterpret_cast<float *>(row_smem);
+  for (int t = threadIdx.x; t < kNumTables * 16 * kRowPad; t += blockDim.x) {
+    const int tb = t / (16 * kRowPad), r = t - tb * 16 * kRowPad, b = r / kRowPad, sidx = r - b * kRowPad;
+    tabsT[t] = sidx < 5 ? ntab[tb * 80 + sidx * 16 + b] : 0.f;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int i = blockIdx.x * kRowWarps + wid;
+  if (i >= p.nt) return;
+  RowRegBuf B = row_reg_buf(row_smem + align16(kNumTables * 16 * kRowPad * 4) + (size_t)wid * row_reg_bytes());
+  const int k0 = m.rowptr[i], nb = m.rowptr[i + 1] - k0;
+  float *Kr = K + 9 * (size_t)k0;
+  if (m.rowkind[i] != 0) {   /* clamped and ghost rows: identity */
+    for (int t = lane; t < 9 * nb; t += 32) {
+      const int q = t % 9;
+      Kr[t] = (m.colind[k0 + t / 9] == i && (q == 0 || q == 4 || q == 8)) ? 1.f : 0.f;
+    }
+    return;
+  }
+  for (int t = lane; t < nb; t += 32) B.cols[t] = m.colind[k0 + t];
+  __syncwarp();
+  /* the two w entries of this lane: t0 = lane, t1 = lane + 32 (< 45) */
+  const int wi0 = lane / 15, wk0 = lane - 15 * wi0;
+  const int wpos0 = kRowPad * (3 * wi0 + wk0 % 3) + wk0 / 3, wd0 = wi0 * 15 + wk0;
+  const int t1 = lane + 32, wi1 = t1 / 15, wk1 = t1 - 15 * wi1;
+  const int wpos1 = kRowPad * (3 * wi1 + wk1 % 3) + wk1 / 3, wd1 = wi1 * 15 + wk1;
+  const bool has1 = t1 < 45;
+  const bool pres_live = p.pressure != 0.0 && !p.pres_dead;
+  const int pd = row_find(B.cols, nb, i);
+  const double fmax = __longlong_as_double((long long)*m.fmax);
+  for (int base = 0; base < nb; base += 32) {
+    float acc[9], comp[9], tmp[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) { acc[q] = 0.f; comp[q] = 0.f; }
+    const int k = base + lane;
+    const int c1 = m.rptr[i + 1];
+    int4 nrec = row_rec_load(m.rrec, m.rptr[i], c1, lane);
+    for (int cb = m.rptr[i]; cb < c1; cb += kRowChunk) {
+      const int np = min(kRowChunk, c1 - cb);
+      if (lane < (kRowRec / 4) * np) reinterpret_cast<int4 *>(B.rec)[lane] = nrec;
+      nrec = row_rec_load(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
+      for (int u = lane; u < kRowChunk * 8; u += 32) reinterpret_cast<unsigned *>(B.inv)[u] = 0xffffffffu;
+      __syncwarp();
+      /* inverse map: owned block -> real slot (lane u -> contribution u / 16, slot u % 16) */
+      for (int u = lane; u < 16 * np; u += 32) {
+        const int pc = u >> 4, b = u & 15;
+        const int *rc = B.rec + kRowRec * pc;
+        const unsigned sl = (unsigned)rc[4 + b];
+        if (b < (rc[1] & 0xff) && !(sl & kRowSlotGhost) && sl >= (unsigned)base && sl < (unsigned)base + 32)
+          B.inv[32 * pc + sl - base] = (unsigned char)b;
+      }
+      for (int pc = 0; pc < np; pc++) {
+        const int *rc = B.rec + kRowRec * pc;
+        const int e = rc[0] & ((1 << 27) - 1), a = rc[0] >> 27, info = rc[1];
+        const float *D = De + (size_t)kDeStride * e;
+        float n[5];
+        load5(tabsT + (info >> 8) * 16 * kRowPad + kRowPad * a, n);
+        float v0 = 0.f, v1 = 0.f;
+#pragma unroll
+        for (int r = 0; r < 5; r++) v0 = fmaf(n[r], __ldg(D + 45 * r + wd0), v0);
+        B.wT[9 * kRowPad * pc + wpos0] = v0;
+        if (has1) {
+#pragma unroll
+          for (int r = 0; r < 5; r++) v1 = fmaf(n[r], __ldg(D + 45 * r + wd1), v1);
+          B.wT[9 * kRowPad * pc + wpos1] = v1;
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < 9; q++) tmp[q] = 0.f;
+      for (int pc = 0; pc < np; pc++) {
+        const int *rc = B.rec + kRowRec * pc;
+        const int a = rc[0] >> 27, info = rc[1], cs = rc[2];
+        const int nen = info & 0xff;
+        const float *tabT = tabsT + (info >> 8) * 16 * kRowPad;
+        const float *wT = B.wT + 9 * kRowPad * pc;
+        const unsigned *slot = reinterpret_cast<const unsigned *>(rc + 4);
+        const int b = B.inv[32 * pc + lane];
+        if (b != 255) {
+          float n[5];
+          load5(tabT + kRowPad * b, n);
+          row_reg_block(wT, n, tmp);
+          const int cslot0 = cs & 31, cslot1 = (cs >> 5) & 31, cslot2 = (cs >> 10) & 31;
+          if (pres_live && (a == cslot0 || a == cslot1 || a == cslot2)) {
+            const int kc = b == cslot0 ? 0 : (b == cslot1 ? 1 : (b == cslot2 ? 2 : -1));
+            if (kc >= 0) {
+              const float *vv = De + (size_t)kDeStride * (rc[0] & ((1 << 27) - 1)) + kDePres + 3 * kc;
+#pragma unroll
+              for (int q = 0; q < 9; q++) tmp[q] += skew_entry(q / 3, q % 3, vv, psc);
+            }
+          }
+        }
+        /* ghost slots, in slot order: the owners of the three parents add +, +, - */
+        const bool ghost_lane = lane < nen && (slot[lane] & kRowSlotGhost);
+        for (unsigned gm = __ballot_sync(0xffffffffu, ghost_lane); gm; gm &= gm - 1) {
+          const int gb = __ffs(gm) - 1;
+          const unsigned sl = slot[gb];
+          const int pos0 = (int)(sl & 1023u), pos1 = (int)((sl >> 10) & 1023u), pos2 = (int)((sl >> 20) & 1023u);
+          if (k == pos0 || k == pos1 || k == pos2) {
+            float n[5], v[9];
+            load5(tabT + kRowPad * gb, n);
+#pragma unroll
+            for (int q = 0; q < 9; q++) v[q] = 0.f;
+            row_reg_block(wT, n, v);
+            const float sg = k == pos2 ? -1.f : 1.f;
+#pragma unroll
+            for (int q = 0; q < 9; q++) tmp[q] = fmaf(sg, v[q], tmp[q]);
+          }
+        }
+      }
+      /* the chunk's partial sums into the row, compensated */
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        const float y = tmp[q] - comp[q];
+        const float t = acc[q] + y;
+        comp[q] = (t - acc[q]) - y;
+        acc[q] = t;
+      }
+      __syncwarp();   /* meta, slot, inv and wT are rewritten by the next chunk */
+    }
+    /* dynamic term diagonal, scale, write-out staged through shared memory */
+    if (k < nb) {
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        float v = acc[q];
+        if (p.dyn && k == pd && (q == 0 || q == 4 || q == 8)) v += (float)m.dyn_diag[i];
+        if (fmax > 1.0) v = (float)((double)v * (1.0 / fmax));
+        B.stage[9 * lane + (colmajor ? 3 * (q % 3) + q / 3 : q)] = v;
+      }
+    }
+    __syncwarp();
+    const int nw = 9 * min(32, nb - base);
+    for (int t = lane; t < nw; t += 32) Kr[9 * base + t] = B.stage[t];
+    __syncwarp();
   }
 }
 
@@ -884,17 +1112,19 @@ int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, doub
 
 size_t row_assemble_smem(int maxblk, bool f32)
 {
-  const size_t rs = f32 ? sizeof(float) : sizeof(double);
-  return ((kNumTables * 80 * rs + 15) & ~(size_t)15) + kRowWarps * row_buf_bytes(maxblk, rs);
+  if (f32) return align16(kNumTables * 16 * kRowPad * 4) + kRowWarps * row_reg_bytes();
+  return align16(kNumTables * 16 * kRowPad * 8) + kRowWarps * row_buf_bytes(maxblk, 8);
 }
+
+int row_assemble_max_blocks(bool f32) { return f32 ? kRowRegMax : kMaxRowBlocks; }
 
 int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, bool colmajor, void *stream)
 {
   const int grid = blocks_for(p.nt, kRowWarps);
   const size_t smem = row_assemble_smem(m.maxblk, f32);
   if (f32)
-    k_row_assemble<float><<<grid, 32 * kRowWarps, smem, (cudaStream_t)stream>>>(
-        m, p, m.DeF, m.ntabF, -p.pres6f, static_cast<float *>(K), m.maxblk, (int)colmajor);
+    k_row_assemble_f32<<<grid, 32 * kRowWarps, smem, (cudaStream_t)stream>>>(
+        m, p, m.DeF, m.ntabF, -p.pres6f, static_cast<float *>(K), (int)colmajor);
   else
     k_row_assemble<double><<<grid, 32 * kRowWarps, smem, (cudaStream_t)stream>>>(
         m, p, m.De, m.ntab, -p.pressure / 6.0, static_cast<double *>(K), m.maxblk, (int)colmajor);
@@ -904,7 +1134,7 @@ int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, b
 int row_assemble_configure(int maxblk, bool f32)
 {
   const size_t smem = row_assemble_smem(maxblk, f32);
-  cudaError_t e = f32 ? cudaFuncSetAttribute(k_row_assemble<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+  cudaError_t e = f32 ? cudaFuncSetAttribute(k_row_assemble_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                       : cudaFuncSetAttribute(k_row_assemble<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return (int)e;
 }

@@ -1,5 +1,5 @@
-"""Build recipe for oracle/_ref/libbiofem_ref.so and oracle/_ref/libbiofem_ref_dyn.so
-(TEST INFRASTRUCTURE ONLY).
+"""Build recipe for oracle/_ref/libbiofem_ref.so, oracle/_ref/libbiofem_ref_dyn.so
+and oracle/_ref/ref_cuda_kernel.cubin (TEST INFRASTRUCTURE ONLY).
 
 libbiofem_ref.so compiles the reference's own, unmodified hot-path C files
 where they lie (``<reference>/src/{active_strain,math,bending,io,external}.c``)
@@ -10,7 +10,11 @@ driver is compiled with -DREF_DRIVER_WITH_MAIN so that main.c's globals are
 the ones used, and every external that main.c names but the dynamic term
 never calls (SNES, DMPlex setup, LV mesh loaders, CUDA / Kokkos bridges, ...)
 is resolved by an abort stub generated here from the linker's list of
-undefined references.  The results are the checkers that pin the restated
+undefined references.  ref_cuda_kernel.cubin is the device code of the
+reference's own GPU kernels (src/cuda_kernel.cu: SubdivGeomKernel_,
+MetricTensorKernel_, ...) compiled unmodified for sm_103a against the
+petsc-lite headers; being device code only, it loads on any host
+(oracle/ref_cuda.py).  The results are the checkers that pin the restated
 oracle and generate tests/golden/.  They are built only where the reference
 sources exist; nothing on the product path links them.
 
@@ -30,6 +34,7 @@ REFERENCE = Path(os.environ.get("BIOFEM_REFERENCE_ROOT", "/root/reference"))
 OUT_DIR = HERE / "_ref"
 LIB = OUT_DIR / "libbiofem_ref.so"
 LIB_DYN = OUT_DIR / "libbiofem_ref_dyn.so"
+CUBIN = OUT_DIR / "ref_cuda_kernel.cubin"
 REF_SOURCES = ["active_strain.c", "math.c", "bending.c", "io.c", "external.c"]
 DYN_SOURCES = ["main.c", "material.c"]
 # -ffp-contract=off keeps every multiply and add separately rounded, so the
@@ -123,8 +128,33 @@ def build_dyn(force: bool = False, verbose: bool = False) -> Path | None:
     return LIB_DYN
 
 
+def build_cuda(force: bool = False, verbose: bool = False) -> Path | None:
+    """Compile the reference's src/cuda_kernel.cu (device code) into
+    ref_cuda_kernel.cubin for sm_103a; returns its path, or None without the
+    reference sources or nvcc."""
+    src = REFERENCE / "src" / "cuda_kernel.cu"
+    if not src.is_file():
+        return None
+    deps = [src, REFERENCE / "include" / "cuda_bridge.h", REFERENCE / "include" / "variables.h"]
+    deps += list((HERE / "petsc_lite").glob("*.h"))
+    if not force and not _stale(CUBIN, [d for d in deps if d.exists()]):
+        return CUBIN
+    OUT_DIR.mkdir(exist_ok=True)
+    cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-w",
+           "-I", str(HERE / "petsc_lite"), "-I", str(REFERENCE / "include"), str(src), "-o", str(CUBIN)]
+    if verbose:
+        print(" ".join(cmd))
+    try:
+        subprocess.run(cmd, check=True)
+    except FileNotFoundError:
+        return None
+    return CUBIN
+
+
 if __name__ == "__main__":
     p = build(force="--force" in sys.argv, verbose=True)
     print(p if p else "reference sources not present; nothing built")
     p = build_dyn(force="--force" in sys.argv, verbose=True)
     print(p if p else "reference sources not present; nothing built")
+    p = build_cuda(force="--force" in sys.argv, verbose=True)
+    print(p if p else "reference CUDA sources or nvcc not present; nothing built")

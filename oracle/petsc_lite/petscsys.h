@@ -24,6 +24,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <time.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -40,6 +41,16 @@ typedef int MPI_Comm;
 typedef int MPI_Datatype;
 typedef int MPI_Op;
 typedef void *PetscOptions;
+typedef double PetscLogDouble;
+
+/* wall-clock seconds (PETSc's PetscTime) */
+static inline PetscErrorCode PetscTime(PetscLogDouble *t)
+{
+  struct timespec ts_;
+  clock_gettime(CLOCK_MONOTONIC, &ts_);
+  *t = (PetscLogDouble)ts_.tv_sec + 1e-9 * (PetscLogDouble)ts_.tv_nsec;
+  return 0;
+}
 
 #define PETSC_SUCCESS 0
 #define PETSC_COMM_WORLD ((MPI_Comm)1)

@@ -1,5 +1,6 @@
-/* Host driver of the tangent contraction of the row assembly (row_w_entry,
-   row_block_entry and skew_entry in element.cuh) for
+/* Host driver of the tangent contraction of the row assembly (row_wt_entry,
+   row_block_accum and skew_entry in element.cuh, with their transposed
+   operand layouts) for
    tests/test_contraction_host.py: reads one case (nen, corner slots, pressure
    flag, D 15x15, the 5x16 basis table, the three corner vectors and the
    scale) from argv[1], forms every block (a, b) of the element matrix the way
@@ -18,18 +19,23 @@ template <class R>
 static void run(const double *Din, const double *tabin, int nen, const int cs[3], bool pres, const double *vvin,
                 double sc, double *out)
 {
-  std::vector<R> D(225), tab(80), w(45), ke((size_t)9 * nen * nen, R(NAN));
+  std::vector<R> D(225), tabT(16 * kRowPad, R(0)), wT(9 * kRowPad, R(0)), ke((size_t)9 * nen * nen, R(NAN));
   for (int i = 0; i < 225; i++) D[i] = (R)Din[i];
-  for (int i = 0; i < 80; i++) tab[i] = (R)tabin[i];
+  for (int s = 0; s < 5; s++)
+    for (int b = 0; b < 16; b++) tabT[kRowPad * b + s] = (R)tabin[16 * s + b];
   R vv[3][3];
   for (int k = 0; k < 3; k++)
     for (int d = 0; d < 3; d++) vv[k][d] = (R)vvin[3 * k + d];
   for (int a = 0; a < nen; a++) {
-    for (int t = 0; t < 45; t++) w[t] = row_w_entry(D.data(), tab.data(), a, t);
+    for (int t = 0; t < 45; t++) {
+      int pos = -1;
+      const R v = row_wt_entry(D.data(), tabT.data() + kRowPad * a, t, &pos);
+      wT[pos] = v;
+    }
     const bool acorner = pres && (a == cs[0] || a == cs[1] || a == cs[2]);
     for (int b = 0; b < nen; b++)
       for (int q = 0; q < 9; q++) {
-        R v = row_block_entry(w.data(), tab.data(), b, q);
+        R v = row_block_accum(wT.data() + kRowPad * q, tabT.data() + kRowPad * b, R(0));
         if (acorner)
           for (int k = 0; k < 3; k++)
             if (b == cs[k]) v += skew_entry(q / 3, q % 3, vv[k], (R)sc);
