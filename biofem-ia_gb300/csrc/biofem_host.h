@@ -75,8 +75,8 @@ struct DevMesh {
   const unsigned char *rowkind; /* nt: 0 free real row, 1 clamped row, 2 ghost row */
   /* residual gather lists */
   const int *rptr, *ridx;    /* nt+1, into fb scratch (slot*3*ne + e) */
-  const int *rcon;           /* the same contributions as e | slot << 27 (row assembly of the tangent) */
-  const int *rrec;           /* kRowRec ints per contribution: e | slot << 27, einfo, ecorner, 0, slot targets */
+  const int *rrec;           /* kRowRec ints per contribution (same order): e | slot << 27, einfo, ecorner, 0,
+                                the slot targets in the row (row assembly of the tangent) */
   const int *pptr, *pidx;    /* nt+1, elements whose corner is the node */
   /* tangent pattern */
   const int *rowptr, *colind;   /* BSR pattern, columns sorted per row */

@@ -127,11 +127,12 @@ int BiofemServeEstimateBytes(int32_t n_v, int32_t n_elmt, int32_t n_ghosts, int3
   const int m = gmres_restart > 0 ? gmres_restart : 30;
   /* per element: tangent block df/dy (240 values), forces, thickness-point
      metrics, primal geometry, resultants and C33 values (FP64; 3 points,
-     3 sub-iterations), reference constants, row-assembly lists; per node:
+     3 sub-iterations), reference constants, row-assembly lists and records
+     (80 bytes for each of the element's ~12 row contributions); per node:
      tangent row (~37 blocks), pattern, flexible-GMRES bases V and Z,
      multigrid hierarchy (FP32 copy of the tangent for FP64 handles, P, A P,
      the coarse operators) */
-  const int64_t per_elem = precision == BIOFEM_FP64 ? 6800 : 3500;
+  const int64_t per_elem = (precision == BIOFEM_FP64 ? 6800 : 3500) + 12 * 80;
   const int64_t per_node = (precision == BIOFEM_FP64 ? 3500 + 1400 : 2100) + (int64_t)(2 * m + 8) * 24 + 3450;
   *bytes = (per_elem * n_elmt + per_node * nt) * 5 / 4 + (8 << 20);
   return 0;
