@@ -38,12 +38,12 @@ for _p in (ROOT, ROOT / "biofem-ia_gb300"):
 METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
 # dram__bytes_read.sum + dram__bytes_write.sum per launch on the 256x192
 # workload, from one ncu capture of each kernel (profiles/, bytes)
-DRAM_BYTES_C2 = {"elem_residual": 60.592e6 + 193.185e6, "elem_tangent": 241.020e6 + 151.647e6,
-                 "row_assemble": 208.975e6 + 101.796e6, "elem_residual_ff": 59.962e6 + 3.430e6,
-                 "elem_tangent_fp32": 36.500e6 + 33.084e6, "row_assemble_fp32": 113.796e6 + 36.740e6}
+DRAM_BYTES_C2 = {"elem_residual": 60.582e6 + 193.670e6, "elem_tangent": 241.122e6 + 151.319e6,
+                 "row_assemble": 289.613e6 + 106.150e6, "elem_residual_ff": 59.959e6 + 3.388e6,
+                 "elem_tangent_fp32": 36.505e6 + 33.795e6, "row_assemble_fp32": 195.308e6 + 48.584e6}
 # sm__pipe_fp64_cycles_active (fraction of peak sustained active) per kernel
 # in the same captures
-FP64_PIPE_ACTIVE_C2 = {"elem_residual": 0.884, "elem_tangent": 0.873, "row_assemble": 0.911}
+FP64_PIPE_ACTIVE_C2 = {"elem_residual": 0.884, "elem_tangent": 0.872, "row_assemble": 0.937}
 # FP64 FMA throughput of this GB300, measured by the DFMA loop of the FP64 pipe
 # probe (biofem-ia_gb300/csrc/probe_fp64.cu): TFLOP/s
 FP64_DFMA_TFLOPS = 1.057
@@ -736,6 +736,8 @@ def run_ours(args):
                       "K_frobenius_rel_err_vs_fp64": fp32_frob, "R_rel_err_vs_fp64": fp32_rrel,
                       "kernels_ms": dict(zip(KERNELS_FP32, (k32 / max(c32, 1)).tolist())),
                       "roofline_hbm_frac": (b_alg - 36 * sh.nnzb) / (f32_step * 1e-3) / 1e9 / hbm_peak,
+                      "dominant_kernel": KERNELS_FP32[int(np.argmax(k32))],
+                      "dominant_kernel_traffic": DRAM_BYTES_C2.get(KERNELS_FP32[int(np.argmax(k32))]),
                       "e2e": e2e32,
                       "note": "residual in float-float arithmetic on the FP32 pipe (about 48 bits), node sums FP64; "
                               "tangent FP32 on patch-local shifted coordinates; K values FP32"},
