@@ -788,6 +788,7 @@ constexpr int kRowRegMax = 64;
 struct RowRegBuf {
   float *wT;          /* kRowChunk x 9 x 8 */
   float *stage;       /* 9 x 32 write-out staging */
+  float *comp;        /* 9 x 32 Kahan compensations of the owned blocks ([q][lane]) */
   int *cols;          /* kRowRegMax */
   int *rec;           /* kRowChunk row-assembly records */
   unsigned char *inv; /* kRowChunk x 32: real slot of each owned block, 255 none */
@@ -795,7 +796,7 @@ struct RowRegBuf {
 
 __host__ __device__ __forceinline__ size_t row_reg_bytes()
 {
-  return kRowChunk * 9 * kRowPad * 4 + 9 * 32 * 4 + kRowRegMax * 4 + kRowChunk * kRowRec * 4 + kRowChunk * 32;
+  return kRowChunk * 9 * kRowPad * 4 + 2 * 9 * 32 * 4 + kRowRegMax * 4 + kRowChunk * kRowRec * 4 + kRowChunk * 32;
 }
 
 __device__ __forceinline__ RowRegBuf row_reg_buf(unsigned char *q)
@@ -804,6 +805,8 @@ __device__ __forceinline__ RowRegBuf row_reg_buf(unsigned char *q)
   b.wT = reinterpret_cast<float *>(q);
   q += kRowChunk * 9 * kRowPad * 4;
   b.stage = reinterpret_cast<float *>(q);
+  q += 9 * 32 * 4;
+  b.comp = reinterpret_cast<float *>(q);
   q += 9 * 32 * 4;
   b.cols = reinterpret_cast<int *>(q);
   q += kRowRegMax * 4;
@@ -856,9 +859,9 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
   const int pd = row_find(B.cols, nb, i);
   const double fmax = __longlong_as_double((long long)*m.fmax);
   for (int base = 0; base < nb; base += 32) {
-    float acc[9], comp[9], tmp[9];
+    float acc[9], tmp[9];
 #pragma unroll
-    for (int q = 0; q < 9; q++) { acc[q] = 0.f; comp[q] = 0.f; }
+    for (int q = 0; q < 9; q++) { acc[q] = 0.f; B.comp[32 * q + lane] = 0.f; }
     const int k = base + lane;
     const int c1 = m.rptr[i + 1];
     int4 nrec = row_rec_load(m.rrec, m.rptr[i], c1, lane);
@@ -935,15 +938,16 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
           }
         }
       }
-      /* the chunk's partial sums into the row, compensated */
+      /* the chunk's partial sums into the row, compensated (each lane keeps its
+         own compensations; no other lane touches them) */
 #pragma unroll
       for (int q = 0; q < 9; q++) {
-        const float y = tmp[q] - comp[q];
+        const float y = tmp[q] - B.comp[32 * q + lane];
         const float t = acc[q] + y;
-        comp[q] = (t - acc[q]) - y;
+        B.comp[32 * q + lane] = (t - acc[q]) - y;
         acc[q] = t;
       }
-      __syncwarp();   /* meta, slot, inv and wT are rewritten by the next chunk */
+      __syncwarp();   /* records, inverse map and wT are rewritten by the next chunk */
     }
     /* dynamic term diagonal, scale, write-out staged through shared memory */
     if (k < nb) {
