@@ -118,6 +118,47 @@ C4 = LVWorkload("C4_lv_ellipsoid", 41, index=3)
 ALL = {w.name: w for w in (C1, C2, C3, C4)}
 
 
+@dataclass(frozen=True)
+class ConeWorkload:
+    """A flat disc with one interior vertex of the given valence (3..10; see
+    mesh.cone_disc): the one-step subdivision of every valence the
+    reference's tables cover, up to the 16-node patch.  Random fibre angle
+    and lambda_a, follower pressure, boundary ring clamped, a seeded smooth
+    bump and a seeded displacement of 1e-2 of the ring spacing."""
+    name: str
+    valence: int
+    rings: int = 5
+    index: int = 0
+    n_qp: int = 3
+    c33_iters: int = 3
+    pressure: float = 1e-3
+    z_sigma: float = 2e-3
+    disp_rel: float = 1e-2
+    basis: int = 0
+    tnormal: int = 0
+    dead_load: int = 0
+    iso_act: int = 0
+
+    @property
+    def seed(self) -> int:
+        return meshmod.SEED_BASE + self.index
+
+    def build_mesh(self) -> meshmod.Mesh:
+        m = meshmod.cone_disc(self.valence, self.rings, z_sigma=self.z_sigma, seed=self.seed)
+        meshmod.set_random_activation(m, self.seed + 1)
+        m.meta["workload"] = self.name
+        return m
+
+    def initial_x(self, m: meshmod.Mesh, xyz0_full: np.ndarray) -> np.ndarray:
+        return meshmod.initial_state(m, xyz0_full, disp_amp=self.disp_rel * m.meta["hmean"], seed=self.seed + 2)
+
+
+def cone(valence: int, **kw) -> ConeWorkload:
+    args = dict(index=60 + valence)
+    args.update(kw)
+    return ConeWorkload(f"cone_v{valence}", valence, **args)
+
+
 def small(nx: int, ny: int, **kw) -> Workload:
     """A small flat case for parity tests (z perturbed, smooth activation, displaced)."""
     args = dict(z_sigma=1e-3, activation="smooth", disp_rel=1e-2, index=10)

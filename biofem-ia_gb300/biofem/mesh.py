@@ -121,6 +121,64 @@ def flat_membrane(nx: int, ny: int, lx: float = 1.0, ly: float = 0.75,
                 meta=dict(kind="flat", nx=nx, ny=ny, lx=lx, ly=ly, z_sigma=z_sigma, seed=seed, z_smooth=z_smooth))
 
 
+def cone_disc(valence: int, rings: int, radius: float = 1.0, z_sigma: float = 0.0,
+              seed: int | None = None) -> Mesh:
+    """A flat disc whose centre vertex has `valence` triangles and every
+    other interior vertex six: `valence` sectors of a triangular lattice,
+    ring r (1..rings) holding valence * r vertices at radius r / rings, the
+    sector k spanning the angles [2 pi k / valence, 2 pi (k + 1) / valence).
+    Ring r and r + 1 are joined sector by sector with 2 r + 1 triangles
+    (valence * rings^2 triangles in all), counter-clockwise.  The single
+    boundary ring is the outer ring, counter-clockwise.  With valence 3..10
+    the centre's triangles take the one-step subdivision of that valence,
+    up to the 16-node patch of valence 10.  ``z_sigma`` > 0 adds a seeded
+    smooth bump a (1 - rho^2) cos(theta - phi) of peak z_sigma."""
+    if not 3 <= valence <= 10 or rings < 3:
+        raise ValueError("cone_disc needs valence 3..10 and at least 3 rings")
+    start = [0]
+    for r in range(1, rings + 1):
+        start.append(start[-1] + (1 if r == 1 else valence * (r - 1)))
+    n_v = 1 + valence * rings * (rings + 1) // 2
+    xyz0 = np.zeros((n_v, 3))
+
+    def vid(r: int, m: int) -> int:
+        return 0 if r == 0 else start[r] + (m % (valence * r))
+
+    for r in range(1, rings + 1):
+        for m in range(valence * r):
+            th = 2.0 * np.pi * m / (valence * r)
+            xyz0[vid(r, m)] = (radius * r / rings * np.cos(th), radius * r / rings * np.sin(th), 0.0)
+    if z_sigma > 0.0:
+        rng = np.random.Generator(np.random.PCG64(SEED_BASE if seed is None else seed))
+        phi = rng.uniform(0.0, 2.0 * np.pi)
+        rho2 = (xyz0[:, 0] ** 2 + xyz0[:, 1] ** 2) / radius ** 2
+        th = np.arctan2(xyz0[:, 1], xyz0[:, 0])
+        z = (1.0 - rho2) * (0.5 + 0.5 * np.cos(th - phi))
+        xyz0[:, 2] = z_sigma * z / max(np.abs(z).max(), 1e-300)
+    tri = []
+    for r in range(rings):
+        for k in range(valence):
+            inner = [vid(r, k * r + m) for m in range(r + 1)]
+            outer = [vid(r + 1, k * (r + 1) + m) for m in range(r + 2)]
+            for m in range(r + 1):
+                tri.append((inner[m], outer[m], outer[m + 1]))
+            for m in range(r):
+                tri.append((inner[m], outer[m + 1], inner[m + 1]))
+    tri = np.array(tri, dtype=np.int32)
+    e1 = xyz0[tri[:, 1]] - xyz0[tri[:, 0]]
+    e2 = xyz0[tri[:, 2]] - xyz0[tri[:, 0]]
+    flip = (e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]) < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    ring = np.array([vid(rings, m) for m in range(valence * rings)], dtype=np.int32)
+    n_e = tri.shape[0]
+    fib = np.zeros((n_e, 3))
+    fib[:, 0] = 1.0
+    return Mesh(xyz0=xyz0, tri=tri, n_bnodes=np.array([ring.size], dtype=np.int32), bnodes=ring, fib=fib,
+                gamma_scale=np.zeros(n_e),
+                meta=dict(kind="cone", valence=valence, rings=rings, radius=radius, z_sigma=z_sigma, seed=seed,
+                          hmean=radius / rings))
+
+
 def element_centroids(mesh: Mesh) -> np.ndarray:
     return mesh.xyz0[mesh.tri].mean(axis=1)
 

@@ -5,7 +5,8 @@ oracle/build_ref.py into oracle/_ref/libbiofem_ref.so):
 
     python tests/golden/make_golden.py
 
-Each fixture holds the workload parameters, the reference topology tables
+Each fixture holds the workload parameters (flat sheets, LV caps, cone
+discs with one extraordinary vertex), the reference topology tables
 (GlobalGhostInit/IrrVer/Patch output), the SNES iterate x and the reference
 residual R, Fint and Fext for that x, plus per-element stress / C33 / geometry
 for a few sample elements.  Larger meshes store checksums and a strided
@@ -38,6 +39,10 @@ def sha(a: np.ndarray) -> str:
 
 def workload_dict(w) -> dict:
     extra = dict(dead_load=w.dead_load, iso_act=w.iso_act) if (w.dead_load or w.iso_act) else {}
+    if isinstance(w, configs.ConeWorkload):
+        return dict(kind="cone", name=w.name, valence=w.valence, rings=w.rings, index=w.index, n_qp=w.n_qp,
+                    c33_iters=w.c33_iters, pressure=w.pressure, z_sigma=w.z_sigma, disp_rel=w.disp_rel,
+                    mu=configs.MU, bulk=configs.BULK, h0=configs.H0, **extra)
     if isinstance(w, configs.LVWorkload):
         return dict(kind="lv", name=w.name, freq=w.freq, index=w.index, n_qp=w.n_qp, c33_iters=w.c33_iters,
                     pressure=w.pressure, lambda_a=w.lambda_a, nflip=w.nflip, jitter=w.jitter,
@@ -95,6 +100,11 @@ CASES_FULL = [
     replace(configs.small(8, 7, index=14, pressure=2e-3, dead_load=1), name="flat_8x7_dead_load"),
     replace(configs.small(9, 6, index=15, activation="random", iso_act=1), name="flat_9x6_isotropic"),
     configs.LVWorkload("lv_f3_iso_dead", 3, index=42, iso_act=1, dead_load=1),
+    # one interior vertex of valence 3, 8 and 10: the one-step subdivision at its
+    # smallest valence (rows overwriting rows) and up to the 16-node patch
+    configs.cone(3),
+    configs.cone(8, n_qp=4),
+    configs.cone(10),
 ]
 
 if __name__ == "__main__":

@@ -43,6 +43,22 @@ def test_host_topology_equals_oracle_ellipsoid(freq, oracle_lib):
     sh.close()
 
 
+@pytest.mark.parametrize("valence", range(3, 11))
+def test_host_topology_equals_oracle_cone(valence, oracle_lib):
+    """One interior vertex of valence 3..10 (the one-step subdivision of every
+    valence the reference's tables cover, up to the 16-node patch)."""
+    w = configs.cone(valence)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    t = sh.topology()
+    sh.close()
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0).topology()
+    for k in ("patch", "ire", "val", "irv", "gtri"):
+        np.testing.assert_array_equal(np.asarray(t[k]).reshape(np.asarray(getattr(o, k)).shape), getattr(o, k),
+                                      err_msg=k)
+    assert int(np.where(o.ire == 0, 12, o.val + 6).max()) == max(12, valence + 6)
+
+
 @pytest.mark.parametrize("name", ["C2_flat_256x192", "C4_lv_ellipsoid"])
 def test_host_topology_matches_reference_checksum(name):
     """C2 (98,304 triangles) and C4 (200,614 triangles, valence-5/7 vertices):
