@@ -55,6 +55,9 @@ struct KParams {
   /* FP32 copies for the FP32-bulk kernels (filled on the host) */
   float muf, Kf, hhalff, pres6f;
   float thetaf[kMaxQp], wf[kMaxQp];
+  /* float-float copies (hi, lo) for the FP32-bulk residual (filled on the host) */
+  float mu2[2], K2[2], hhalf2[2];
+  float theta2[kMaxQp][2], w2[kMaxQp][2];
 };
 
 /* Device views of one mesh handle. */

@@ -539,6 +539,11 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   gauss(params->n_qp, kp.theta, kp.w);
   kp.muf = (float)kp.mu; kp.Kf = (float)kp.K; kp.hhalff = (float)kp.hhalf; kp.pres6f = (float)(kp.pressure / 6.0);
   for (int q = 0; q < kMaxQp; q++) { kp.thetaf[q] = (float)kp.theta[q]; kp.wf[q] = (float)kp.w[q]; }
+  {
+    auto split = [](double d, float out[2]) { const FF f(d); out[0] = f.hi; out[1] = f.lo; };
+    split(kp.mu, kp.mu2); split(kp.K, kp.K2); split(kp.hhalf, kp.hhalf2);
+    for (int q = 0; q < kMaxQp; q++) { split(kp.theta[q], kp.theta2[q]); split(kp.w[q], kp.w2[q]); }
+  }
 
   DevMesh &dm = m->dm;
   std::vector<int> ghost3(3 * (size_t)ng);

@@ -201,11 +201,16 @@ template <> __host__ __device__ __forceinline__ EPar<double> epar<double>(const 
   return e;
 }
 /* Float-float parameters (the FP32-bulk residual) */
+/* float-float parameters were split on the host */
 template <> __host__ __device__ __forceinline__ EPar<FF> epar<FF>(const KParams &p)
 {
   EPar<FF> e;
-  e.mu = FF(p.mu); e.K = FF(p.K); e.hhalf = FF(p.hhalf); e.nq = p.nq; e.iters = p.iters; e.tnormal = p.tnormal;
-  for (int q = 0; q < kMaxQp; q++) { e.theta[q] = FF(p.theta[q]); e.w[q] = FF(p.w[q]); }
+  e.mu = FF(p.mu2[0], p.mu2[1]); e.K = FF(p.K2[0], p.K2[1]); e.hhalf = FF(p.hhalf2[0], p.hhalf2[1]);
+  e.nq = p.nq; e.iters = p.iters; e.tnormal = p.tnormal;
+  for (int q = 0; q < kMaxQp; q++) {
+    e.theta[q] = FF(p.theta2[q][0], p.theta2[q][1]);
+    e.w[q] = FF(p.w2[q][0], p.w2[q][1]);
+  }
   return e;
 }
 /* FP32 parameters were converted on the host: no FP64 work in FP32 kernels */

@@ -18,6 +18,8 @@
 #define BIOFEM_FF_CUH
 
 #include <cmath>
+#include <cstdint>
+#include <cstring>
 
 namespace biofem {
 
@@ -99,6 +101,93 @@ __host__ __device__ __forceinline__ FF dsqrt(FF a)
 }
 
 __host__ __device__ __forceinline__ FF val(FF a) { return a; }
+
+/* Bit-level conversions between double and float-float that run on the
+   integer and FP32 pipes only (no double-precision instruction): on this GPU
+   the FP64 pipe issues at 1/64 of the FP32 rate, and the conversion
+   instructions share it.  IEEE-754 binary64 = sign | 11-bit exponent | 52-bit
+   fraction; binary32 = sign | 8-bit exponent | 23-bit fraction. */
+__host__ __device__ __forceinline__ uint64_t ff_bits64(double d)
+{
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(d);
+#else
+  uint64_t b;
+  memcpy(&b, &d, 8);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ double ff_from_bits64(uint64_t b)
+{
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+#endif
+}
+__host__ __device__ __forceinline__ uint32_t ff_bits32(float f)
+{
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t b;
+  memcpy(&b, &f, 4);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ float ff_from_bits32(uint32_t b)
+{
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float f;
+  memcpy(&f, &b, 4);
+  return f;
+#endif
+}
+
+/* d as hi + lo: hi = d with its fraction cut to 23 bits, lo = the remaining
+   29 bits (converted to float, so at most 5 of them are rounded away: hi + lo
+   equals d to 2^-47 relative), then renormalised.  |d| below 2^-126 gives 0,
+   infinities and NaN give themselves. */
+__host__ __device__ __forceinline__ FF ff_split(double d)
+{
+  const uint64_t b = ff_bits64(d);
+  const uint32_t sign = (uint32_t)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const uint64_t m = b & 0xfffffffffffffull;
+  if (e == 0x7ff) return FF(ff_from_bits32(sign | 0x7f800000u | (m ? 0x400000u : 0u)), 0.f);
+  const int ef = e - 1023 + 127;
+  if (ef >= 255) return FF(ff_from_bits32(sign | 0x7f800000u), 0.f);
+  if (ef <= 0) return FF(ff_from_bits32(sign), 0.f);
+  const float hi = ff_from_bits32(sign | ((uint32_t)ef << 23) | (uint32_t)(m >> 29));
+  /* the remainder is rem * 2^(e - 1023 - 52): scale by two exact powers of two
+     (each within the float exponent range for every |d| >= 2^-126) */
+  const float rem = (float)(uint32_t)(m & 0x1fffffffu);
+  const int sh = e - 1023 - 52;                          /* -178 .. 75 */
+  const int sh1 = sh < -100 ? -100 : sh, sh2 = sh - sh1;  /* sh1 >= -100, sh2 in -78 .. 0 */
+  float lo = rem * ff_from_bits32((uint32_t)(sh1 + 127) << 23) * ff_from_bits32((uint32_t)(sh2 + 127) << 23);
+  if (sign) lo = -lo;
+  return ff_fast_two_sum(hi, lo);
+}
+
+/* (double)f exactly, from the bits: a normal float's 24-bit significand fits
+   the double's; subnormal floats (below 2^-126) give 0. */
+__host__ __device__ __forceinline__ double ff_widen(float f)
+{
+  const uint32_t b = ff_bits32(f);
+  const uint64_t sign = (uint64_t)(b >> 31) << 63;
+  const uint32_t ef = (b >> 23) & 0xff;
+  const uint64_t m = b & 0x7fffffu;
+  if (ef == 0) return ff_from_bits64(sign);
+  if (ef == 255) return ff_from_bits64(sign | 0x7ff0000000000000ull | (m << 29));
+  return ff_from_bits64(sign | ((uint64_t)(ef - 127 + 1023) << 52) | (m << 29));
+}
+
+/* hi + lo as a double: two exact widenings and one double addition. */
+__host__ __device__ __forceinline__ double ff_to_double_bits(FF a) { return ff_widen(a.hi) + ff_widen(a.lo); }
 
 } /* namespace biofem */
 #endif

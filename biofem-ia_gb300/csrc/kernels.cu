@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(128) k_elem_residual_ff(DevMesh m, KParams p)
   load_node(m.pos, m.etri[3 * (size_t)e], xc[0], xc[1], xc[2]);
   FF y[15];
   {
-    const FF c[3] = {FF(xc[0]), FF(xc[1]), FF(xc[2])};
+    const FF c[3] = {ff_split(xc[0]), ff_split(xc[1]), ff_split(xc[2])};
 #pragma unroll
     for (int r = 0; r < 5; r++)
 #pragma unroll
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(128) k_elem_residual_ff(DevMesh m, KParams p)
   for (int i = 0; i < nen; i++) {
     double X, Y, Z;
     load_node(m.pos, __ldg(pe + i), X, Y, Z);
-    const FF d[3] = {FF(X - xc[0]), FF(Y - xc[1]), FF(Z - xc[2])};
+    const FF d[3] = {ff_split(X - xc[0]), ff_split(Y - xc[1]), ff_split(Z - xc[2])};
 #pragma unroll
     for (int r = 0; r < 5; r++) {
       const FF c = tab[r * 16 + i];
@@ -348,9 +348,9 @@ __global__ void __launch_bounds__(128) k_elem_residual_ff(DevMesh m, KParams p)
       const FF c = tab[r * 16 + a];
       fx = fx + c * f[3 * r]; fy = fy + c * f[3 * r + 1]; fz = fz + c * f[3 * r + 2];
     }
-    m.fb[(3 * a) * ne + e] = ff_to_double(fx);
-    m.fb[(3 * a + 1) * ne + e] = ff_to_double(fy);
-    m.fb[(3 * a + 2) * ne + e] = ff_to_double(fz);
+    m.fb[(3 * a) * ne + e] = ff_to_double_bits(fx);
+    m.fb[(3 * a + 1) * ne + e] = ff_to_double_bits(fy);
+    m.fb[(3 * a + 2) * ne + e] = ff_to_double_bits(fz);
   }
   if (p.pressure != 0.0) elem_pressure_force(m, p, e);
 }

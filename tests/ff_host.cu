@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 
 #include "../biofem-ia_gb300/csrc/ff.cuh"
 
@@ -45,6 +46,25 @@ int main()
     const long double lp = ldv(p);
     e_sqrt = std::fmax(e_sqrt, (double)(std::fabs(ld(dsqrt(FF(p))) - std::sqrt(lp)) / std::sqrt(lp)));
   }
-  std::printf("%.3e %.3e %.3e %.3e %.3e\n", e_add, e_cancel, e_mul, e_div, e_sqrt);
+  /* the bit-level conversions: ff_split(d) = d to 2^-47 and normalised;
+     ff_widen(f) = (double)f bit for bit; ff_to_double_bits(a) = hi + lo in double */
+  double e_split = 0.0;
+  long bad_norm = 0, bad_widen = 0, bad_todouble = 0;
+  for (int k = 0; k < 200000; k++) {
+    const double d = operand();
+    const FF a = ff_split(d);
+    e_split = std::fmax(e_split, (double)(std::fabs(ld(a) - (long double)d) / std::fabs((long double)d)));
+    if (std::fabs(a.lo) > std::ldexp(std::fabs(a.hi), -24)) bad_norm++;
+    const float f = (float)d;
+    const double w = ff_widen(f), wr = (double)f;
+    if (std::memcmp(&w, &wr, 8) != 0) bad_widen++;
+    const FF b(d);
+    const double t = ff_to_double_bits(b), tr = (double)b.hi + (double)b.lo;
+    if (std::memcmp(&t, &tr, 8) != 0) bad_todouble++;
+  }
+  const FF z = ff_split(0.0), nz = ff_split(-0.0);
+  const bool zeros = z.hi == 0.f && z.lo == 0.f && nz.hi == 0.f && std::signbit(nz.hi) && ff_widen(0.f) == 0.0;
+  std::printf("%.3e %.3e %.3e %.3e %.3e %.3e %ld %ld %ld %d\n", e_add, e_cancel, e_mul, e_div, e_sqrt, e_split,
+              bad_norm, bad_widen, bad_todouble, zeros ? 1 : 0);
   return 0;
 }
