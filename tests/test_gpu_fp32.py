@@ -5,7 +5,7 @@ coordinates.
 
 Stated tolerances for the FP32-bulk form:
   ||R32 - R_o||_2 <= 1e-10 ||R_o||_2  (R_o the oracle's FP64 residual; the
-                                       spec budget is 1e-6),
+                                       FP32-bulk form's budget is 1e-6),
   ||K32 - K64||_F <= 2e-5 ||K64||_F,  ||K32 v - J v||_2 <= 2e-5 ||J v||_2
 (J v = exact dual-number directional derivative of the oracle residual).
 """
