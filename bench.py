@@ -52,7 +52,7 @@ KERNELS_FP32 = ["positions", "elem_residual_ff", "elem_tangent_fp32", "node_gath
 UNIT = "elems/s"
 L2_FLUSH_BYTES = 256 << 20
 CPU_SAMPLE_ELEMS = 2048
-REF_SAMPLE_ELEMS = 4096
+REF_SAMPLE_ELEMS = 2048
 
 
 def parse():
