@@ -102,7 +102,10 @@ extern "C" int RunGpuResidualNoAlloc(BiofemGpuMesh *m, const double *d_x, double
   v.fp = v.fb + 48LL * kp->ne;
   v.fmax = reinterpret_cast<unsigned long long *>(v.fp + 3LL * kp->ne);
   cudaStream_t st = (cudaStream_t)stream;
-  if ((rc = launch_positions(v, *kp, d_x, st)) || (rc = launch_elem_residual(v, *kp, st)) ||
+  /* the element kernel of the handle's precision (FP32-bulk handles carry the
+     float-float constants), so the result is RunGpuResidualDevice's */
+  if ((rc = launch_positions(v, *kp, d_x, st)) ||
+      (rc = v.erefFF ? launch_elem_residual_ff(v, *kp, st) : launch_elem_residual(v, *kp, st)) ||
       (rc = launch_node_gather(v, *kp, d_x, d_R, st)) || (rc = launch_scale(v, *kp, d_R, st)))
     return noalloc_fail(76, std::string("no-alloc residual launch: ") + cudaGetErrorString((cudaError_t)rc));
   return 0;

@@ -157,7 +157,8 @@ int BiofemGpuSync(BiofemGpuMesh *m, void *stream);
    pool) and must not have the library reach cudaMalloc, which can fail under
    the budget, fragments the pool and synchronises the device.  No
    counterpart in the reference.  Same result as RunGpuResidualDevice for a
-   prepared handle; d_x / d_R are device pointers the caller owns; allocates
+   prepared handle (the same element kernel: FP64, or float-float for an
+   FP32-bulk handle); d_x / d_R are device pointers the caller owns; allocates
    nothing.  The per-call work arrays live in one fixed 8 MiB device array
    (1,048,576 doubles) that each GPU loading the library holds until exit:
    meshes needing more than 4*(n_v+n_ghosts) + 51*n_elmt + 1 doubles (about

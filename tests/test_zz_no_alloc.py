@@ -19,10 +19,10 @@ from biofem import configs
 pytestmark = pytest.mark.gpu
 
 
-def _shell(w):
+def _shell(w, precision=0):
     from biofem.gpu import GpuShell
     m = w.build_mesh()
-    return m, GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    return m, GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=precision)
 
 
 def test_no_alloc_residual_matches_existing_entry_point_twice():
@@ -43,6 +43,23 @@ def test_no_alloc_residual_matches_existing_entry_point_twice():
         R = out.cpu().numpy()
         assert np.isfinite(R).all(), call
         assert np.linalg.norm(R - Rref) <= 1e-10 * np.linalg.norm(Rref), call
+    sh.close()
+
+
+def test_no_alloc_residual_of_an_fp32_bulk_handle_is_its_residual():
+    """An FP32-bulk handle's residual is the float-float kernel's; the
+    no-allocation call runs the same kernel, so the two agree bit for bit."""
+    torch = pytest.importorskip("torch")
+    w = configs.C1
+    m, sh = _shell(w, precision=1)
+    x = w.initial_x(m, sh.topology()["xyz0_full"])
+    dx = torch.tensor(x, device="cuda")
+    ref = torch.empty_like(dx)
+    sh.residual_device(dx.data_ptr(), ref.data_ptr(), 0)
+    out = torch.full_like(dx, float("nan"))
+    sh.residual_device_noalloc(dx.data_ptr(), out.data_ptr(), 0)
+    sh.sync(0)
+    assert torch.equal(out, ref)
     sh.close()
 
 
