@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(128) k_elem_residual(DevMesh m, KParams p, dou
    relative to the element's first corner in FP64 before the split, the shift
    is put back through (sum_i N_r[i]) x_c; the element forces leave as
    doubles (hi + lo is exact in FP64) for the FP64 node sums. */
-__global__ void __launch_bounds__(128) k_elem_residual_ff(DevMesh m, KParams p)
+__global__ void __launch_bounds__(128, 3) k_elem_residual_ff(DevMesh m, KParams p)
 {
   __shared__ FF tabs[kNumTables * 85];   /* tables, then their row sums */
   const FF *ntab = static_cast<const FF *>(m.ntabFF);
@@ -379,7 +379,7 @@ __device__ __forceinline__ void store_pressure_vectors(const R av[3], const R bv
   }
 }
 
-__global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
+__global__ void __launch_bounds__(128, 3) k_elem_tangent(DevMesh m, KParams p)
 {
   __shared__ double tabs[kNumTables * 80];
   __shared__ double Jsh[kTanElemsPerCta][kMaxQp * 21]; /* constitutive derivatives per thickness point */
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(128) k_elem_tangent(DevMesh m, KParams p)
    element-size digits; the shift is put back through (sum_i N_r[i]) * x_c,
    which is not zero for the truncated second-derivative rows (their rows sum
    to -1e-4 / -1e-4 / +2e-4).  D = df/dy is written in FP32 for the row assembly. */
-__global__ void __launch_bounds__(128) k_elem_tangent_f32(DevMesh m, KParams p)
+__global__ void __launch_bounds__(128, 5) k_elem_tangent_f32(DevMesh m, KParams p)
 {
   __shared__ float tabs[kNumTables * 80];
   __shared__ float tsum[kNumTables * 5];
