@@ -18,7 +18,13 @@
 
 namespace biofem {
 
-static const int kMissing = 1000000;  /* bending.c sentinel */
+/* The reference's Patch() marks an unresolved stencil slot with the node id
+   1000000 (bending.c:1291), which collides with real node ids from 10^6 nodes
+   on.  The search here marks it with -1, which no node id can equal; the
+   slots past the stencil (16 - nen of them) are still filled with 1000000 so
+   that the tables equal the reference's bit for bit. */
+static const int kUnset = -1;
+static const int kMissing = 1000000;
 
 /* node -> incident triangles (increasing triangle index), CSR */
 static void incidence(int n_nodes, int n_tri, const std::vector<int> &tri, std::vector<int> &ptr, std::vector<int> &idx)
@@ -71,7 +77,7 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
     if (d.n_bnodes[e] < 3) { err = "a boundary ring needs at least 3 nodes"; return 62; }
     ng += d.n_bnodes[e];
   }
-  if ((long long)nv + ng >= kMissing) { err = "n_v + n_ghosts must stay below the 1000000 sentinel"; return 63; }
+  if ((long long)nv + ng >= (1LL << 31) - 1) { err = "n_v + n_ghosts must fit in int32"; return 63; }
   for (int i = 0; i < 3 * ne; i++)
     if (d.tri[i] < 0 || d.tri[i] >= nv) { err = "triangle corner out of range"; return 63; }
   for (int i = 0; i < ng; i++)
@@ -154,7 +160,7 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
   for (int ec = 0; ec < ne; ec++) {
     const int v = T.val[ec];
     if (v + 6 > 16 || v < 3) { err = "element valence outside the 16-wide patch (3 <= v <= 10)"; return 56; }
-    for (int i = 0; i < v + 6; i++) p[i] = kMissing;
+    for (int i = 0; i < v + 6; i++) p[i] = kUnset;
     const int n1 = T.tri_all[3 * ec], n2 = T.tri_all[3 * ec + 1], n3 = T.tri_all[3 * ec + 2];
     cand.clear();
     for (int n : {n1, n2, n3})
@@ -212,14 +218,14 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
     }
     int fix = -1, gfix = -1;
     for (int i = 0; i < v + 6; i++) {
-      if (p[i] == kMissing) continue;
+      if (p[i] == kUnset) continue;
       if (fix < 0) fix = p[i];
       if (p[i] >= nv) { gfix = p[i]; break; }
     }
     if (gfix >= 0) fix = gfix;
-    if (fix >= 0) for (int i = 0; i < v + 6; i++) if (p[i] == kMissing) p[i] = fix;
+    if (fix >= 0) for (int i = 0; i < v + 6; i++) if (p[i] == kUnset) p[i] = fix;
     for (int i = 0; i < v + 6; i++) {
-      if (p[i] == kMissing) { err = "patch stencil incomplete after ghost resolution"; return 77; }
+      if (p[i] == kUnset) { err = "patch stencil incomplete after ghost resolution"; return 77; }
       T.patch[16 * (size_t)ec + i] = p[i];
     }
   }

@@ -171,3 +171,29 @@ def test_host_call_into_pinned_buffers(precision):
     np.testing.assert_array_equal(hR.numpy(), R)
     np.testing.assert_array_equal(hK.numpy().reshape(K.shape), K)
     sh.close()
+
+
+def test_node_ids_beyond_the_reference_sentinel_on_the_device():
+    """R and K of a mesh whose node ids all sit at 10^6 and above (the
+    reference's 1000000 sentinel among them) equal the small mesh's, shifted:
+    the same element and summation order, so bit for bit."""
+    import copy
+    pad = 1_000_000
+    w = configs.small(8, 6, index=96, pressure=1e-3)
+    m = w.build_mesh()
+    m2 = copy.deepcopy(m)
+    m2.xyz0 = np.vstack([np.zeros((pad, 3)), m.xyz0])
+    m2.tri = (m.tri + pad).astype(np.int32)
+    m2.bnodes = (m.bnodes + pad).astype(np.int32)
+    sh, sh2 = shell_for(m, w), shell_for(m2, w)
+    x = w.initial_x(m, sh.topology()["xyz0_full"])
+    x2 = np.concatenate([np.zeros(3 * pad), x])
+    R, K = sh.form_jacobian(x)
+    R2, K2 = sh2.form_jacobian(x2)
+    np.testing.assert_array_equal(R2[3 * pad:], R)
+    v = np.random.default_rng(97).standard_normal(x.size)
+    Kv = sh.to_scipy(K) @ v
+    Kv2 = sh2.to_scipy(K2) @ np.concatenate([np.zeros(3 * pad), v])
+    np.testing.assert_array_equal(Kv2[3 * pad:], Kv)
+    sh.close()
+    sh2.close()

@@ -43,6 +43,40 @@ def test_host_topology_equals_oracle_ellipsoid(freq, oracle_lib):
     sh.close()
 
 
+def _padded(m, pad):
+    """The mesh with `pad` unreferenced nodes put in front, so every node id
+    of its triangles is at least `pad`."""
+    import copy
+    m2 = copy.deepcopy(m)
+    m2.xyz0 = np.vstack([np.zeros((pad, 3)), m.xyz0])
+    m2.tri = (m.tri + pad).astype(np.int32)
+    m2.bnodes = (m.bnodes + pad).astype(np.int32)
+    return m2
+
+
+def test_node_ids_beyond_the_reference_sentinel():
+    """The reference's Patch() marks unresolved stencil slots with the node id
+    1000000, which collides with real nodes from 10^6 on.  A mesh whose nodes
+    all sit at ids 10^6 and above (node 1000000 among them) must get the
+    small mesh's tables shifted by the offset."""
+    pad = 1_000_000
+    w = configs.small(8, 6, index=95)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    t = sh.topology()
+    sh.close()
+    sh2 = GpuShell(_padded(m, pad), w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    t2 = sh2.topology()
+    sh2.close()
+    nen = np.where(np.asarray(t["ire"]) == 0, 12, np.asarray(t["val"]) + 6)
+    pa, pb = np.asarray(t["patch"]).reshape(-1, 16), np.asarray(t2["patch"]).reshape(-1, 16)
+    used = np.arange(16)[None, :] < nen[:, None]
+    np.testing.assert_array_equal(pb[used], pa[used] + pad)
+    np.testing.assert_array_equal(pb[~used], pa[~used])      # the reference's filler in the unused slots
+    for k in ("ire", "val", "irv"):
+        np.testing.assert_array_equal(t2[k], t[k])
+
+
 @pytest.mark.parametrize("valence", range(3, 11))
 def test_host_topology_equals_oracle_cone(valence, oracle_lib):
     """One interior vertex of valence 3..10 (the one-step subdivision of every
