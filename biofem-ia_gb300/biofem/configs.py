@@ -153,6 +153,38 @@ class ConeWorkload:
         return meshmod.initial_state(m, xyz0_full, disp_amp=self.disp_rel * m.meta["hmean"], seed=self.seed + 2)
 
 
+@dataclass(frozen=True)
+class SphereWorkload:
+    """A closed surface (mesh.closed_sphere): no boundary ring, so no ghost
+    nodes and no clamp; internal follower pressure, fibres along the local
+    east direction, a seeded displacement of 1e-2 of the mean edge."""
+    name: str
+    freq: int
+    index: int = 0
+    n_qp: int = 3
+    c33_iters: int = 3
+    pressure: float = 1e-3
+    lambda_a: float = 0.9
+    jitter: float = 0.1
+    disp_rel: float = 1e-2
+    basis: int = 0
+    tnormal: int = 0
+    dead_load: int = 0
+    iso_act: int = 0
+
+    @property
+    def seed(self) -> int:
+        return meshmod.SEED_BASE + self.index
+
+    def build_mesh(self) -> meshmod.Mesh:
+        m = meshmod.closed_sphere(self.freq, self.seed, jitter=self.jitter, lambda_a=self.lambda_a)
+        m.meta["workload"] = self.name
+        return m
+
+    def initial_x(self, m: meshmod.Mesh, xyz0_full: np.ndarray) -> np.ndarray:
+        return meshmod.initial_state(m, xyz0_full, disp_amp=self.disp_rel * m.meta["hmean"], seed=self.seed + 2)
+
+
 def cone(valence: int, **kw) -> ConeWorkload:
     args = dict(index=60 + valence)
     args.update(kw)

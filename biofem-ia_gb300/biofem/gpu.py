@@ -194,8 +194,12 @@ class GpuShell:
     """One mesh resident on the GPU (or, with host_only=True, only its host tables)."""
 
     def __init__(self, mesh, workload, mu: float, bulk: float, h0: float, gamma: float = 1.0,
-                 clamp_edge: int = 0, precision: int = BIOFEM_FP64, host_only: bool = False,
+                 clamp_edge: int | None = None, precision: int = BIOFEM_FP64, host_only: bool = False,
                  block_layout: int = BIOFEM_BLOCK_ROW_MAJOR):
+        """clamp_edge: the boundary ring clamped in x, y, z; by default ring 0,
+        or none (-1) when the mesh has no boundary ring (a closed surface)."""
+        if clamp_edge is None:
+            clamp_edge = 0 if mesh.n_edge > 0 else -1
         self.lib = load_library()
         self._arrays = dict(
             tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),

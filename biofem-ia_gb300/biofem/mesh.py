@@ -179,6 +179,39 @@ def cone_disc(valence: int, rings: int, radius: float = 1.0, z_sigma: float = 0.
                           hmean=radius / rings))
 
 
+def closed_sphere(freq: int, seed: int, radius: float = 1.0, jitter: float = 0.1, lambda_a: float = 0.9) -> Mesh:
+    """A closed surface: the icosahedron's frequency-`freq` geodesic sphere
+    (12 vertices of valence 5, the rest 6; 20 freq^2 triangles), outward
+    triangles, no boundary ring (so no ghost nodes and nothing to clamp);
+    every node moved tangentially by a seeded `jitter` x its shortest edge and
+    pulled back to the sphere; fibres along the local east direction,
+    activation lambda_a on every element."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    V, F = _icosahedron()
+    F = _orient_outward(V, F)
+    V, F = _geodesic(V, F, freq)
+    F = _orient_outward(V, F)
+    e = np.sort(np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1)
+    elen = np.linalg.norm(V[e[:, 0]] - V[e[:, 1]], axis=1)
+    hmin = np.full(len(V), np.inf)
+    np.minimum.at(hmin, e[:, 0], elen)
+    np.minimum.at(hmin, e[:, 1], elen)
+    nrm = V / np.linalg.norm(V, axis=1)[:, None]
+    d = rng.uniform(-1.0, 1.0, size=V.shape) * (jitter * hmin)[:, None]
+    d -= (d * nrm).sum(1)[:, None] * nrm
+    W = V + d
+    V = radius * W / np.linalg.norm(W, axis=1)[:, None]
+    c = V[F].mean(1)
+    east = np.cross(np.array([0.0, 0.0, 1.0])[None, :], c)
+    small = np.linalg.norm(east, axis=1) <= 1e-10
+    east[small] = np.array([1.0, 0.0, 0.0])
+    east -= ((east * c).sum(1) / (c * c).sum(1))[:, None] * c
+    east /= np.linalg.norm(east, axis=1)[:, None]
+    return Mesh(xyz0=V, tri=F.astype(np.int32), n_bnodes=np.zeros(0, dtype=np.int32), bnodes=np.zeros(0, dtype=np.int32),
+                fib=east, gamma_scale=np.full(len(F), 1.0 - lambda_a),
+                meta=dict(kind="sphere", freq=freq, seed=seed, radius=radius, jitter=jitter, hmean=float(elen.mean())))
+
+
 def element_centroids(mesh: Mesh) -> np.ndarray:
     return mesh.xyz0[mesh.tri].mean(axis=1)
 

@@ -80,7 +80,8 @@ class _Base:
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
         rc = f(mesh.n_v, mesh.n_elmt, _p(from_mesh["tri"]), _p(from_mesh["xyz"]), mesh.n_edge,
                _p(from_mesh["nb"]), _p(from_mesh["bn"]), _p(from_mesh["fib"]), _p(from_mesh["gs"]),
-               w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure, int(clamp))
+               w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure,
+               int(clamp and mesh.n_edge > 0))
         if rc:
             raise RuntimeError(f"{self.prefix}_setup failed with code {rc}")
         ng, nd = _c_int(), _c_int()
@@ -188,7 +189,8 @@ class Oracle(_Base):
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
         rc = f(mesh.n_v, mesh.n_elmt, _p(keep["gtri"]), _p(keep["x"]), mesh.n_edge, _p(keep["nb"]), _p(keep["bn"]),
                _p(keep["patch"]), _p(keep["ire"]), _p(keep["val"]), _p(keep["irv"]), _p(keep["gnv3"]),
-               _p(keep["fib"]), _p(keep["gs"]), w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure, int(clamp))
+               _p(keep["fib"]), _p(keep["gs"]), w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure,
+               int(clamp and mesh.n_edge > 0))
         if rc:
             raise RuntimeError(f"oracle_setup_given_topology failed with code {rc}")
         ng_, nd = _c_int(), _c_int()

@@ -30,6 +30,9 @@ def golden_case(path):
     d = np.load(path)
     meta = json.loads(str(d["meta"]))
     opt = {k: meta[k] for k in ("dead_load", "iso_act") if k in meta}
+    if meta.get("kind") == "sphere":
+        keys = ("name", "freq", "index", "n_qp", "c33_iters", "pressure", "lambda_a", "jitter", "disp_rel")
+        return configs.SphereWorkload(**{k: meta[k] for k in keys}, **opt), meta, d
     if meta.get("kind") == "cone":
         keys = ("name", "valence", "rings", "index", "n_qp", "c33_iters", "pressure", "z_sigma", "disp_rel")
         return configs.ConeWorkload(**{k: meta[k] for k in keys}, **opt), meta, d

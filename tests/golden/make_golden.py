@@ -6,7 +6,7 @@ oracle/build_ref.py into oracle/_ref/libbiofem_ref.so):
     python tests/golden/make_golden.py
 
 Each fixture holds the workload parameters (flat sheets, LV caps, cone
-discs with one extraordinary vertex), the reference topology tables
+discs with one extraordinary vertex, a closed sphere), the reference topology tables
 (GlobalGhostInit/IrrVer/Patch output), the SNES iterate x and the reference
 residual R, Fint and Fext for that x, plus per-element stress / C33 / geometry
 for a few sample elements.  Larger meshes store checksums and a strided
@@ -39,6 +39,10 @@ def sha(a: np.ndarray) -> str:
 
 def workload_dict(w) -> dict:
     extra = dict(dead_load=w.dead_load, iso_act=w.iso_act) if (w.dead_load or w.iso_act) else {}
+    if isinstance(w, configs.SphereWorkload):
+        return dict(kind="sphere", name=w.name, freq=w.freq, index=w.index, n_qp=w.n_qp, c33_iters=w.c33_iters,
+                    pressure=w.pressure, lambda_a=w.lambda_a, jitter=w.jitter, disp_rel=w.disp_rel,
+                    mu=configs.MU, bulk=configs.BULK, h0=configs.H0, **extra)
     if isinstance(w, configs.ConeWorkload):
         return dict(kind="cone", name=w.name, valence=w.valence, rings=w.rings, index=w.index, n_qp=w.n_qp,
                     c33_iters=w.c33_iters, pressure=w.pressure, z_sigma=w.z_sigma, disp_rel=w.disp_rel,
@@ -105,6 +109,8 @@ CASES_FULL = [
     configs.cone(3),
     configs.cone(8, n_qp=4),
     configs.cone(10),
+    # a closed surface: no boundary ring, no ghost nodes, nothing clamped
+    configs.SphereWorkload("sphere_f5", 5, index=70),
 ]
 
 if __name__ == "__main__":
