@@ -373,9 +373,9 @@ struct SolverWork {
   double *hscal = nullptr;   /* pinned host scalar */
   int *hstat = nullptr;      /* pinned host copy of the element status word */
   cudaEvent_t ev = nullptr;
-  /* captured restart cycle and the arguments it was captured for */
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
+  /* captured pieces of a restart cycle (start, iteration chunks, end) and
+     the arguments they were captured for */
+  std::vector<cudaGraphExec_t> gexec;
   const double *g_b = nullptr;
   double *g_dx = nullptr;
   const void *g_K = nullptr;
@@ -384,15 +384,13 @@ struct SolverWork {
   long long bytes = 0;         /* device memory allocated above */
 };
 
-/* Restarted GMRES(m) with right block-Jacobi preconditioning; the Arnoldi
-   process, the Givens rotations and the small triangular solve all run on the
-   device.  Kernels skip their work once the cycle has converged, so the host
-   enqueues iterations ahead and only reads the convergence flag every
-   kCheck iterations. */
+/* Restarted flexible GMRES(m), right-preconditioned (multigrid V-cycle or
+   block-Jacobi); the Arnoldi process, the Givens rotations and the small
+   triangular solve all run on the device.  Kernels skip their work once the
+   cycle has converged, so the host enqueues a chunk of iterations ahead and
+   reads the convergence flag after each chunk. */
 class Gmres {
  public:
-  static constexpr int kCheck = 8;
-
   Gmres(const DevMesh &dm, const KParams &kp, bool f32, const void *K, SolverWork &w, AmgHier *amg, cudaStream_t st)
       : dm_(dm), kp_(kp), f32_(f32), K_(K), w_(w), amg_(amg), st_(st) {}
 
@@ -419,24 +417,37 @@ class Gmres {
     return 0;
   }
 
-  /* Enqueue one full GMRES cycle (all m iterations; kernels after
-     convergence do nothing) followed by the update of dx.  The cycle starts
-     from r = b - K dx (dx = 0 on the first cycle), and the tolerance and ||b||
-     live in the device state, so one captured graph serves every cycle of
-     every solve with the same buffers. */
-  void enqueue_cycle(const double *b, double *dx)
+  /* A restart cycle in three kinds of piece: the start (r = b - K dx,
+     ||r||, v_0), the iterations in chunks of kChunk (kernels after
+     convergence do nothing), and the end (the triangular solve and
+     dx += Z y).  The host reads the convergence state after every chunk, so
+     a cycle that converges after a few iterations launches a few chunks, not
+     all m iterations.  The tolerance and ||b|| live in the device state, so
+     the pieces captured for a set of buffers serve every later cycle. */
+  static constexpr int kChunk = 5;
+
+  int nchunks() const { return (w_.m + kChunk - 1) / kChunk; }
+
+  void enqueue_start(const double *b, double *dx)
   {
     const int n = w_.n, m = w_.m;
-    double *V = w_.V;
     GmState *gs = w_.gs;
     matvec(dx, w_.w, nullptr);
     k_axpby<<<nblk(n, 256), 256, 0, st_>>>(n, 1.0, b, -1.0, w_.w);
     k_multidot<<<dim3(kDotBlocks, 1), 256, 0, st_>>>(n, 1, w_.w, (size_t)n, w_.w, w_.part);
     k_reduce_parts<<<1, 128, 0, st_>>>(1, kDotBlocks, w_.part, w_.h1);
     k_cycle_start<<<1, 32, 0, st_>>>(m, w_.h1, w_.g, gs);
-    k_gs_update<<<nblk(n, 256), 256, 0, st_>>>(n, 0, V, (size_t)n, w_.h2, w_.w, V, gs);
+    k_gs_update<<<nblk(n, 256), 256, 0, st_>>>(n, 0, w_.V, (size_t)n, w_.h2, w_.w, w_.V, gs);
+  }
+
+  /* iterations j0 .. j1-1, then the state to the host */
+  void enqueue_iters(int j0, int j1)
+  {
+    const int n = w_.n, m = w_.m;
+    double *V = w_.V;
+    GmState *gs = w_.gs;
     const int nch = std::min(kGsChunks, nblk(n, 256));       /* row chunks per column */
-    for (int j = 0; j < m; j++) {
+    for (int j = j0; j < j1; j++) {
       double *vn = V + (size_t)(j + 1) * n, *zj = w_.Z + (size_t)j * n;
       precond(V + (size_t)j * n, zj, gs);                     /* z_j = M^-1 v_j */
       matvec(zj, vn, gs);                                     /* w = K z_j */
@@ -448,15 +459,52 @@ class Gmres {
                                      w_.H, w_.cs, w_.sn, w_.g, gs);
       k_gs_update<<<nblk(n, 256), 256, 0, st_>>>(n, j + 1, V, (size_t)n, w_.h2, vn, vn, gs);
     }
-    k_backsolve<<<1, 32, 0, st_>>>(m, w_.H, w_.g, w_.y, gs);
-    k_combine<<<nblk(n, 256), 256, 0, st_>>>(n, w_.Z, (size_t)n, w_.y, dx, gs);
     cudaMemcpyAsync(w_.hgs, gs, sizeof(GmState), cudaMemcpyDeviceToHost, st_);
   }
 
-  /* solve K dx = b (dx zeroed on entry); iterations in *its.  Each cycle
-     runs from a graph captured on first use for these buffers and replayed
-     for every later cycle and solve; one host synchronisation per cycle
-     reads the convergence state. */
+  void enqueue_end(double *dx)
+  {
+    const int n = w_.n, m = w_.m;
+    k_backsolve<<<1, 32, 0, st_>>>(m, w_.H, w_.g, w_.y, w_.gs);
+    k_combine<<<nblk(n, 256), 256, 0, st_>>>(n, w_.Z, (size_t)n, w_.y, dx, w_.gs);
+    cudaMemcpyAsync(w_.hgs, w_.gs, sizeof(GmState), cudaMemcpyDeviceToHost, st_);
+  }
+
+  /* piece p: 0 the start, 1 .. nchunks() the iteration chunks, nchunks() + 1
+     the end; launched from its captured graph (enqueued directly on the
+     legacy default stream, which cannot be captured) */
+  int run_piece(int p, const double *b, double *dx)
+  {
+    auto enqueue = [&]() {
+      if (p == 0) enqueue_start(b, dx);
+      else if (p <= nchunks()) enqueue_iters((p - 1) * kChunk, std::min(p * kChunk, w_.m));
+      else enqueue_end(dx);
+    };
+    if (st_ == nullptr) { enqueue(); return (int)cudaGetLastError(); }
+    const int npieces = nchunks() + 2;
+    if ((int)w_.gexec.size() != npieces || w_.g_b != b || w_.g_dx != dx || w_.g_K != K_ ||
+        w_.g_pc != (const void *)amg_) {
+      for (cudaGraphExec_t g : w_.gexec) if (g) cudaGraphExecDestroy(g);
+      w_.gexec.assign(npieces, nullptr);
+      w_.g_b = b; w_.g_dx = dx; w_.g_K = K_; w_.g_pc = amg_;
+    }
+    if (!w_.gexec[p]) {
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return (int)e;
+      enqueue();
+      e = cudaStreamEndCapture(st_, &graph);
+      if (e != cudaSuccess) return (int)e;
+      e = cudaGraphInstantiate(&w_.gexec[p], graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return (int)e;
+    }
+    return (int)cudaGraphLaunch(w_.gexec[p], st_);
+  }
+
+  /* solve K dx = b (dx zeroed on entry); iterations in *its.  Per cycle: the
+     start, iteration chunks until the state says converged (one host
+     synchronisation per chunk), the end. */
   int solve(const double *b, double *dx, double rtol, int maxit, int *its, double *relres)
   {
     const int n = w_.n;
@@ -466,8 +514,14 @@ class Gmres {
     k_solve_begin<<<1, 32, 0, st_>>>(rtol, w_.gs);
     int rc = 0;
     while (*its < maxit) {
-      if (st_ == nullptr) enqueue_cycle(b, dx);   /* the legacy default stream cannot be captured */
-      else if ((rc = replay_cycle(b, dx))) return rc;
+      if ((rc = run_piece(0, b, dx))) return rc;
+      for (int c = 1; c <= nchunks(); c++) {
+        if ((rc = run_piece(c, b, dx))) return rc;
+        cudaError_t e = cudaStreamSynchronize(st_);
+        if (e != cudaSuccess) return (int)e;
+        if (w_.hgs->done) break;
+      }
+      if ((rc = run_piece(nchunks() + 1, b, dx))) return rc;
       cudaError_t e = cudaStreamSynchronize(st_);
       if (e != cudaSuccess) return (int)e;
       const GmState &h = *w_.hgs;
@@ -476,24 +530,6 @@ class Gmres {
       if (h.bnorm == 0.0 || h.resid <= rtol * h.bnorm || h.jdone == 0) break;
     }
     return (int)cudaGetLastError();
-  }
-
-  int replay_cycle(const double *b, double *dx)
-  {
-    if (!w_.graph || w_.g_b != b || w_.g_dx != dx || w_.g_K != K_ || w_.g_pc != (const void *)amg_) {
-      if (w_.gexec) { cudaGraphExecDestroy(w_.gexec); w_.gexec = nullptr; }
-      if (w_.graph) { cudaGraphDestroy(w_.graph); w_.graph = nullptr; }
-      cudaStream_t cap = st_;
-      cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-      if (e != cudaSuccess) return (int)e;
-      enqueue_cycle(b, dx);
-      e = cudaStreamEndCapture(cap, &w_.graph);
-      if (e != cudaSuccess) return (int)e;
-      e = cudaGraphInstantiate(&w_.gexec, w_.graph, 0);
-      if (e != cudaSuccess) return (int)e;
-      w_.g_b = b; w_.g_dx = dx; w_.g_K = K_; w_.g_pc = amg_;
-    }
-    return (int)cudaGraphLaunch(w_.gexec, st_);
   }
 
  private:
@@ -552,8 +588,7 @@ void solver_destroy(SolverWork *w)
   if (w->hscal) cudaFreeHost(w->hscal);
   if (w->hstat) cudaFreeHost(w->hstat);
   if (w->ev) cudaEventDestroy(w->ev);
-  if (w->gexec) cudaGraphExecDestroy(w->gexec);
-  if (w->graph) cudaGraphDestroy(w->graph);
+  for (cudaGraphExec_t g : w->gexec) if (g) cudaGraphExecDestroy(g);
   delete w;
 }
 
