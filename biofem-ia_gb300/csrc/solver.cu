@@ -424,7 +424,7 @@ class Gmres {
      a cycle that converges after a few iterations launches a few chunks, not
      all m iterations.  The tolerance and ||b|| live in the device state, so
      the pieces captured for a set of buffers serve every later cycle. */
-  static constexpr int kChunk = 5;
+  static constexpr int kChunk = 3;
 
   int nchunks() const { return (w_.m + kChunk - 1) / kChunk; }
 
