@@ -111,6 +111,8 @@ int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, doub
                        double *parts = nullptr);
 int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double *th, void *stream);
 int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, bool colmajor, void *stream);
+int launch_row_records(const DevMesh &m, const KParams &p, int *rrec, void *stream);   /* once per mesh */
+extern thread_local bool t_blocking_waits;   /* solver host waits sleep instead of spinning (serving workers) */
 int row_assemble_configure(int maxblk, bool f32);   /* dynamic shared memory of the row assembly */
 size_t row_assemble_smem(int maxblk, bool f32);
 int row_assemble_max_blocks(bool f32);             /* blocks per row each row assembly handles */

@@ -241,7 +241,7 @@ static double tri_area0(const HostTopo &T, int t)
 
 static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const BiofemParams &prm,
                            std::vector<int> &einfo, std::vector<int> &ecorner, std::vector<unsigned char> &rowkind,
-                           std::vector<int> &rptr, std::vector<int> &ridx, std::vector<int> &rcon, std::vector<int> &pptr,
+                           std::vector<int> &rptr, std::vector<int> &ridx, std::vector<int> &pptr,
                            std::vector<int> &pidx)
 {
   std::string err;
@@ -291,7 +291,6 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   }
   for (int i = 0; i < nt; i++) rptr[i + 1] += rptr[i];
   ridx.assign(rptr[nt], 0);
-  rcon.assign(rptr[nt], 0);
   std::vector<int> r_elem(rptr[nt]);   /* the contribution's element, for the pattern sweep below */
   {
     std::vector<int> fill(rptr.begin(), rptr.end() - 1);
@@ -302,7 +301,6 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
         if (node < nv) {
           const int c = fill[node]++;
           ridx[c] = (int)((long long)3 * a * ne + e);
-          rcon[c] = e | (a << 27);
           r_elem[c] = e;
         }
       }
@@ -374,44 +372,6 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   m->dA0.assign(ne, 0.0);
   for (int e = 0; e < ne; e++) m->dA0[e] = tri_area0(T, e);
   return 0;
-}
-
-/* Row-assembly records, one per contribution c of a free row i (kRowRec
-   ints): the contribution (e | a << 27), einfo[e], ecorner[e], 0, then for
-   each patch slot b < nen of e the block of row i it adds to: the block's
-   position in the row's sorted columns, or for a ghost slot the positions
-   of its parents nv2, nv1, nv3 (10 bits each) with kRowSlotGhost set.  They
-   depend on the topology only, so the row assembly reads them instead of
-   searching the row's columns on every call.  Rows with an identity block
-   (clamped, ghost) get zero records; the row assembly does not read them. */
-static void build_row_records(const BiofemGpuMesh *m, const std::vector<int> &einfo, const std::vector<int> &ecorner,
-                              const std::vector<unsigned char> &rowkind, const std::vector<int> &rptr,
-                              const std::vector<int> &rcon, std::vector<int> &rrec)
-{
-  const HostTopo &T = m->topo;
-  const int nv = T.n_v, nt = T.n_v + T.n_ghosts;
-  rrec.assign((size_t)kRowRec * rptr[nt], 0);
-  for (int i = 0; i < nt; i++) {
-    if (rowkind[i] != 0) continue;
-    const int *c0 = m->colind.data() + m->rowptr[i], *c1 = m->colind.data() + m->rowptr[i + 1];
-    auto pos = [&](int node) { return (unsigned)(std::lower_bound(c0, c1, node) - c0); };
-    for (int c = rptr[i]; c < rptr[i + 1]; c++) {
-      const int e = rcon[c] & ((1 << 27) - 1), nen = einfo[e] & 0xff;
-      int *r = &rrec[(size_t)kRowRec * c];
-      r[0] = rcon[c]; r[1] = einfo[e]; r[2] = ecorner[e]; r[3] = 0;
-      for (int b = 0; b < nen; b++) {
-        const int node = T.patch[16 * (size_t)e + b];
-        unsigned sl;
-        if (node < nv) {
-          sl = pos(node);
-        } else {
-          const int g = node - nv;
-          sl = kRowSlotGhost | pos(T.ghost_nv2[g]) | (pos(T.ghost_nv1[g]) << 10) | (pos(T.ghost_nv3[g]) << 20);
-        }
-        r[4 + b] = (int)sl;
-      }
-    }
-  }
 }
 
 static int check_params(const BiofemParams &p)
@@ -495,9 +455,9 @@ int BuildHostMesh(const BiofemMeshDesc *mesh, const BiofemParams *params, Biofem
   if (rc) return rc;
   BiofemGpuMesh *m = new BiofemGpuMesh();
   m->prm = *params;
-  std::vector<int> einfo, ecorner, rptr, ridx, rcon, pptr, pidx;
+  std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx;
   std::vector<unsigned char> rowkind;
-  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, rowkind, rptr, ridx, rcon, pptr, pidx);
+  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, rowkind, rptr, ridx, pptr, pidx);
   if (rc) { delete m; return rc; }
   *out = m;
   return 0;
@@ -521,9 +481,9 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   m->prm = *params;
   m->st = stream ? (cudaStream_t)stream : g_stream;
   if (cudaGetDevice(&m->device) != cudaSuccess) { delete m; return fail(76, "cudaGetDevice failed"); }
-  std::vector<int> einfo, ecorner, rptr, ridx, rcon, pptr, pidx;
+  std::vector<int> einfo, ecorner, rptr, ridx, pptr, pidx;
   std::vector<unsigned char> rowkind;
-  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, rowkind, rptr, ridx, rcon, pptr, pidx);
+  rc = build_host_maps(m, *mesh, *params, einfo, ecorner, rowkind, rptr, ridx, pptr, pidx);
   if (rc) { delete m; return rc; }
   m->rowkind = rowkind;
   const HostTopo &T = m->topo;
@@ -566,12 +526,12 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3);
   UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(pptr, pptr); UP(pidx, pidx);
   UP(rowptr, m->rowptr); UP(colind, m->colind);
-  {
-    std::vector<int> rrec;
-    build_row_records(m, einfo, ecorner, rowkind, rptr, rcon, rrec);
-    UP(rrec, rrec);
-  }
 #undef UP
+  {   /* the row-assembly records, built on the device from the arrays above */
+    int *d_rrec = nullptr;
+    if ((rc = dalloc(m, &d_rrec, (size_t)kRowRec * rptr[nt]))) { free_mesh(m); return rc; }
+    dm.rrec = d_rrec;
+  }
   dm.nnzb = m->nnzb;
   dm.maxblk = m->maxblk;
   if (m->maxblk > row_assemble_max_blocks(params->precision != BIOFEM_FP64)) {
@@ -620,7 +580,8 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   CUDA_TRY(cudaMemsetAsync(dm.status, 0, sizeof(int), m->st));
   CUDA_TRY(cudaMemsetAsync(dm.fp, 0, 3 * sizeof(double) * (size_t)ne, m->st));
   /* reference positions (ghosts included) -> one-time reference geometry */
-  if ((rc = launch_positions(dm, kp, dm.X, m->st)) || (rc = launch_ref_prep(dm, kp, d_fib, d_gsc, d_eref, m->st))) {
+  if ((rc = launch_positions(dm, kp, dm.X, m->st)) || (rc = launch_ref_prep(dm, kp, d_fib, d_gsc, d_eref, m->st)) ||
+      (rc = launch_row_records(dm, kp, const_cast<int *>(dm.rrec), m->st))) {
     free_mesh(m);
     return fail(76, std::string("reference preparation launch: ") + cudaGetErrorString((cudaError_t)rc));
   }

@@ -966,6 +966,64 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
   }
 }
 
+/* Row-assembly records (see DevMesh::rrec), built on the device once per
+   mesh: one warp per row, lanes over (contribution, patch slot); the slot's
+   target is its node's position in the row's sorted columns (a lower-bound
+   search), a ghost slot packs its parents nv2, nv1, nv3 at 10 bits each with
+   kRowSlotGhost.  Rows with an identity block get zero records. */
+__device__ __forceinline__ unsigned col_lower_bound(const int *cols, int nb, int node)
+{
+  int lo = 0, hi = nb;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (cols[mid] < node) lo = mid + 1; else hi = mid;
+  }
+  return (unsigned)lo;
+}
+
+__global__ void k_row_records(DevMesh m, KParams p, int *__restrict__ rrec)
+{
+  const int lane = threadIdx.x & 31;
+  const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= p.nt) return;
+  const int c0 = m.rptr[i], c1 = m.rptr[i + 1];
+  const bool live = m.rowkind[i] == 0;
+  const int k0 = m.rowptr[i], nb = m.rowptr[i + 1] - k0;
+  const int *cols = m.colind + k0;
+  for (int u = lane; u < 16 * (c1 - c0); u += 32) {
+    const int c = c0 + (u >> 4), b = u & 15;
+    int *r = rrec + (size_t)kRowRec * c;
+    const int code = m.ridx[c];                  /* 3 a ne + e */
+    const int e = code % p.ne, a = code / (3 * p.ne);
+    const int info = m.einfo[e], nen = info & 0xff;
+    if (b == 0) {
+      r[0] = live ? (e | (a << 27)) : 0;
+      r[1] = live ? info : 0;
+      r[2] = live ? m.ecorner[e] : 0;
+      r[3] = 0;
+    }
+    unsigned sl = 0;
+    if (live && b < nen) {
+      const int node = m.patch[16 * (size_t)e + b];
+      if (node < p.nv) {
+        sl = col_lower_bound(cols, nb, node);
+      } else {
+        const int g = node - p.nv;
+        sl = kRowSlotGhost | col_lower_bound(cols, nb, m.ghost3[3 * g + 1]) |
+             (col_lower_bound(cols, nb, m.ghost3[3 * g]) << 10) | (col_lower_bound(cols, nb, m.ghost3[3 * g + 2]) << 20);
+      }
+    }
+    r[4 + b] = (int)sl;
+  }
+}
+
+int launch_row_records(const DevMesh &m, const KParams &p, int *rrec, void *stream)
+{
+  const long long threads = 32LL * p.nt;
+  k_row_records<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(m, p, rrec);
+  return (int)cudaGetLastError();
+}
+
 /* ---------------- scaling ---------------- */
 __global__ void k_scale(DevMesh m, KParams p, double *__restrict__ R)
 {

@@ -75,6 +75,11 @@ extern "C" int BiofemServeEstimateBytes(int32_t n_v, int32_t n_elmt, int32_t n_g
 static void worker_main(BiofemServe_ *E)
 {
   cudaSetDevice(E->device);
+  biofem::t_blocking_waits = true;
+  /* one stream per worker, reused by every request it serves */
+  cudaStream_t s = nullptr;
+  const int src = (int)cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  struct StreamGuard { cudaStream_t s; ~StreamGuard() { if (s) cudaStreamDestroy(s); } } guard{s};
   for (;;) {
     ServeReq *r = nullptr;
     {
@@ -95,14 +100,12 @@ static void worker_main(BiofemServe_ *E)
       if (E->active > E->peak_active) E->peak_active = E->active;
       r->t_start = now_s(E->t0);
     }
-    cudaStream_t s = nullptr;
-    int rc = (int)cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    int rc = src;
     BiofemGpuMesh *h = nullptr;
     if (!rc) rc = PrepareGpuMeshOnStream(&r->desc, &r->prm, (void *)s, &h);
     if (!rc) rc = RunGpuNewtonSolve(h, r->x.data(), &r->opt, &r->st);
     if (rc) r->err = BiofemGpuLastError();
     if (h) DestroyGpuMesh(h);
-    if (s) cudaStreamDestroy(s);
     {
       std::lock_guard<std::mutex> lk(E->mu);
       E->in_use -= r->est;

@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -362,6 +363,54 @@ __global__ void k_solve_begin(double tol, GmState *__restrict__ gs)
 /* ---------------- host side ---------------- */
 static inline int nblk(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+/* Host waits of the solver.  A serving worker sets t_blocking_waits so that
+   its thread sleeps on a blocking-sync event instead of spinning in
+   cudaStreamSynchronize: with one worker per core the spinning threads took
+   the cores the other requests' host preparation needed. */
+thread_local bool t_blocking_waits = false;
+
+static cudaError_t host_wait(cudaStream_t st, cudaEvent_t evb)
+{
+  if (t_blocking_waits && evb) {
+    cudaError_t e = cudaEventRecord(evb, st);
+    return e != cudaSuccess ? e : cudaEventSynchronize(evb);
+  }
+  return cudaStreamSynchronize(st);
+}
+
+/* Page-locked scalars a solver reads back (its GMRES state, one dot product,
+   the element status word), from a process-wide free list: freeing
+   page-locked memory can synchronise the whole device, which would make
+   every request that finishes wait for all the others. */
+struct PinnedScalars {
+  GmState gs;
+  double scal;
+  int stat;
+};
+static std::mutex g_pin_mu;
+static std::vector<PinnedScalars *> g_pin_free;
+
+static PinnedScalars *pin_acquire()
+{
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    if (!g_pin_free.empty()) {
+      PinnedScalars *p = g_pin_free.back();
+      g_pin_free.pop_back();
+      return p;
+    }
+  }
+  void *p = nullptr;
+  return cudaMallocHost(&p, sizeof(PinnedScalars)) == cudaSuccess ? static_cast<PinnedScalars *>(p) : nullptr;
+}
+
+static void pin_release(PinnedScalars *p)
+{
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_free.push_back(p);
+}
+
 struct SolverWork {
   int n = 0, nb = 0, m = 0;
   double *V = nullptr, *Z = nullptr, *w = nullptr, *dinv = nullptr, *part = nullptr;
@@ -369,10 +418,12 @@ struct SolverWork {
   double *dx = nullptr, *xt = nullptr, *Rt = nullptr, *xh = nullptr;
   GmState *gs = nullptr;
   unsigned *ticket = nullptr;  /* last-block counter of k_gs_dots (returns to 0 after each launch) */
+  PinnedScalars *pin = nullptr;   /* the page-locked block of the three below */
   GmState *hgs = nullptr;    /* pinned host copy */
   double *hscal = nullptr;   /* pinned host scalar */
   int *hstat = nullptr;      /* pinned host copy of the element status word */
   cudaEvent_t ev = nullptr;
+  cudaEvent_t evb = nullptr; /* blocking-sync event for host_wait */
   /* captured pieces of a restart cycle (start, iteration chunks, end) and
      the arguments they were captured for */
   std::vector<cudaGraphExec_t> gexec;
@@ -411,7 +462,7 @@ class Gmres {
     k_multidot<<<dim3(kDotBlocks, 1), 256, 0, st_>>>(w_.n, 1, a, (size_t)w_.n, b, w_.part);
     k_reduce_parts<<<1, 128, 0, st_>>>(1, kDotBlocks, w_.part, w_.h1);
     cudaMemcpyAsync(w_.hscal, w_.h1, sizeof(double), cudaMemcpyDeviceToHost, st_);
-    cudaError_t e = cudaStreamSynchronize(st_);
+    cudaError_t e = host_wait(st_, w_.evb);
     if (e != cudaSuccess) return (int)e;
     out = *w_.hscal;
     return 0;
@@ -517,12 +568,12 @@ class Gmres {
       if ((rc = run_piece(0, b, dx))) return rc;
       for (int c = 1; c <= nchunks(); c++) {
         if ((rc = run_piece(c, b, dx))) return rc;
-        cudaError_t e = cudaStreamSynchronize(st_);
+        cudaError_t e = host_wait(st_, w_.evb);
         if (e != cudaSuccess) return (int)e;
         if (w_.hgs->done) break;
       }
       if ((rc = run_piece(nchunks() + 1, b, dx))) return rc;
-      cudaError_t e = cudaStreamSynchronize(st_);
+      cudaError_t e = host_wait(st_, w_.evb);
       if (e != cudaSuccess) return (int)e;
       const GmState &h = *w_.hgs;
       *its += h.jdone;
@@ -565,10 +616,13 @@ SolverWork *solver_create(int n, int nb, int m, void *stream, int *rc)
   A((void **)&w->gs, sizeof(GmState));
   A((void **)&w->ticket, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemsetAsync(w->ticket, 0, sizeof(unsigned), w->st);
-  if (e == cudaSuccess) e = cudaMallocHost(&w->hgs, sizeof(GmState));
-  if (e == cudaSuccess) e = cudaMallocHost(&w->hscal, sizeof(double));
-  if (e == cudaSuccess) e = cudaMallocHost(&w->hstat, sizeof(int));
+  if (e == cudaSuccess) {
+    w->pin = pin_acquire();
+    if (!w->pin) e = cudaErrorMemoryAllocation;
+    else { w->hgs = &w->pin->gs; w->hscal = &w->pin->scal; w->hstat = &w->pin->stat; }
+  }
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->evb, cudaEventDisableTiming | cudaEventBlockingSync);
   if (e == cudaSuccess) e = cudaStreamSynchronize(w->st);
   *rc = (int)e;
   if (e != cudaSuccess) { solver_destroy(w); return nullptr; }
@@ -584,11 +638,10 @@ void solver_destroy(SolverWork *w)
                   w->cs, w->sn, w->g, w->y, w->gs, w->ticket};
   for (void *p : ptrs) if (p) cudaFreeAsync(p, st);
   cudaStreamSynchronize(st);
-  if (w->hgs) cudaFreeHost(w->hgs);
-  if (w->hscal) cudaFreeHost(w->hscal);
-  if (w->hstat) cudaFreeHost(w->hstat);
   if (w->ev) cudaEventDestroy(w->ev);
+  if (w->evb) cudaEventDestroy(w->evb);
   for (cudaGraphExec_t g : w->gexec) if (g) cudaGraphExecDestroy(g);
+  pin_release(w->pin);    /* after the graphs that write into it */
   delete w;
 }
 
