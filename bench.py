@@ -38,12 +38,12 @@ for _p in (ROOT, ROOT / "biofem-ia_gb300"):
 METRIC = "K+R assembly elems/s & %HBM; served load-steps/s, p50/p99; FP32 vs FP64"
 # dram__bytes_read.sum + dram__bytes_write.sum per launch on the 256x192
 # workload, from one ncu capture of each kernel (profiles/, bytes)
-DRAM_BYTES_C2 = {"elem_residual": 60.582e6 + 193.670e6, "elem_tangent": 241.122e6 + 151.319e6,
+DRAM_BYTES_C2 = {"elem_residual": 60.582e6 + 193.670e6, "elem_tangent": 241.039e6 + 160.028e6,
                  "row_assemble": 289.613e6 + 106.150e6, "elem_residual_ff": 59.955e6 + 2.915e6,
                  "elem_tangent_fp32": 36.505e6 + 33.795e6, "row_assemble_fp32": 195.243e6 + 48.489e6}
 # sm__pipe_fp64_cycles_active (fraction of peak sustained active) per kernel
 # in the same captures
-FP64_PIPE_ACTIVE_C2 = {"elem_residual": 0.884, "elem_tangent": 0.872, "row_assemble": 0.937}
+FP64_PIPE_ACTIVE_C2 = {"elem_residual": 0.884, "elem_tangent": 0.893, "row_assemble": 0.937}
 # FP64 FMA throughput of this GB300, measured by the DFMA loop of the FP64 pipe
 # probe (biofem-ia_gb300/csrc/probe_fp64.cu): TFLOP/s
 FP64_DFMA_TFLOPS = 1.057
