@@ -185,6 +185,52 @@ class SphereWorkload:
         return meshmod.initial_state(m, xyz0_full, disp_amp=self.disp_rel * m.meta["hmean"], seed=self.seed + 2)
 
 
+@dataclass(frozen=True)
+class CappedLVWorkload:
+    """A truncated prolate spheroid of structured quad strips closed at the
+    apex by flat cap triangles (mesh.capped_lv, ibm->n_elmt_base): a fan from
+    an apex node, or from the apex ring's first node.  Follower pressure,
+    mid-wall helix fibres, no activation on the cap, a seeded displacement of
+    1e-2 of the mean edge.  No ring is clamped unless ``clamp`` (ring 0, the
+    apex ring: in the fan from the apex ring every cap row would be a
+    clamped row)."""
+    name: str
+    n_phi: int
+    n_theta: int
+    apex_vertex: bool = False
+    clamp: bool = False
+    index: int = 0
+    n_qp: int = 3
+    c33_iters: int = 3
+    pressure: float = 1e-3
+    jitter: float = 0.1
+    disp_rel: float = 1e-2
+    basis: int = 0
+    tnormal: int = 0
+    dead_load: int = 0
+    iso_act: int = 0
+
+    @property
+    def seed(self) -> int:
+        return meshmod.SEED_BASE + self.index
+
+    def build_mesh(self) -> meshmod.Mesh:
+        m = meshmod.capped_lv(self.n_phi, self.n_theta, apex_vertex=self.apex_vertex, seed=self.seed,
+                              jitter=self.jitter)
+        m.meta["workload"] = self.name
+        return m
+
+    def initial_x(self, m: meshmod.Mesh, xyz0_full: np.ndarray) -> np.ndarray:
+        return meshmod.initial_state(m, xyz0_full, disp_amp=self.disp_rel * m.meta["hmean"], seed=self.seed + 2)
+
+
+def capped(n_phi: int, n_theta: int, apex_vertex: bool = False, **kw) -> CappedLVWorkload:
+    args = dict(index=80 + n_phi + (1 if apex_vertex else 0))
+    args.update(kw)
+    tag = "apex" if apex_vertex else "fan"
+    return CappedLVWorkload(f"capped_{tag}_{n_phi}x{n_theta}", n_phi, n_theta, apex_vertex, **args)
+
+
 def cone(valence: int, **kw) -> ConeWorkload:
     args = dict(index=60 + valence)
     args.update(kw)

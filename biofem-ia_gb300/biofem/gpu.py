@@ -49,7 +49,7 @@ class BiofemError(RuntimeError):
 class MeshDesc(ctypes.Structure):
     _fields_ = [("n_v", ctypes.c_int32), ("n_elmt", ctypes.c_int32), ("n_edge", ctypes.c_int32),
                 ("tri", _i32p), ("xyz0", _f64p), ("n_bnodes", _i32p), ("bnodes", _i32p),
-                ("n_fib", _f64p), ("gamma_scale", _f64p)]
+                ("n_fib", _f64p), ("gamma_scale", _f64p), ("n_elmt_base", ctypes.c_int32)]
 
 
 class Params(ctypes.Structure):
@@ -197,9 +197,10 @@ class GpuShell:
                  clamp_edge: int | None = None, precision: int = BIOFEM_FP64, host_only: bool = False,
                  block_layout: int = BIOFEM_BLOCK_ROW_MAJOR):
         """clamp_edge: the boundary ring clamped in x, y, z; by default ring 0,
-        or none (-1) when the mesh has no boundary ring (a closed surface)."""
+        or none (-1) when the mesh has no boundary ring (a closed surface) or
+        the workload asks for none (``workload.clamp`` False)."""
         if clamp_edge is None:
-            clamp_edge = 0 if mesh.n_edge > 0 else -1
+            clamp_edge = 0 if mesh.n_edge > 0 and getattr(workload, "clamp", True) else -1
         self.lib = load_library()
         self._arrays = dict(
             tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),
@@ -212,7 +213,8 @@ class GpuShell:
         self.desc = MeshDesc(mesh.n_v, mesh.n_elmt, mesh.n_edge,
                              a["tri"].ctypes.data_as(_i32p), a["xyz0"].ctypes.data_as(_f64p),
                              a["nb"].ctypes.data_as(_i32p), a["bn"].ctypes.data_as(_i32p),
-                             a["fib"].ctypes.data_as(_f64p), a["gs"].ctypes.data_as(_f64p))
+                             a["fib"].ctypes.data_as(_f64p), a["gs"].ctypes.data_as(_f64p),
+                             int(getattr(mesh, "n_elmt_base", 0)))
         self.params = Params(workload.n_qp, workload.c33_iters, mu, bulk, h0, gamma, workload.pressure,
                              clamp_edge, precision, getattr(workload, "basis", BIOFEM_BASIS_REFERENCE),
                              getattr(workload, "tnormal", 0), block_layout, getattr(workload, "dead_load", 0),
@@ -421,7 +423,7 @@ def mesh_desc(mesh):
              gs=np.ascontiguousarray(mesh.gamma_scale, dtype=np.float64))
     d = MeshDesc(mesh.n_v, mesh.n_elmt, mesh.n_edge, a["tri"].ctypes.data_as(_i32p), a["xyz0"].ctypes.data_as(_f64p),
                  a["nb"].ctypes.data_as(_i32p), a["bn"].ctypes.data_as(_i32p), a["fib"].ctypes.data_as(_f64p),
-                 a["gs"].ctypes.data_as(_f64p))
+                 a["gs"].ctypes.data_as(_f64p), int(getattr(mesh, "n_elmt_base", 0)))
     return d, a
 
 

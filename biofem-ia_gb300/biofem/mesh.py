@@ -36,6 +36,7 @@ class Mesh:
     fib: np.ndarray
     gamma_scale: np.ndarray
     meta: dict = field(default_factory=dict)
+    n_elmt_base: int = 0   # ibm->n_elmt_base: > 0 makes the elements from it on flat apex-cap triangles
 
     @property
     def n_v(self) -> int:
@@ -210,6 +211,107 @@ def closed_sphere(freq: int, seed: int, radius: float = 1.0, jitter: float = 0.1
     return Mesh(xyz0=V, tri=F.astype(np.int32), n_bnodes=np.zeros(0, dtype=np.int32), bnodes=np.zeros(0, dtype=np.int32),
                 fib=east, gamma_scale=np.full(len(F), 1.0 - lambda_a),
                 meta=dict(kind="sphere", freq=freq, seed=seed, radius=radius, jitter=jitter, hmean=float(elen.mean())))
+
+
+def capped_lv(n_phi: int, n_theta: int, a: float = 2.0, b: float = 1.0, f_cut: float = 0.375,
+              apex_vertex: bool = False, seed: int = SEED_BASE, jitter: float = 0.1,
+              alpha_apex: float = 60.0, alpha_base: float = -60.0, lambda_a: float = 0.88) -> Mesh:
+    """Truncated prolate spheroid x^2/b^2 + y^2/b^2 + z^2/a^2 = 1 as structured
+    quad strips, closed at the apex by flat cap triangles (ibm->n_elmt_base,
+    the LV options -lv_a, -lv_b, -lv_f_cut).
+
+    Ring k (0..n_theta-1) holds n_phi nodes at polar angle (k + 1) t_cut /
+    n_theta, t_cut = acos(1 - 2 f_cut), node j at azimuth 2 pi j / n_phi.  Ring
+    k and k + 1 are joined by n_phi quads, each cut along the same diagonal, so
+    that every node counts six base triangles (ring nodes three, which IrrVer's
+    boundary rule makes six).  The base triangles come first (n_elmt_base of
+    them); then the cap: a fan from an apex node at z = a (n_phi triangles)
+    when ``apex_vertex``, else a fan from ring-0 node 0 over the apex ring
+    (n_phi - 2 triangles, no apex node).  Boundary rings: ring 0 (the apex
+    ring, edge 0, whose ghosts reflect through the base strip) and the base
+    ring, both following the base triangles' boundary edges.  Interior ring
+    nodes get a seeded tangential jitter of `jitter` x the azimuthal step.
+    Triangles face outward.  Fibres: the mid-wall helix with the latitude
+    sweep, as lv_ellipsoid; cap triangles carry no activation (gamma_scale
+    0), the rest 1 - lambda_a.
+    """
+    if n_phi < 4 or n_theta < 3:
+        raise ValueError("capped_lv needs n_phi >= 4 and n_theta >= 3")
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t_cut = np.arccos(1.0 - 2.0 * f_cut)
+    th = (np.arange(n_theta) + 1.0) * t_cut / n_theta
+    ph = 2.0 * np.pi * np.arange(n_phi) / n_phi
+    if jitter > 0.0:
+        dph = rng.uniform(-1.0, 1.0, size=(n_theta, n_phi)) * jitter * (2.0 * np.pi / n_phi)
+        dph[0] = 0.0
+        dph[-1] = 0.0
+    else:
+        dph = np.zeros((n_theta, n_phi))
+    PH = ph[None, :] + dph
+    TH = np.repeat(th[:, None], n_phi, axis=1)
+    V = np.stack([b * np.sin(TH) * np.cos(PH), b * np.sin(TH) * np.sin(PH), a * np.cos(TH)], axis=-1).reshape(-1, 3)
+
+    def nid(k, j):
+        return k * n_phi + (j % n_phi)
+
+    F = []
+    for k in range(n_theta - 1):
+        for j in range(n_phi):
+            A, B, C, D = nid(k, j), nid(k, j + 1), nid(k + 1, j + 1), nid(k + 1, j)
+            F.append((A, B, C))
+            F.append((A, C, D))
+    n_base = len(F)
+    if apex_vertex:
+        apex = len(V)
+        V = np.vstack([V, [[0.0, 0.0, a]]])
+        for j in range(n_phi):
+            F.append((apex, nid(0, j), nid(0, j + 1)))
+    else:
+        for j in range(1, n_phi - 1):
+            F.append((nid(0, 0), nid(0, j), nid(0, j + 1)))
+    F = np.array(F, dtype=np.int64)
+    # outward: the normal points away from the spheroid's centre
+    c = V[F].mean(1)
+    nrm = np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]])
+    flip = (nrm * c).sum(1) < 0.0
+    F[flip] = F[flip][:, [0, 2, 1]]
+    # boundary rings from the base triangles' boundary half-edges
+    base = F[:n_base]
+    he = np.concatenate([base[:, [0, 1]], base[:, [1, 2]], base[:, [2, 0]]])
+    hs = set(map(tuple, he))
+    nxt = {h[0]: h[1] for h in map(tuple, he) if (h[1], h[0]) not in hs}
+    rings = []
+    for first in (nid(0, 0), nid(n_theta - 1, 0)):
+        ring = [first]
+        while nxt[ring[-1]] != first:
+            ring.append(nxt[ring[-1]])
+        if len(ring) != n_phi:
+            raise RuntimeError("a boundary ring is not a closed loop of n_phi nodes")
+        rings.append(ring)
+    bnodes = np.array(rings[0] + rings[1], dtype=np.int32)
+    # fibres and activation
+    z_base = a * np.cos(t_cut)
+    c = V[F].mean(1)
+    en = c / np.array([b * b, b * b, a * a])
+    en /= np.linalg.norm(en, axis=1)[:, None]
+    down = np.array([0.0, 0.0, -1.0])
+    el = down[None, :] - (en @ down)[:, None] * en
+    small = np.linalg.norm(el, axis=1) <= 1e-10
+    ex = np.array([1.0, 0.0, 0.0])
+    el[small] = ex - (en[small] @ ex)[:, None] * en[small]
+    el /= np.linalg.norm(el, axis=1)[:, None]
+    ec_ = np.cross(en, el)
+    zs = np.clip((a - c[:, 2]) / (a - z_base), 0.0, 1.0)
+    alpha = np.deg2rad((1.0 - zs) * alpha_apex + zs * alpha_base)
+    fib = np.cos(alpha)[:, None] * ec_ + np.sin(alpha)[:, None] * el
+    gs = np.full(len(F), 1.0 - lambda_a)
+    gs[n_base:] = 0.0
+    e = np.sort(np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]), axis=1)
+    hmean = float(np.linalg.norm(V[e[:, 0]] - V[e[:, 1]], axis=1).mean())
+    return Mesh(xyz0=V, tri=F.astype(np.int32), n_bnodes=np.array([n_phi, n_phi], dtype=np.int32), bnodes=bnodes,
+                fib=fib, gamma_scale=gs, n_elmt_base=n_base,
+                meta=dict(kind="capped_lv", n_phi=n_phi, n_theta=n_theta, a=a, b=b, f_cut=f_cut,
+                          apex_vertex=apex_vertex, seed=seed, jitter=jitter, hmean=hmean))
 
 
 def element_centroids(mesh: Mesh) -> np.ndarray:

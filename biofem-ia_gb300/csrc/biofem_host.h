@@ -20,7 +20,8 @@ constexpr int kRefPerQp = 20;     /* FP64 reference constants per (element, qp) 
 constexpr int kRefPerElem = 4;    /* gamma, gamma', c1, pref0 */
 constexpr int kGeomShape = 18;    /* primal element geometry stored for the FP64 tangent (elem_geom_store) */
 constexpr int kGeomPrimal = kGeomShape + 17;   /* + the primal resultants (elem_res_store) */
-constexpr int kNumTables = 11;    /* 0 = regular 12-node patch, v = 3..10 irregular */
+constexpr int kCapTable = 11;     /* flat apex-cap triangle: a1 = x2 - x1, a2 = x3 - x1, no curvature */
+constexpr int kNumTables = 12;    /* 0 = regular 12-node patch, v = 3..10 irregular, kCapTable */
 constexpr int kDeStride = 240;    /* per-element tangent block: D = df/dy (15 x 15, row-major), */
 constexpr int kDePres = 225;      /* then the three follower-pressure corner vectors (9) */
 constexpr int kMaxRowBlocks = 1023;   /* tangent blocks per row the row assembly handles (10-bit slot targets) */
@@ -30,9 +31,11 @@ constexpr unsigned kRowSlotGhost = 1u << 31;   /* record slot target of a ghost 
 /* Topology in IBMNodes layout (see topology.cpp). */
 struct HostTopo {
   int n_v = 0, n_elmt = 0, n_ghosts = 0, n_edge = 0;
+  int n_elmt_base = 0;                             /* > 0: elements from n_elmt_base on are apex-cap triangles */
   std::vector<int> tri_all;                        /* 3*(n_elmt + 2 n_ghosts) */
   std::vector<int> ghost_nv1, ghost_nv2, ghost_nv3;/* per ghost: x_g = x_nv2 + x_nv1 - x_nv3 */
-  std::vector<int> ire, irv, val, patch;           /* patch: 16*n_elmt */
+  std::vector<int> ire, irv, val, patch;           /* patch: 16*n_elmt, the reference's tables */
+  std::vector<int> dpatch;                         /* the kernels' stencils: patch, cap corners in slots 0-2 */
   std::vector<double> xyz0_full;                   /* 3*(n_v + n_ghosts) */
 };
 

@@ -92,7 +92,9 @@ static void subpatch_rows(int v, int rows[12])
    BIOFEM_BASIS_EXACT: the rationals they round (k/324 for the first
    derivatives, k/108 for the second), whose rows sum to zero, so that a flat
    uniform patch has exactly zero second derivatives.  The irregular tables
-   are built from whichever regular table is chosen. */
+   are built from whichever regular table is chosen.  Table kCapTable is the
+   flat apex-cap triangle on its corners (slots 0-2): a1 = x2 - x1,
+   a2 = x3 - x1 and no second derivatives (active_strain.c:448-470). */
 void host_tables(double *out, int basis)
 {
   std::fill(out, out + kNumTables * 80, 0.0);
@@ -103,7 +105,7 @@ void host_tables(double *out, int basis)
       out[(2 + r) * 16 + i] = basis ? std::nearbyint(kNabC[r][i] * 108.0) / 108.0 : kNabC[r][i];
   }
   const double pi = 3.14159265358979323846264338327950288419716939937510582;
-  for (int v = 3; v < kNumTables; v++) {
+  for (int v = 3; v < kCapTable; v++) {
     const int nen = v + 6, nr = v + 12;
     std::vector<double> B((size_t)nr * nen, 0.0);
     /* Loop's vertex rule, weight w(v) = (5/8 - (3/8 + cos(2 pi / v)/4)^2) / v */
@@ -127,6 +129,9 @@ void host_tables(double *out, int basis)
         out[v * 80 + rr * 16 + j] = scale[rr] * s;
       }
   }
+  double *cap = out + kCapTable * 80;
+  cap[0] = -1.0; cap[1] = 1.0;             /* a1 */
+  cap[16 + 0] = -1.0; cap[16 + 2] = 1.0;   /* a2 */
 }
 
 } /* namespace biofem */
@@ -255,9 +260,11 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   einfo.assign(ne, 0);
   ecorner.assign(ne, 0);
   m->n_irregular = 0;
+  const int ncap_from = T.n_elmt_base > 0 ? T.n_elmt_base : ne;
   for (int e = 0; e < ne; e++) {
-    const int nen = T.ire[e] ? T.val[e] + 6 : 12;
-    const int tab = T.ire[e] ? T.val[e] : 0;
+    const bool cap = e >= ncap_from;
+    const int nen = cap ? 3 : T.ire[e] ? T.val[e] + 6 : 12;
+    const int tab = cap ? kCapTable : T.ire[e] ? T.val[e] : 0;
     if (T.ire[e]) m->n_irregular++;
     einfo[e] = nen | (tab << 8);
     /* patch slots holding the triangle's corners (first occurrence) */
@@ -265,7 +272,7 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
     for (int k = 0; k < 3; k++) {
       const int node = T.tri_all[3 * (size_t)e + k];
       int slot = -1;
-      for (int a = 0; a < nen && slot < 0; a++) if (T.patch[16 * (size_t)e + a] == node) slot = a;
+      for (int a = 0; a < nen && slot < 0; a++) if (T.dpatch[16 * (size_t)e + a] == node) slot = a;
       if (slot < 0) return fail(77, "a triangle corner is missing from its own patch");
       packed |= slot << (5 * k);
     }
@@ -285,7 +292,7 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
   for (int e = 0; e < ne; e++) {
     const int nen = einfo[e] & 0xff;
     for (int a = 0; a < nen; a++) {
-      const int node = T.patch[16 * (size_t)e + a];
+      const int node = T.dpatch[16 * (size_t)e + a];
       if (node < nv) rptr[node + 1]++;
     }
   }
@@ -297,7 +304,7 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
     for (int e = 0; e < ne; e++) {
       const int nen = einfo[e] & 0xff;
       for (int a = 0; a < nen; a++) {
-        const int node = T.patch[16 * (size_t)e + a];
+        const int node = T.dpatch[16 * (size_t)e + a];
         if (node < nv) {
           const int c = fill[node]++;
           ridx[c] = (int)((long long)3 * a * ne + e);
@@ -352,7 +359,7 @@ static int build_host_maps(BiofemGpuMesh *m, const BiofemMeshDesc &d, const Biof
       const int nen = einfo[e] & 0xff;
       for (int b = 0; b < nen; b++) {
         int cols[3], sg[3];
-        const int k = expand(T.patch[16 * (size_t)e + b], cols, sg);
+        const int k = expand(T.dpatch[16 * (size_t)e + b], cols, sg);
         ncontrib += k;
         for (int q = 0; q < k; q++)
           if (mark[cols[q]] != i) { mark[cols[q]] = i; cols_acc.push_back(cols[q]); }
@@ -523,7 +530,7 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   std::vector<double> fib(mesh->n_fib, mesh->n_fib + 3 * (size_t)ne), gsc(mesh->gamma_scale, mesh->gamma_scale + ne);
 
 #define UP(field, vec) do { rc = dupload(m, const_cast<std::remove_const<std::remove_pointer<decltype(dm.field)>::type>::type **>(&dm.field), vec); if (rc) { free_mesh(m); return rc; } } while (0)
-  UP(patch, T.patch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3);
+  UP(patch, T.dpatch); UP(einfo, einfo); UP(ecorner, ecorner); UP(ntab, tabs); UP(ntabF, tabsF); UP(etri, etri); UP(ghost3, ghost3);
   UP(X, T.xyz0_full); UP(rowkind, rowkind); UP(rptr, rptr); UP(ridx, ridx); UP(pptr, pptr); UP(pidx, pidx);
   UP(rowptr, m->rowptr); UP(colind, m->colind);
 #undef UP
@@ -1056,10 +1063,13 @@ int SetGpuElementGamma(BiofemGpuMesh *m, const double *gamma_e)
 }
 
 /* Basis-derivative tables (regular + irregular valences 3..10), 11*5*16. */
+/* the 11 subdivision tables (the cap table is internal) */
 int GetGpuBasisTables(double *out)
 {
   if (!out) return fail(85, "null argument");
-  host_tables(out, BIOFEM_BASIS_REFERENCE);
+  double tabs[kNumTables * 80];
+  host_tables(tabs, BIOFEM_BASIS_REFERENCE);
+  std::copy(tabs, tabs + kCapTable * 80, out);
   return 0;
 }
 
@@ -1067,7 +1077,9 @@ int GetGpuBasisTablesKind(int32_t basis, double *out)
 {
   if (!out) return fail(85, "null argument");
   if (basis != BIOFEM_BASIS_REFERENCE && basis != BIOFEM_BASIS_EXACT) return fail(63, "unknown basis tables");
-  host_tables(out, basis);
+  double tabs[kNumTables * 80];
+  host_tables(tabs, basis);
+  std::copy(tabs, tabs + kCapTable * 80, out);
   return 0;
 }
 

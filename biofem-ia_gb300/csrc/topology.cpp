@@ -4,7 +4,11 @@
  *
  * Produces tables bit-identical to the reference's O(N^2) searches
  * GlobalGhostInit (bending.c:1670-1757), IrrVer (bending.c:1188-1267) and
- * Patch (bending.c:1270-1667).  The reference scans every triangle for each
+ * Patch (bending.c:1270-1667), including their apex-cap rules: with
+ * n_elmt_base > 0 the elements from n_elmt_base on are flat cap triangles,
+ * which count towards no node's valence (bending.c:1204-1222), take no part
+ * in the apex ring's ghost reflection (bending.c:1683-1687) and whose patch
+ * holds only their corners, in slots 3, 6 and 7 (bending.c:1282-1294).  The reference scans every triangle for each
  * stencil query and keeps the LAST triangle that matches; every query of
  * Patch() involves one of the element's three corner nodes, so scanning only
  * the triangles incident to those corners, in increasing triangle index,
@@ -83,7 +87,10 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
   for (int i = 0; i < ng; i++)
     if (d.bnodes[i] < 0 || d.bnodes[i] >= nv) { err = "boundary node out of range"; return 63; }
 
-  T.n_v = nv; T.n_elmt = ne; T.n_ghosts = ng; T.n_edge = nedge;
+  const int nbase = d.n_elmt_base;
+  if (nbase < 0 || nbase > ne) { err = "n_elmt_base outside [0, n_elmt]"; return 63; }
+  const int ec_limit = nbase > 0 ? nbase : ne;   /* elements counted by IrrVer */
+  T.n_v = nv; T.n_elmt = ne; T.n_ghosts = ng; T.n_edge = nedge; T.n_elmt_base = nbase;
   const int ntri = ne + 2 * ng, ntot = nv + ng;
   T.tri_all.assign(3 * (size_t)ntri, 0);
   std::copy(d.tri, d.tri + 3 * (size_t)ne, T.tri_all.begin());
@@ -99,12 +106,14 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
   for (int edge_n = 0; edge_n < nedge; edge_n++) {
     const int n_local = d.n_bnodes[edge_n];
     const int ring_first = count;
+    const int ring_limit = (edge_n == 0) ? ec_limit : ne;   /* the apex ring reflects through base elements */
     for (int li = 0; li < n_local; li++) {
       const int nv1 = d.bnodes[start + (li + 1) % n_local], nv2 = d.bnodes[start + li];
       int nv3 = -1;
       /* last real triangle holding both nv1 and nv2 */
       for (int j = rptr[nv1]; j < rptr[nv1 + 1]; j++) {
         const int ec = ridx[j];
+        if (ec >= ring_limit) break;   /* increasing triangle index */
         const int a = T.tri_all[3 * ec], b = T.tri_all[3 * ec + 1], c = T.tri_all[3 * ec + 2];
         if (!(nv2 == a || nv2 == b || nv2 == c)) continue;
         if (a != nv1 && a != nv2) nv3 = a;
@@ -131,7 +140,8 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
   std::vector<char> irr(nv, 0);
   std::vector<int> nval(nv, 6);
   for (int n = 0; n < nv; n++) {
-    const int cnt = rptr[n + 1] - rptr[n];
+    int cnt = 0;   /* base elements holding n */
+    for (int j = rptr[n]; j < rptr[n + 1] && ridx[j] < ec_limit; j++) cnt++;
     if (!is_b[n]) { if (cnt != 6) { irr[n] = 1; nval[n] = cnt; } }
     else if (cnt + 3 != 6) { irr[n] = 1; nval[n] = cnt + 3; }
   }
@@ -144,8 +154,7 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
       if (irr[n] && n > best) best = n;
     }
     if (best >= 0) {
-      T.ire[ec] = 1;
-      T.val[ec] = nval[best];
+      if (ec < ec_limit) { T.ire[ec] = 1; T.val[ec] = nval[best]; }   /* cap elements keep ire 0, val 6 */
       for (int k = 0; k < 3; k++) if (T.tri_all[3 * ec + k] == best) T.irv[ec] = k + 1;
     }
   }
@@ -159,6 +168,12 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
   int p[64];
   for (int ec = 0; ec < ne; ec++) {
     const int v = T.val[ec];
+    if (ec >= ec_limit) {
+      T.patch[16 * (size_t)ec + 3] = T.tri_all[3 * ec];
+      T.patch[16 * (size_t)ec + 6] = T.tri_all[3 * ec + 1];
+      T.patch[16 * (size_t)ec + 7] = T.tri_all[3 * ec + 2];
+      continue;
+    }
     if (v + 6 > 16 || v < 3) { err = "element valence outside the 16-wide patch (3 <= v <= 10)"; return 56; }
     for (int i = 0; i < v + 6; i++) p[i] = kUnset;
     const int n1 = T.tri_all[3 * ec], n2 = T.tri_all[3 * ec + 1], n3 = T.tri_all[3 * ec + 2];
@@ -228,6 +243,15 @@ int build_topology(const BiofemMeshDesc &d, HostTopo &T, std::string &err)
       if (p[i] == kUnset) { err = "patch stencil incomplete after ghost resolution"; return 77; }
       T.patch[16 * (size_t)ec + i] = p[i];
     }
+  }
+
+  /* the stencils the kernels read: a cap element's three corners in slots
+     0-2 (the cap basis table acts on those), the rest a copy of the first
+     corner (never read) */
+  T.dpatch = T.patch;
+  for (int ec = ec_limit; ec < ne; ec++) {
+    int *q = &T.dpatch[16 * (size_t)ec];
+    for (int k = 0; k < 16; k++) q[k] = T.tri_all[3 * ec + (k < 3 ? k : 0)];
   }
   return 0;
 }

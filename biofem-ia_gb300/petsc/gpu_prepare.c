@@ -37,7 +37,7 @@ PetscErrorCode GpuSnesPrepareFE(FE *fem, PetscReal pressure, PetscInt clamp_ring
   for (PetscInt r = 0; r < ibm->n_edge; r++) nb[r] = (int32_t)ibm->n_bnodes[r];
   for (PetscInt i = 0; i < ibm->sum_n_bnodes; i++) bn[i] = (int32_t)ibm->bnodes[i];
   BiofemMeshDesc d = {(int32_t)ibm->n_v, (int32_t)ibm->n_elmt, (int32_t)ibm->n_edge, tri, xyz, nb, bn, fib,
-                      ibm->gamma_scale};
+                      ibm->gamma_scale, (int32_t)ibm->n_elmt_base};
   BiofemParams p = {0};
   p.n_qp = (int32_t)fem->act_data.n_qp;
   p.c33_subitr_nums = (int32_t)fem->act_data.C33_subitr_nums;

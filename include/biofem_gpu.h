@@ -45,6 +45,9 @@ typedef struct {
   const int32_t *bnodes;       /* sum(n_bnodes) ring node ids in ring order */
   const double  *n_fib;        /* 3*n_elmt fibre directions (ibm->n_fib) */
   const double  *gamma_scale;  /* n_elmt per-element activation multiplier (ibm->gamma_scale) */
+  int32_t n_elmt_base;         /* ibm->n_elmt_base: 0, or the count of subdivision elements, the
+                                  elements from it on being flat apex-cap triangles (bending.c:1204-1294,
+                                  active_strain.c:444-470, 1801-1853) */
 } BiofemMeshDesc;
 
 /* Options of the path (active_strain.c:90-110, main.c:190-252). */

@@ -173,9 +173,12 @@ struct Params {
 
 /* load / activation options of the next setup (oracle_set_load_options) */
 static int g_dead_load = 0, g_iso_act = 0;
+/* n_elmt_base of the next setup (oracle_set_elmt_base) */
+static int g_elmt_base = 0;
 
 struct Mesh {
   int n_v = 0, n_elmt = 0, n_ghosts = 0, n_edge = 0;
+  int n_elmt_base = 0;                     /* > 0: elements ec >= n_elmt_base are apex-cap triangles */
   std::vector<int> nv1, nv2, nv3;          /* n_elmt + 2 n_ghosts */
   std::vector<int> n_bnodes, bnodes;
   std::vector<int> ire, irv, val, patch;   /* patch: 16 n_elmt */
@@ -183,6 +186,11 @@ struct Mesh {
   std::vector<double> x0, y0, z0;          /* n_v + n_ghosts reference coordinates */
   std::vector<double> fib, gscale, dA0;
 };
+
+/* Apex-cap element (ec >= n_elmt_base when n_elmt_base > 0): a flat
+   constant-strain triangle closing the apex (bending.c:1282-1294,
+   active_strain.c:448-470, 1807-1853). */
+inline bool is_cap(const Mesh &m, int ec) { return m.n_elmt_base > 0 && ec >= m.n_elmt_base; }
 
 /* ---------------- topology (bending.c) ---------------- */
 /* The reference's searches scan every triangle for each query
@@ -238,10 +246,13 @@ static void global_ghost_init(Mesh &m, std::vector<double> &x, std::vector<doubl
     start = end - m.n_bnodes[edge_n];
     const int n_local = end - start;
     const int ring_first = count;
+    /* the apex ring (edge 0) reflects through base elements only, bending.c:1687 */
+    const int ec_limit = (edge_n == 0 && m.n_elmt_base > 0) ? m.n_elmt_base : m.n_elmt;
     for (int li = 0; li < n_local; li++) {
       const int i = start + li, inext = start + (li + 1) % n_local;
       const int nv1 = m.bnodes[inext], nv2 = m.bnodes[i];
       scan(nv1, [&](int ec) {
+        if (ec >= ec_limit) return;
         int c = 0;
         if (nv1 == m.nv1[ec] || nv1 == m.nv2[ec] || nv1 == m.nv3[ec]) c++;
         if (nv2 == m.nv1[ec] || nv2 == m.nv2[ec] || nv2 == m.nv3[ec]) c++;
@@ -269,7 +280,9 @@ static void global_ghost_init(Mesh &m, std::vector<double> &x, std::vector<doubl
   }
 }
 
-/* IrrVer, bending.c:1188-1267 (n_elmt_base = 0: all elements counted). */
+/* IrrVer, bending.c:1188-1267: only base elements (ec < n_elmt_base, when
+   set) count towards a node's valence (bending.c:1204-1210); irv is set over
+   every element. */
 static void irrver(Mesh &m)
 {
   std::vector<int> irr(m.n_v, 0), elmt;
@@ -278,6 +291,7 @@ static void irrver(Mesh &m)
   const int nb = (int)m.bnodes.size();
   const bool fast = g_fast_topology != 0;
   const TriScan scan(m, m.n_elmt, m.n_v, fast);
+  const int ec_limit = (m.n_elmt_base > 0) ? m.n_elmt_base : m.n_elmt;
   std::vector<char> bflag;
   if (fast) { bflag.assign(m.n_v, 0); for (int i = 0; i < nb; i++) if (m.bnodes[i] >= 0 && m.bnodes[i] < m.n_v) bflag[m.bnodes[i]] = 1; }
   for (int nc = 0; nc < m.n_v; nc++) {
@@ -286,6 +300,7 @@ static void irrver(Mesh &m)
     if (fast) is_b = bflag[nc];
     else for (int i = 0; i < nb; i++) if (nc == m.bnodes[i]) { is_b = 1; break; }
     scan(nc, [&](int ec) {
+      if (ec >= ec_limit) return;
       if (nc == m.nv1[ec] || nc == m.nv2[ec] || nc == m.nv3[ec]) { elmt.push_back(ec); count++; }
     });
     if (is_b) bcount = count + 3;
@@ -332,7 +347,9 @@ static inline void patch_pick(int *p, int A, int B, int n1, int n2, int n3, int 
   }
 }
 
-/* Patch, bending.c:1270-1667 (n_elmt_base = 0).  In every pick the node
+/* Patch, bending.c:1270-1667.  A cap element's patch holds only its corners,
+   in slots 3, 6 and 7, and the sentinel elsewhere (bending.c:1282-1294).  In
+   every pick the node
    p[A] is a corner of the element (p[3], p[6], p[7] regular; p[0], p[1], p[v]
    irregular), and no pick overwrites a corner slot for valence v >= 4, so a
    triangle can match only if it holds one of the three corners: the fast mode
@@ -350,6 +367,13 @@ static void patch_build(Mesh &m)
   int p[64];
   for (int ec = 0; ec < m.n_elmt; ec++) {
     const int v = m.val[ec];
+    if (is_cap(m, ec)) {
+      for (int i = 0; i < 16; i++) m.patch[16 * ec + i] = kMissing;
+      m.patch[16 * ec + 3] = m.nv1[ec];
+      m.patch[16 * ec + 6] = m.nv2[ec];
+      m.patch[16 * ec + 7] = m.nv3[ec];
+      continue;
+    }
     const std::vector<int> *tris = &all;
     if (fast && v >= 4) {
       cand.clear();
@@ -482,7 +506,13 @@ template <class T>
 static int elem_geom(const Mesh &m, int ec, const T *xb, const T *yb, const T *zb, Geom<T> &G)
 {
   const int *pt = &m.patch[16 * ec];
-  if (m.ire[ec] == 0) {
+  if (is_cap(m, ec)) {   /* flat triangle, active_strain.c:448-470 */
+    const int n1 = m.nv1[ec], n2 = m.nv2[ec], n3 = m.nv3[ec];
+    G.a1 = {xb[n2] - xb[n1], yb[n2] - yb[n1], zb[n2] - zb[n1]};
+    G.a2 = {xb[n3] - xb[n1], yb[n3] - yb[n1], zb[n3] - zb[n1]};
+    G.Aaa = {0.0, 0.0, 0.0}; G.Abb = {0.0, 0.0, 0.0}; G.Aab = {0.0, 0.0, 0.0};
+    G.nen = 12;
+  } else if (m.ire[ec] == 0) {
     T x[12], y[12], z[12];
     for (int i = 0; i < 12; i++) {
       if (pt[i] == kMissing) return 77;
@@ -715,6 +745,37 @@ static int elem_forces(const Mesh &m, const Params &P, int ec, const RefElem &R,
   const double pref0 = 0.5 * P.h0 * A0;
   const int nen = G.nen;
   for (int i = 0; i < 3 * nen; i++) Fb[i] = 0.0;
+  if (is_cap(m, ec)) {
+    /* constant-strain membrane force into the patch slots of the corners,
+       active_strain.c:1807-1853 */
+    const int tri_nodes[3] = {m.nv1[ec], m.nv2[ec], m.nv3[ec]};
+    const double dN[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+    int tri_slot[3] = {-1, -1, -1};
+    const int nslot = m.val[ec] + 6;
+    for (int a = 0; a < 3; a++) {
+      for (int i = 0; i < nslot && i < 16; i++)
+        if (m.patch[16 * ec + i] == tri_nodes[a]) { tri_slot[a] = i; break; }
+      if (tri_slot[a] < 0) return 62;
+    }
+    const V3<T> d21 = G.a1, d31 = G.a2;
+    for (int q = 0; q < nq; q++) {
+      const double wq = P.w[q];
+      const T Sv[3] = {S[q][0][0], S[q][1][1], S[q][0][1]};
+      for (int a = 0; a < 3; a++) {
+        const int base = 3 * tri_slot[a];
+        const double Na0 = dN[a][0], Na1 = dN[a][1];
+        const T Bm0x = Na0 * d21.x, Bm0y = Na0 * d21.y, Bm0z = Na0 * d21.z;
+        const T Bm1x = Na1 * d31.x, Bm1y = Na1 * d31.y, Bm1z = Na1 * d31.z;
+        const T Bm2x = Na0 * d31.x + Na1 * d21.x;
+        const T Bm2y = Na0 * d31.y + Na1 * d21.y;
+        const T Bm2z = Na0 * d31.z + Na1 * d21.z;
+        Fb[base + 0] = Fb[base + 0] + pref0 * wq * (Bm0x * Sv[0] + Bm1x * Sv[1] + Bm2x * Sv[2]);
+        Fb[base + 1] = Fb[base + 1] + pref0 * wq * (Bm0y * Sv[0] + Bm1y * Sv[1] + Bm2y * Sv[2]);
+        Fb[base + 2] = Fb[base + 2] + pref0 * wq * (Bm0z * Sv[0] + Bm1z * Sv[1] + Bm2z * Sv[2]);
+      }
+    }
+    return 0;
+  }
   const bool reg = (m.ire[ec] == 0);
   for (int q = 0; q < nq; q++) {
     const double wq = P.w[q], xi = P.theta[q];
@@ -936,6 +997,8 @@ int oracle_setup(int n_v, int n_elmt, const int *tri, const double *xyz0,
   P.gamma = gamma; P.pressure = pressure; P.clamp = clamp_edge0;
   P.dead_load = g_dead_load; P.iso_act = g_iso_act;
   m.n_v = n_v; m.n_elmt = n_elmt; m.n_edge = n_edge;
+  if (g_elmt_base < 0 || g_elmt_base > n_elmt) return 63;
+  m.n_elmt_base = g_elmt_base;
   m.n_bnodes.assign(n_bnodes, n_bnodes + n_edge);
   int sum = 0;
   for (int e = 0; e < n_edge; e++) sum += n_bnodes[e];
@@ -991,6 +1054,8 @@ int oracle_setup_given_topology(int n_v, int n_elmt, const int *tri_all, const d
   P.gamma = gamma; P.pressure = pressure; P.clamp = clamp_edge0;
   P.dead_load = g_dead_load; P.iso_act = g_iso_act;
   m.n_v = n_v; m.n_elmt = n_elmt; m.n_edge = n_edge;
+  if (g_elmt_base < 0 || g_elmt_base > n_elmt) return 63;
+  m.n_elmt_base = g_elmt_base;
   m.n_bnodes.assign(n_bnodes, n_bnodes + n_edge);
   int sum = 0;
   for (int e = 0; e < n_edge; e++) sum += n_bnodes[e];
@@ -1022,6 +1087,11 @@ int oracle_setup_given_topology(int n_v, int n_elmt, const int *tri_all, const d
 }
 
 int oracle_set_threads(int n) { g_threads = n > 0 ? n : 1; return 0; }
+
+/* ibm->n_elmt_base of the next setup: 0 (every element a subdivision
+   element) or the count of base elements, the rest being apex-cap
+   triangles. */
+int oracle_set_elmt_base(int n_elmt_base) { g_elmt_base = n_elmt_base; return 0; }
 
 /* 1: oracle_setup builds the topology with the corner-incident scans (O(N),
    same tables); 0: with the reference's full scans (O(N_e^2)). */

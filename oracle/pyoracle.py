@@ -63,6 +63,13 @@ class _Base:
         f.argtypes = [_c_int, _c_int]
         f(int(getattr(w, "dead_load", 0)), int(getattr(w, "iso_act", 0)))
 
+    def _select_elmt_base(self, mesh):
+        """ibm->n_elmt_base of the next setup: 0, or the count of base
+        elements (the rest are apex-cap triangles)."""
+        f = self._fn("set_elmt_base")
+        f.argtypes = [_c_int]
+        f(int(getattr(mesh, "n_elmt_base", 0)))
+
     def setup(self, mesh, w, mu: float, bulk: float, h0: float, gamma: float = 1.0, clamp: bool = True):
         from_mesh = dict(
             tri=np.ascontiguousarray(mesh.tri, dtype=np.int32),
@@ -75,13 +82,14 @@ class _Base:
         self._keep = from_mesh
         self._select_basis(getattr(w, "basis", 0), getattr(w, "tnormal", 0))
         self._select_load(w)
+        self._select_elmt_base(mesh)
         f = self._fn("setup")
         f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp,
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
         rc = f(mesh.n_v, mesh.n_elmt, _p(from_mesh["tri"]), _p(from_mesh["xyz"]), mesh.n_edge,
                _p(from_mesh["nb"]), _p(from_mesh["bn"]), _p(from_mesh["fib"]), _p(from_mesh["gs"]),
                w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure,
-               int(clamp and mesh.n_edge > 0))
+               int(clamp and getattr(w, "clamp", True) and mesh.n_edge > 0))
         if rc:
             raise RuntimeError(f"{self.prefix}_setup failed with code {rc}")
         ng, nd = _c_int(), _c_int()
@@ -184,13 +192,14 @@ class Oracle(_Base):
         self._keep = keep
         self._select_basis(getattr(w, "basis", 0), getattr(w, "tnormal", 0))
         self._select_load(w)
+        self._select_elmt_base(mesh)
         f = self.lib.oracle_setup_given_topology
         f.argtypes = [_c_int, _c_int, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                       _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int]
         rc = f(mesh.n_v, mesh.n_elmt, _p(keep["gtri"]), _p(keep["x"]), mesh.n_edge, _p(keep["nb"]), _p(keep["bn"]),
                _p(keep["patch"]), _p(keep["ire"]), _p(keep["val"]), _p(keep["irv"]), _p(keep["gnv3"]),
                _p(keep["fib"]), _p(keep["gs"]), w.n_qp, w.c33_iters, mu, bulk, h0, gamma, w.pressure,
-               int(clamp and mesh.n_edge > 0))
+               int(clamp and getattr(w, "clamp", True) and mesh.n_edge > 0))
         if rc:
             raise RuntimeError(f"oracle_setup_given_topology failed with code {rc}")
         ng_, nd = _c_int(), _c_int()

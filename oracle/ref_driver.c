@@ -158,6 +158,15 @@ int ref_set_load_options(int dead_load, int iso_act)
   return 0;
 }
 
+/* ibm->n_elmt_base of the next ref_setup: 0, or the count of base elements
+   (the elements from n_elmt_base on are apex-cap triangles). */
+static int g_elmt_base = 0;
+int ref_set_elmt_base(int n_elmt_base)
+{
+  g_elmt_base = n_elmt_base;
+  return 0;
+}
+
 static void RefFreeAll_(void)
 {
   /* The reference never frees a body before exit; the driver leaks the
@@ -218,7 +227,8 @@ int ref_setup(int n_v, int n_elmt, const int *tri, const double *xyz0,
   ibm->n_v = n_v;
   ibm->n_elmt = n_elmt;
   ibm->n_edge = n_edge;
-  ibm->n_elmt_base = 0;
+  if (g_elmt_base < 0 || g_elmt_base > n_elmt) return PETSC_ERR_ARG_OUTOFRANGE;
+  ibm->n_elmt_base = g_elmt_base;
   int sum = 0;
   for (int e = 0; e < n_edge; e++) sum += n_bnodes[e];
   ibm->n_ghosts = sum; /* one ghost per boundary node per closed ring */

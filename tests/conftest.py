@@ -36,6 +36,10 @@ def golden_case(path):
     if meta.get("kind") == "cone":
         keys = ("name", "valence", "rings", "index", "n_qp", "c33_iters", "pressure", "z_sigma", "disp_rel")
         return configs.ConeWorkload(**{k: meta[k] for k in keys}, **opt), meta, d
+    if meta.get("kind") == "capped":
+        keys = ("name", "n_phi", "n_theta", "apex_vertex", "clamp", "index", "n_qp", "c33_iters", "pressure",
+                "jitter", "disp_rel")
+        return configs.CappedLVWorkload(**{k: meta[k] for k in keys}, **opt), meta, d
     if meta.get("kind") == "lv":
         keys = ("name", "freq", "index", "n_qp", "c33_iters", "pressure", "lambda_a", "nflip", "jitter")
         return configs.LVWorkload(**{k: meta[k] for k in keys}, **opt), meta, d

@@ -29,6 +29,7 @@ static void dump(const BiofemMeshDesc *d, const BiofemParams *p)
   fwrite(d->tri, 4, 3 * (size_t)d->n_elmt, f); fwrite(d->xyz0, 8, 3 * (size_t)d->n_v, f);
   fwrite(d->n_bnodes, 4, (size_t)d->n_edge, f); fwrite(d->bnodes, 4, (size_t)sb, f);
   fwrite(d->n_fib, 8, 3 * (size_t)d->n_elmt, f); fwrite(d->gamma_scale, 8, (size_t)d->n_elmt, f);
+  fwrite(&d->n_elmt_base, 4, 1, f);
   fclose(f);
 }
 

@@ -47,6 +47,10 @@ def workload_dict(w) -> dict:
         return dict(kind="cone", name=w.name, valence=w.valence, rings=w.rings, index=w.index, n_qp=w.n_qp,
                     c33_iters=w.c33_iters, pressure=w.pressure, z_sigma=w.z_sigma, disp_rel=w.disp_rel,
                     mu=configs.MU, bulk=configs.BULK, h0=configs.H0, **extra)
+    if isinstance(w, configs.CappedLVWorkload):
+        return dict(kind="capped", name=w.name, n_phi=w.n_phi, n_theta=w.n_theta, apex_vertex=w.apex_vertex,
+                    clamp=w.clamp, index=w.index, n_qp=w.n_qp, c33_iters=w.c33_iters, pressure=w.pressure,
+                    jitter=w.jitter, disp_rel=w.disp_rel, mu=configs.MU, bulk=configs.BULK, h0=configs.H0, **extra)
     if isinstance(w, configs.LVWorkload):
         return dict(kind="lv", name=w.name, freq=w.freq, index=w.index, n_qp=w.n_qp, c33_iters=w.c33_iters,
                     pressure=w.pressure, lambda_a=w.lambda_a, nflip=w.nflip, jitter=w.jitter,
@@ -76,7 +80,9 @@ def make(w, full: bool, sample_elems=(0, 1, 5, 17)):
             s, c, g = ref.elem_state(ec, w.n_qp)
             S.append(s); C33.append(c); G.append(g)
         # irregular samples too
-        irr = np.nonzero(t.ire)[0][:4]
+        irr = list(np.nonzero(t.ire)[0][:4])
+        if m.n_elmt_base > 0:                       # apex-cap triangles
+            irr += [m.n_elmt_base, m.n_elmt - 1]
         for ec in irr:
             s, c, g = ref.elem_state(int(ec), w.n_qp)
             S.append(s); C33.append(c); G.append(g)
@@ -111,6 +117,10 @@ CASES_FULL = [
     configs.cone(10),
     # a closed surface: no boundary ring, no ghost nodes, nothing clamped
     configs.SphereWorkload("sphere_f5", 5, index=70),
+    # apex-cap triangles (ibm->n_elmt_base): a fan over the apex ring, and a
+    # fan from an apex node with the apex ring clamped
+    configs.capped(10, 5),
+    configs.capped(12, 6, True, clamp=True, n_qp=4),
 ]
 
 if __name__ == "__main__":

@@ -36,7 +36,7 @@ int main(int argc, char **argv)
   RD(x, 8, ndof); RD(v, 8, ndof);
   fclose(f);
 
-  BiofemMeshDesc d = {nv, ne, nedge, tri, xyz, nb, bn, fib, gs};
+  BiofemMeshDesc d = {nv, ne, nedge, tri, xyz, nb, bn, fib, gs, 0};
   BiofemParams p = {0};
   p.n_qp = h[4]; p.c33_subitr_nums = h[5]; p.clamp_edge = h[6]; p.precision = h[7];
   p.mu = r[0]; p.bulk_modulus = r[1]; p.h0 = r[2]; p.gamma = r[3]; p.pressure = r[4];

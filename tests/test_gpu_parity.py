@@ -72,6 +72,8 @@ def test_residual_is_deterministic():
                                 configs.LVWorkload("lv_f3", 3, index=50, iso_act=1, dead_load=1),
                                 configs.cone(3), configs.cone(9, n_qp=5), configs.cone(10),
                                 configs.SphereWorkload("sphere_f6", 6, index=71),
+                                configs.capped(10, 5), configs.capped(12, 6, True, clamp=True, n_qp=4),
+                                configs.capped(16, 8, True, pressure=2e-3),
                                 configs.C1],
                          ids=lambda w: w.name + ("_exact" if w.basis else "") + ("_tnormal" if w.tnormal else "")
                          + ("_dead" if w.dead_load else "") + ("_iso" if w.iso_act else ""))

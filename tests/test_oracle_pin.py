@@ -67,6 +67,28 @@ def test_oracle_matches_live_reference(oracle_lib):
     assert np.array_equal(ref.residual(x), o.residual(x))
 
 
+@pytest.mark.parametrize("apex_vertex", [False, True], ids=["fan", "apex"])
+def test_oracle_matches_live_reference_capped(apex_vertex, oracle_lib):
+    """Apex-cap triangles (n_elmt_base) on a shape not in the fixtures, free
+    rings, against the live reference build."""
+    from oracle import build_ref
+    if not build_ref.available():
+        pytest.skip("reference sources not on this host")
+    from oracle.pyoracle import RefOracle
+    w = configs.capped(9, 4, apex_vertex, n_qp=2, c33_iters=2, index=23)
+    m = w.build_mesh()
+    ref = RefOracle().setup(m, w, configs.MU, configs.BULK, configs.H0)
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0)
+    tr, to = ref.topology(), o.topology()
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        assert np.array_equal(getattr(tr, k), getattr(to, k)), k
+    x = w.initial_x(m, tr.xyz0_full)
+    R = ref.residual(x)
+    assert np.array_equal(R, o.residual(x))
+    cap_nodes = np.unique(m.tri[m.n_elmt_base:])
+    assert np.abs(R.reshape(-1, 3)[cap_nodes]).max() > 0.0
+
+
 def test_oracle_jvp_matches_central_differences(oracle_lib):
     """The dual-number directional derivative is the tangent checker; it must
     agree with central differences of the (bitwise-pinned) residual."""

@@ -140,6 +140,7 @@ def test_adapter_prepare_passes_the_reference_fe_through(tmp_path):
     np.testing.assert_array_equal(take(np.int32, sb), m.bnodes)
     np.testing.assert_array_equal(take(np.float64, 3 * ne), np.asarray(m.fib).ravel())
     np.testing.assert_array_equal(take(np.float64, ne), m.gamma_scale)
+    assert take(np.int32, 1)[0] == 0                                   # ibm->n_elmt_base
 
 
 @pytest.mark.gpu

@@ -93,6 +93,32 @@ def test_host_topology_equals_oracle_cone(valence, oracle_lib):
     assert int(np.where(o.ire == 0, 12, o.val + 6).max()) == max(12, valence + 6)
 
 
+@pytest.mark.parametrize("apex_vertex", [False, True], ids=["fan", "apex"])
+@pytest.mark.parametrize("n_phi,n_theta", [(8, 4), (12, 6), (17, 5)])
+def test_host_topology_equals_oracle_capped(n_phi, n_theta, apex_vertex, oracle_lib):
+    """Apex-cap triangles (n_elmt_base): they count towards no node's
+    valence, the apex ring's ghosts reflect through the base strip only, and
+    a cap's patch holds only its corners (slots 3, 6, 7)."""
+    w = configs.capped(n_phi, n_theta, apex_vertex)
+    m = w.build_mesh()
+    assert 0 < m.n_elmt_base < m.n_elmt
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    t = sh.topology()
+    sh.close()
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0).topology()
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        np.testing.assert_array_equal(np.asarray(t[k]).reshape(np.asarray(getattr(o, k)).shape), getattr(o, k),
+                                      err_msg=k)
+    cap = np.asarray(t["patch"]).reshape(-1, 16)[m.n_elmt_base:]
+    np.testing.assert_array_equal(cap[:, [3, 6, 7]], m.tri[m.n_elmt_base:])
+    assert (np.delete(cap, [3, 6, 7], axis=1) == 1_000_000).all()
+    assert not np.asarray(t["ire"])[m.n_elmt_base:].any()
+    # the apex ring's ghosts reflect through ring-1 nodes (the base strip),
+    # not through the cap triangles that share the apex ring's edges
+    g3 = np.asarray(t["ghost_nv3"])[:n_phi]
+    assert ((g3 >= n_phi) & (g3 < 2 * n_phi)).all()
+
+
 @pytest.mark.parametrize("name", ["C2_flat_256x192", "C4_lv_ellipsoid"])
 def test_host_topology_matches_reference_checksum(name):
     """C2 (98,304 triangles) and C4 (200,614 triangles, valence-5/7 vertices):
