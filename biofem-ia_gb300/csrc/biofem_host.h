@@ -88,6 +88,7 @@ struct DevMesh {
   const int *rowptr, *colind;   /* BSR pattern, columns sorted per row */
   long long nnzb;
   int maxblk;                /* most blocks in one row */
+  int ntabs;                 /* basis tables the row assembly stages: kCapTable, or kNumTables with cap elements */
   /* work arrays */
   double *pos;               /* 4*nt padded positions */
   double *fb;                /* 48*ne element forces */
@@ -116,8 +117,8 @@ int launch_elem_thickness(const DevMesh &m, const KParams &p, double h0, double 
 int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, bool colmajor, void *stream);
 int launch_row_records(const DevMesh &m, const KParams &p, int *rrec, void *stream);   /* once per mesh */
 extern thread_local bool t_blocking_waits;   /* solver host waits sleep instead of spinning (serving workers) */
-int row_assemble_configure(int maxblk, bool f32);   /* dynamic shared memory of the row assembly */
-size_t row_assemble_smem(int maxblk, bool f32);
+int row_assemble_configure(int maxblk, bool f32, int ntabs);   /* dynamic shared memory of the row assembly */
+size_t row_assemble_smem(int maxblk, bool f32, int ntabs);
 int row_assemble_max_blocks(bool f32);             /* blocks per row each row assembly handles */
 int launch_scale(const DevMesh &m, const KParams &p, double *R, void *stream);
 int launch_elem_tangent_f32(const DevMesh &m, const KParams &p, void *stream);

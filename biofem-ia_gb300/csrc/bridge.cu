@@ -541,12 +541,13 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   }
   dm.nnzb = m->nnzb;
   dm.maxblk = m->maxblk;
+  dm.ntabs = (T.n_elmt_base > 0 && T.n_elmt_base < ne) ? kNumTables : kCapTable;
   if (m->maxblk > row_assemble_max_blocks(params->precision != BIOFEM_FP64)) {
     free_mesh(m);
     return fail(63, "a tangent row has more blocks than the FP32 row assembly holds in registers");
   }
   {
-    cudaError_t ce = (cudaError_t)row_assemble_configure(m->maxblk, params->precision != BIOFEM_FP64);
+    cudaError_t ce = (cudaError_t)row_assemble_configure(m->maxblk, params->precision != BIOFEM_FP64, dm.ntabs);
     if (ce != cudaSuccess) { free_mesh(m); return fail(76, std::string("row assembly configuration: ") + cudaGetErrorString(ce)); }
   }
   double *d_fib = nullptr, *d_gsc = nullptr, *d_eref = nullptr;

@@ -667,8 +667,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
                                                                  int maxblk, int colmajor)
 {
   extern __shared__ __align__(16) unsigned char row_smem[];
-  R *tabsT = reinterpret_cast<R *>(row_smem);       /* kNumTables x 16 x 8: N[s][b] at 8 b + s */
-  for (int t = threadIdx.x; t < kNumTables * 16 * kRowPad; t += blockDim.x) {
+  R *tabsT = reinterpret_cast<R *>(row_smem);       /* m.ntabs x 16 x 8: N[s][b] at 8 b + s */
+  for (int t = threadIdx.x; t < m.ntabs * 16 * kRowPad; t += blockDim.x) {
     const int tb = t / (16 * kRowPad), r = t - tb * 16 * kRowPad, b = r / kRowPad, sidx = r - b * kRowPad;
     tabsT[t] = sidx < 5 ? ntab[tb * 80 + sidx * 16 + b] : R(0);
   }
@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int i = blockIdx.x * kRowWarps + wid;
   if (i >= p.nt) return;
-  RowAsmBuf<R> B = row_buf<R>(row_smem + align16(kNumTables * 16 * kRowPad * sizeof(R)) +
+  RowAsmBuf<R> B = row_buf<R>(row_smem + align16(m.ntabs * 16 * kRowPad * sizeof(R)) +
                               (size_t)wid * row_buf_bytes(maxblk, sizeof(R)), maxblk);
   const int k0 = m.rowptr[i], nb = m.rowptr[i + 1] - k0;
   const int kind = m.rowkind[i];
@@ -829,7 +829,7 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
 {
   extern __shared__ __align__(16) unsigned char row_smem[];
   float *tabsT = reinterpret_cast<float *>(row_smem);
-  for (int t = threadIdx.x; t < kNumTables * 16 * kRowPad; t += blockDim.x) {
+  for (int t = threadIdx.x; t < m.ntabs * 16 * kRowPad; t += blockDim.x) {
     const int tb = t / (16 * kRowPad), r = t - tb * 16 * kRowPad, b = r / kRowPad, sidx = r - b * kRowPad;
     tabsT[t] = sidx < 5 ? ntab[tb * 80 + sidx * 16 + b] : 0.f;
   }
@@ -837,7 +837,7 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int i = blockIdx.x * kRowWarps + wid;
   if (i >= p.nt) return;
-  RowRegBuf B = row_reg_buf(row_smem + align16(kNumTables * 16 * kRowPad * 4) + (size_t)wid * row_reg_bytes());
+  RowRegBuf B = row_reg_buf(row_smem + align16(m.ntabs * 16 * kRowPad * 4) + (size_t)wid * row_reg_bytes());
   const int k0 = m.rowptr[i], nb = m.rowptr[i + 1] - k0;
   float *Kr = K + 9 * (size_t)k0;
   if (m.rowkind[i] != 0) {   /* clamped and ghost rows: identity */
@@ -1172,10 +1172,12 @@ int launch_node_gather(const DevMesh &m, const KParams &p, const double *x, doub
   return (int)cudaGetLastError();
 }
 
-size_t row_assemble_smem(int maxblk, bool f32)
+/* the staged tables (only the cap table when the mesh has cap elements),
+   then each warp's row buffer */
+size_t row_assemble_smem(int maxblk, bool f32, int ntabs)
 {
-  if (f32) return align16(kNumTables * 16 * kRowPad * 4) + kRowWarps * row_reg_bytes();
-  return align16(kNumTables * 16 * kRowPad * 8) + kRowWarps * row_buf_bytes(maxblk, 8);
+  if (f32) return align16(ntabs * 16 * kRowPad * 4) + kRowWarps * row_reg_bytes();
+  return align16(ntabs * 16 * kRowPad * 8) + kRowWarps * row_buf_bytes(maxblk, 8);
 }
 
 int row_assemble_max_blocks(bool f32) { return f32 ? kRowRegMax : kMaxRowBlocks; }
@@ -1183,7 +1185,7 @@ int row_assemble_max_blocks(bool f32) { return f32 ? kRowRegMax : kMaxRowBlocks;
 int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, bool colmajor, void *stream)
 {
   const int grid = blocks_for(p.nt, kRowWarps);
-  const size_t smem = row_assemble_smem(m.maxblk, f32);
+  const size_t smem = row_assemble_smem(m.maxblk, f32, m.ntabs);
   if (f32)
     k_row_assemble_f32<<<grid, 32 * kRowWarps, smem, (cudaStream_t)stream>>>(
         m, p, m.DeF, m.ntabF, -p.pres6f, static_cast<float *>(K), (int)colmajor);
@@ -1193,9 +1195,9 @@ int launch_row_assemble(const DevMesh &m, const KParams &p, void *K, bool f32, b
   return (int)cudaGetLastError();
 }
 
-int row_assemble_configure(int maxblk, bool f32)
+int row_assemble_configure(int maxblk, bool f32, int ntabs)
 {
-  const size_t smem = row_assemble_smem(maxblk, f32);
+  const size_t smem = row_assemble_smem(maxblk, f32, ntabs);
   cudaError_t e = f32 ? cudaFuncSetAttribute(k_row_assemble_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
                       : cudaFuncSetAttribute(k_row_assemble<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return (int)e;

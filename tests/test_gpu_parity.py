@@ -3,8 +3,12 @@ fixtures, through the C-ABI (libbiofem_gpu.so).
 
 Tolerances (FP64 plain path):
   residual   ||R_gpu - R_ref||_2 <= 1e-10 * ||R_ref||_2 and per-entry
-             |R_gpu - R_ref| <= 1e-12 * max|Fint| (rounding of the closed-form
-             stress vs the reference's 3^6 / 3^8 loops, and of fused multiply-add);
+             |R_gpu - R_ref| <= 1e-12 * max|Fint| + 4 d_ulp (rounding of the
+             closed-form stress vs the reference's 3^6 / 3^8 loops, and of fused
+             multiply-add), d_ulp = the largest change of the oracle residual
+             when x moves by one rounding (x (1 + 2^-52 z), z ~ N(0, 1), three
+             draws): the residual's own rounding floor, which exceeds
+             1e-12 max|Fint| where stiff rows carry little net force;
   tangent    ||K v - J v||_2 <= 1e-9 * ||J v||_2 on the non-ghost rows, where
              J v is the exact (dual-number) directional derivative of the
              oracle residual; ghost rows of K are identity.
@@ -32,8 +36,17 @@ def shell_for(m, w):
     return GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
 
 
+def rounding_floor(o, x):
+    """Largest change of the oracle residual under a one-rounding relative
+    perturbation of x (three seeded draws)."""
+    R0 = o.residual(x)
+    rng = np.random.default_rng(17)
+    return max(np.abs(o.residual(x * (1.0 + 2.0 ** -52 * rng.standard_normal(x.size))) - R0).max()
+               for _ in range(3))
+
+
 @pytest.mark.parametrize("path", FULL, ids=lambda p: p.stem)
-def test_residual_matches_reference_golden(path):
+def test_residual_matches_reference_golden(path, oracle_lib):
     w, meta, d = load_case(path)
     m = w.build_mesh()
     sh = shell_for(m, w)
@@ -43,7 +56,8 @@ def test_residual_matches_reference_golden(path):
     Rref = d["R"]
     err = np.linalg.norm(R - Rref)
     assert err <= 1e-10 * np.linalg.norm(Rref), (err, np.linalg.norm(Rref))
-    assert np.abs(R - Rref).max() <= 1e-12 * np.abs(d["Fint"]).max()
+    floor = rounding_floor(oracle_lib.setup(m, w, meta["mu"], meta["bulk"], meta["h0"]), d["x"])
+    assert np.abs(R - Rref).max() <= 1e-12 * np.abs(d["Fint"]).max() + 4 * floor
     sh.close()
 
 
@@ -97,7 +111,8 @@ def test_tangent_matches_oracle_directional_derivative(wl, oracle_lib):
         Kv = Ks @ v
         assert np.linalg.norm(Kv[~ghost] - Jv[~ghost]) <= 1e-9 * np.linalg.norm(Jv[~ghost])
         np.testing.assert_array_equal(Kv[ghost], v[ghost])
-    np.testing.assert_allclose(R, Ro, rtol=0, atol=1e-12 * max(1e-30, np.abs(Ro).max()) + 1e-17)
+    np.testing.assert_allclose(R, Ro, rtol=0, atol=1e-12 * max(1e-30, np.abs(Ro).max()) + 1e-17
+                               + 4 * rounding_floor(o, x))
     sh.close()
 
 
