@@ -291,7 +291,10 @@ class GpuShell:
     def newton_options(self, **kw) -> NewtonOptions:
         o = NewtonOptions()
         self.lib.BiofemNewtonDefaults(ctypes.byref(o))
+        names = {f[0] for f in NewtonOptions._fields_}
         for k, v in kw.items():
+            if k not in names:
+                raise TypeError(f"unknown Newton option {k!r} (fields: {sorted(names)})")
             setattr(o, k, v)
         return o
 

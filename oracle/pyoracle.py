@@ -277,7 +277,7 @@ class Oracle(_Base):
         infl = [set([j]) for j in range(nv)]         # rows influenced by column node j
         for e in range(ne):
             nen = 12 if ire[e] == 0 else val[e] + 6
-            nodes = [int(q) for q in patch[e, :nen]]
+            nodes = [int(q) for q in patch[e, :nen] if q != 1000000]   # a cap element's unused slots
             rows = {q for q in nodes if q < nv}
             cols = set()
             for q in nodes:

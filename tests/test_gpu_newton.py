@@ -121,3 +121,31 @@ def test_device_gmres_step_matches_scipy_gmres(pc):
     assert np.linalg.norm(A @ dx_ref + R) <= 1e-10 * rn
     assert np.linalg.norm(dx - dx_ref) <= 1e-6 * np.linalg.norm(dx_ref), np.linalg.norm(dx - dx_ref) / np.linalg.norm(dx_ref)
     sh.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32_bulk"])
+def test_newton_capped_lv_is_a_root_of_the_oracle_residual(precision, oracle_lib):
+    """A truncated spheroid closed at the apex by cap triangles around an
+    apex node (n_elmt_base), base ring clamped (clamp_edge 1), activation on
+    the strip: the device Newton root zeroes the oracle's residual on every
+    free row (the oracle's rows are unclamped; the clamp only replaces the
+    base rows by x - X)."""
+    from biofem.gpu import GpuShell
+    w = configs.capped(16, 8, True)
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, clamp_edge=1, precision=precision)
+    t = sh.topology()
+    x0 = w.initial_x(m, t["xyz0_full"])
+    x, st = sh.newton(x0, rtol=1e-10, max_newton=30)
+    assert st["converged"] == 1, st
+    base = np.asarray(m.bnodes[m.n_bnodes[0]:])
+    free = np.ones(3 * m.n_v, bool)
+    free[(3 * base[:, None] + np.arange(3)).ravel()] = False
+    X = np.asarray(t["xyz0_full"]).ravel()[: 3 * m.n_v]
+    np.testing.assert_allclose(x[: 3 * m.n_v][~free], X[~free], rtol=0, atol=1e-14)   # the clamp: x = X
+    o = oracle_lib.setup_given_topology(m, w, t, configs.MU, configs.BULK, configs.H0)
+    R0 = o.residual(x0)[: 3 * m.n_v][free]
+    R = o.residual(x)[: 3 * m.n_v][free]
+    assert np.linalg.norm(R) <= 1e-9 * np.linalg.norm(R0), (np.linalg.norm(R), np.linalg.norm(R0), st)
+    assert np.abs(x - x0)[: 3 * m.n_v].max() > 1e-2          # a large deformation, not a trivial root
+    sh.close()
