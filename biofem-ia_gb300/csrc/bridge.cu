@@ -167,6 +167,8 @@ struct BiofemGpuMesh_ {
   AmgHier *amg = nullptr;                   /* multigrid hierarchy, created on first multigrid solve */
   std::vector<unsigned char> rowkind;       /* host copy: 0 free, 1 clamped, 2 ghost */
   cudaStream_t st = nullptr;                /* stream of the host-array calls and of setup/teardown */
+  cudaStream_t side = nullptr;              /* second stream: independent kernels of one call overlap */
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   KernelTimer timer;
   int device = -1;                          /* the device the handle's arrays live on */
 };
@@ -228,6 +230,9 @@ static void free_mesh(BiofemGpuMesh *m)
   for (void *p : m->allocs) cudaFreeAsync(p, m->st);
   m->allocs.clear();
   if (m->st) cudaStreamSynchronize(m->st);
+  if (m->side) { cudaStreamSynchronize(m->side); cudaStreamDestroy(m->side); }
+  if (m->ev_fork) cudaEventDestroy(m->ev_fork);
+  if (m->ev_join) cudaEventDestroy(m->ev_join);
   delete m;
 }
 
@@ -492,6 +497,12 @@ int PrepareGpuMeshOnStream(const BiofemMeshDesc *mesh, const BiofemParams *param
   std::vector<unsigned char> rowkind;
   rc = build_host_maps(m, *mesh, *params, einfo, ecorner, rowkind, rptr, ridx, pptr, pidx);
   if (rc) { delete m; return rc; }
+  if (cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    free_mesh(m);
+    return fail(76, "side stream or events could not be created");
+  }
   m->rowkind = rowkind;
   const HostTopo &T = m->topo;
   const int ne = T.n_elmt, nv = T.n_v, ng = T.n_ghosts, nt = nv + ng;
@@ -730,6 +741,24 @@ static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, v
   if (!m->dm.patch) return fail(58, "host-only handle");
   cudaStream_t st = pick_stream(stream);
   int rc = 0;
+  /* Independent kernels run side by side on the handle's second stream: the
+     node gather beside the FP64 tangent, the FP32 tangent beside the
+     float-float residual and the gather.  The row assembly waits for both
+     (it reads D and the gather's max |Fext|).  With per-kernel timing on,
+     every launch stays on the call's stream so that the events bracket one
+     kernel each. */
+  const bool overlap = !m->timer.on;
+  cudaStream_t sd = overlap ? m->side : st;
+  auto fork = [&]() {
+    if (!overlap || rc) return;
+    rc = (int)cudaEventRecord(m->ev_fork, st);
+    if (!rc) rc = (int)cudaStreamWaitEvent(sd, m->ev_fork, 0);
+  };
+  auto join = [&]() {
+    if (!overlap || rc) return;
+    rc = (int)cudaEventRecord(m->ev_join, sd);
+    if (!rc) rc = (int)cudaStreamWaitEvent(st, m->ev_join, 0);
+  };
   tmark(m, st, 0);
   if (m->prm.precision == BIOFEM_FP64) {
     /* R from the residual kernel, so that the Jacobian call returns exactly
@@ -737,17 +766,32 @@ static int residual_jacobian(BiofemGpuMesh *m, const double *d_x, double *d_R, v
     double *K = static_cast<double *>(d_K);
     if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
     if (!rc) { rc = launch_elem_residual(m->dm, m->kp, st, true); tmark(m, st, 2); }
-    if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 3); }
-    if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
+    if (overlap) {
+      fork();
+      if (!rc) rc = launch_node_gather(m->dm, m->kp, d_x, d_R, sd);
+      if (!rc) rc = launch_elem_tangent(m->dm, m->kp, st);
+      join();
+    } else {
+      if (!rc) { rc = launch_elem_tangent(m->dm, m->kp, st); tmark(m, st, 3); }
+      if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
+    }
     if (!rc) { rc = launch_row_assemble(m->dm, m->kp, K, false, colmajor, st); tmark(m, st, 5); }
     if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   } else {
     /* FP32-bulk: residual in float-float, tangent (D, K) in FP32 */
     float *K = static_cast<float *>(d_K);
     if (!rc) { rc = launch_positions(m->dm, m->kp, d_x, st); tmark(m, st, 1); }
-    if (!rc) { rc = launch_elem_residual_ff(m->dm, m->kp, st); tmark(m, st, 2); }
-    if (!rc) { rc = launch_elem_tangent_f32(m->dm, m->kp, st); tmark(m, st, 3); }
-    if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
+    if (overlap) {
+      fork();
+      if (!rc) rc = launch_elem_tangent_f32(m->dm, m->kp, sd);
+      if (!rc) rc = launch_elem_residual_ff(m->dm, m->kp, st);
+      if (!rc) rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st);
+      join();
+    } else {
+      if (!rc) { rc = launch_elem_residual_ff(m->dm, m->kp, st); tmark(m, st, 2); }
+      if (!rc) { rc = launch_elem_tangent_f32(m->dm, m->kp, st); tmark(m, st, 3); }
+      if (!rc) { rc = launch_node_gather(m->dm, m->kp, d_x, d_R, st); tmark(m, st, 4); }
+    }
     if (!rc) { rc = launch_row_assemble(m->dm, m->kp, K, true, colmajor, st); tmark(m, st, 5); }
     if (!rc) { rc = launch_scale(m->dm, m->kp, d_R, st); tmark(m, st, 6); }
   }
