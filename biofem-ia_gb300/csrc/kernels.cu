@@ -771,32 +771,34 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
   }
 }
 
-/* FP32 row assembly with the row's blocks in registers: lane k owns block
-   base + k of the row (base = 0, then 32 for the rare rows of more than 32
-   blocks, which repeat the contribution loop), holding its 9 values and
-   their Kahan compensations.  Per chunk of kRowChunk contributions: slot
-   targets and an inverse map (owned block -> real patch slot) in shared
-   memory, then w of each contribution (lane t and t + 32 of its 45 entries,
-   index arithmetic done once per row); each contribution's block values are
-   formed by the lane that owns the block (N[.][b] from the table, the 9 x 5
-   values of w read by every lane at once) and fused into a per-chunk partial
-   sum; a ghost slot's values go to the lanes owning its parents, after the
-   real slots, in slot order.  The partial sums are added into the row with
-   Kahan compensation once per chunk, in element order. */
+/* FP32 row assembly with the row's blocks owned by lanes: lane k owns block k
+   of the row in registers (9 values) and, in rows of more than 32 blocks
+   (most interior rows: 36 on average in a regular mesh), block 32 + k in
+   shared memory.  One pass over the row's contributions, kRowChunk at a
+   time: slot targets and an inverse map (owned block -> real patch slot) in
+   shared memory, then w of each contribution (lane t and t + 32 of its 45
+   entries), then each owned block's values formed by its owner lane (N[.][b]
+   from the table, the 9 x 5 values of w read by every lane at once) and fused
+   into a per-chunk partial sum; a ghost slot's values go to the lanes owning
+   its parents, after the real slots, in slot order.  The partial sums are
+   added into the row with Kahan compensation once per chunk, in element
+   order; the second 32 blocks' pass is skipped for a chunk that touches none
+   of them. */
 constexpr int kRowRegMax = 64;
 
 struct RowRegBuf {
   float *wT;          /* kRowChunk x 9 x 8 */
-  float *stage;       /* 9 x 32 write-out staging */
-  float *comp;        /* 9 x 32 Kahan compensations of the owned blocks ([q][lane]) */
+  float *acc1;        /* 32 x 9 values of the owned blocks 32..63 ([lane][q]); the write-out staging */
+  float *comp;        /* 9 x 32 Kahan compensations of the owned blocks 0..31 ([q][lane]) */
+  float *comp1;       /* 32 x 9 compensations of the owned blocks 32..63 ([lane][q]) */
   int *cols;          /* kRowRegMax */
   int *rec;           /* kRowChunk row-assembly records */
-  unsigned char *inv; /* kRowChunk x 32: real slot of each owned block, 255 none */
+  unsigned char *inv; /* kRowChunk x 64: real slot of each owned block, 255 none */
 };
 
 __host__ __device__ __forceinline__ size_t row_reg_bytes()
 {
-  return kRowChunk * 9 * kRowPad * 4 + 2 * 9 * 32 * 4 + kRowRegMax * 4 + kRowChunk * kRowRec * 4 + kRowChunk * 32;
+  return kRowChunk * 9 * kRowPad * 4 + 3 * 9 * 32 * 4 + kRowRegMax * 4 + kRowChunk * kRowRec * 4 + kRowChunk * 64;
 }
 
 __device__ __forceinline__ RowRegBuf row_reg_buf(unsigned char *q)
@@ -804,9 +806,11 @@ __device__ __forceinline__ RowRegBuf row_reg_buf(unsigned char *q)
   RowRegBuf b;
   b.wT = reinterpret_cast<float *>(q);
   q += kRowChunk * 9 * kRowPad * 4;
-  b.stage = reinterpret_cast<float *>(q);
+  b.acc1 = reinterpret_cast<float *>(q);
   q += 9 * 32 * 4;
   b.comp = reinterpret_cast<float *>(q);
+  q += 9 * 32 * 4;
+  b.comp1 = reinterpret_cast<float *>(q);
   q += 9 * 32 * 4;
   b.cols = reinterpret_cast<int *>(q);
   q += kRowRegMax * 4;
@@ -821,6 +825,54 @@ __device__ __forceinline__ void row_reg_block(const float *wT, const float n[5],
 {
 #pragma unroll
   for (int q = 0; q < 9; q++) tmp[q] = row_block_accum(wT + kRowPad * q, n, tmp[q]);
+}
+
+/* The chunk's contributions to owned block k (k = lane or 32 + lane, inverse
+   map column kc) added into tmp: the real slot mapped to k (with its
+   follower-pressure term), then the ghost slots whose parents include k. */
+__device__ __forceinline__ void row_reg_chunk(const RowRegBuf &B, const float *tabsT, const float *De, float psc,
+                                              bool pres_live, int np, int lane, int k, int kc, float tmp[9])
+{
+  for (int pc = 0; pc < np; pc++) {
+    const int *rc = B.rec + kRowRec * pc;
+    const int a = rc[0] >> 27, info = rc[1], cs = rc[2];
+    const int nen = info & 0xff;
+    const float *tabT = tabsT + (info >> 8) * 16 * kRowPad;
+    const float *wT = B.wT + 9 * kRowPad * pc;
+    const unsigned *slot = reinterpret_cast<const unsigned *>(rc + 4);
+    const int b = B.inv[64 * pc + kc];
+    if (b != 255) {
+      float n[5];
+      load5(tabT + kRowPad * b, n);
+      row_reg_block(wT, n, tmp);
+      const int cslot0 = cs & 31, cslot1 = (cs >> 5) & 31, cslot2 = (cs >> 10) & 31;
+      if (pres_live && (a == cslot0 || a == cslot1 || a == cslot2)) {
+        const int kcr = b == cslot0 ? 0 : (b == cslot1 ? 1 : (b == cslot2 ? 2 : -1));
+        if (kcr >= 0) {
+          const float *vv = De + (size_t)kDeStride * (rc[0] & ((1 << 27) - 1)) + kDePres + 3 * kcr;
+#pragma unroll
+          for (int q = 0; q < 9; q++) tmp[q] += skew_entry(q / 3, q % 3, vv, psc);
+        }
+      }
+    }
+    /* ghost slots, in slot order: the owners of the three parents add +, +, - */
+    const bool ghost_lane = lane < nen && (slot[lane] & kRowSlotGhost);
+    for (unsigned gm = __ballot_sync(0xffffffffu, ghost_lane); gm; gm &= gm - 1) {
+      const int gb = __ffs(gm) - 1;
+      const unsigned sl = slot[gb];
+      const int pos0 = (int)(sl & 1023u), pos1 = (int)((sl >> 10) & 1023u), pos2 = (int)((sl >> 20) & 1023u);
+      if (k == pos0 || k == pos1 || k == pos2) {
+        float n[5], v[9];
+        load5(tabT + kRowPad * gb, n);
+#pragma unroll
+        for (int q = 0; q < 9; q++) v[q] = 0.f;
+        row_reg_block(wT, n, v);
+        const float sg = k == pos2 ? -1.f : 1.f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) tmp[q] = fmaf(sg, v[q], tmp[q]);
+      }
+    }
+  }
 }
 
 __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh m, KParams p, const float *__restrict__ De,
@@ -848,7 +900,6 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
     return;
   }
   for (int t = lane; t < nb; t += 32) B.cols[t] = m.colind[k0 + t];
-  __syncwarp();
   /* the two w entries of this lane: t0 = lane, t1 = lane + 32 (< 45) */
   const int wi0 = lane / 15, wk0 = lane - 15 * wi0;
   const int wpos0 = kRowPad * (3 * wi0 + wk0 % 3) + wk0 / 3, wd0 = wi0 * 15 + wk0;
@@ -856,114 +907,113 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
   const int wpos1 = kRowPad * (3 * wi1 + wk1 % 3) + wk1 / 3, wd1 = wi1 * 15 + wk1;
   const bool has1 = t1 < 45;
   const bool pres_live = p.pressure != 0.0 && !p.pres_dead;
-  const int pd = row_find(B.cols, nb, i);
+  const bool two = nb > 32;
   const double fmax = __longlong_as_double((long long)*m.fmax);
-  for (int base = 0; base < nb; base += 32) {
-    float acc[9], tmp[9];
+  float acc[9], tmp[9];
 #pragma unroll
-    for (int q = 0; q < 9; q++) { acc[q] = 0.f; B.comp[32 * q + lane] = 0.f; }
-    const int k = base + lane;
-    const int c1 = m.rptr[i + 1];
-    int4 nrec = row_rec_load(m.rrec, m.rptr[i], c1, lane);
-    for (int cb = m.rptr[i]; cb < c1; cb += kRowChunk) {
-      const int np = min(kRowChunk, c1 - cb);
-      if (lane < (kRowRec / 4) * np) reinterpret_cast<int4 *>(B.rec)[lane] = nrec;
-      nrec = row_rec_load(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
-      for (int u = lane; u < kRowChunk * 8; u += 32) reinterpret_cast<unsigned *>(B.inv)[u] = 0xffffffffu;
-      __syncwarp();
-      /* inverse map: owned block -> real slot (lane u -> contribution u / 16, slot u % 16) */
-      for (int u = lane; u < 16 * np; u += 32) {
-        const int pc = u >> 4, b = u & 15;
-        const int *rc = B.rec + kRowRec * pc;
-        const unsigned sl = (unsigned)rc[4 + b];
-        if (b < (rc[1] & 0xff) && !(sl & kRowSlotGhost) && sl >= (unsigned)base && sl < (unsigned)base + 32)
-          B.inv[32 * pc + sl - base] = (unsigned char)b;
-      }
-      for (int pc = 0; pc < np; pc++) {
-        const int *rc = B.rec + kRowRec * pc;
-        const int e = rc[0] & ((1 << 27) - 1), a = rc[0] >> 27, info = rc[1];
-        const float *D = De + (size_t)kDeStride * e;
-        float n[5];
-        load5(tabsT + (info >> 8) * 16 * kRowPad + kRowPad * a, n);
-        float v0 = 0.f, v1 = 0.f;
-#pragma unroll
-        for (int r = 0; r < 5; r++) v0 = fmaf(n[r], __ldg(D + 45 * r + wd0), v0);
-        B.wT[9 * kRowPad * pc + wpos0] = v0;
-        if (has1) {
-#pragma unroll
-          for (int r = 0; r < 5; r++) v1 = fmaf(n[r], __ldg(D + 45 * r + wd1), v1);
-          B.wT[9 * kRowPad * pc + wpos1] = v1;
+  for (int q = 0; q < 9; q++) {
+    acc[q] = 0.f;
+    B.comp[32 * q + lane] = 0.f;
+    B.acc1[9 * lane + q] = 0.f;
+    B.comp1[9 * lane + q] = 0.f;
+  }
+  __syncwarp();
+  const int pd = row_find(B.cols, nb, i);
+  const int c1 = m.rptr[i + 1];
+  int4 nrec = row_rec_load(m.rrec, m.rptr[i], c1, lane);
+  for (int cb = m.rptr[i]; cb < c1; cb += kRowChunk) {
+    const int np = min(kRowChunk, c1 - cb);
+    if (lane < (kRowRec / 4) * np) reinterpret_cast<int4 *>(B.rec)[lane] = nrec;
+    nrec = row_rec_load(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
+    for (int u = lane; u < kRowChunk * 16; u += 32) reinterpret_cast<unsigned *>(B.inv)[u] = 0xffffffffu;
+    __syncwarp();
+    /* inverse map: owned block -> real slot (lane u -> contribution u / 16, slot u % 16);
+       hi: the chunk reaches a block from 32 on (a real slot or a ghost's parent) */
+    bool hi = false;
+    for (int u = lane; u < 16 * np; u += 32) {
+      const int pc = u >> 4, b = u & 15;
+      const int *rc = B.rec + kRowRec * pc;
+      const unsigned sl = (unsigned)rc[4 + b];
+      if (b < (rc[1] & 0xff)) {
+        if (!(sl & kRowSlotGhost)) {
+          B.inv[64 * pc + sl] = (unsigned char)b;
+          hi |= sl >= 32u;
+        } else {
+          hi |= (sl & 1023u) >= 32u || ((sl >> 10) & 1023u) >= 32u || ((sl >> 20) & 1023u) >= 32u;
         }
       }
-      __syncwarp();
+    }
+    hi = __any_sync(0xffffffffu, hi);
+    for (int pc = 0; pc < np; pc++) {
+      const int *rc = B.rec + kRowRec * pc;
+      const int e = rc[0] & ((1 << 27) - 1), a = rc[0] >> 27, info = rc[1];
+      const float *D = De + (size_t)kDeStride * e;
+      float n[5];
+      load5(tabsT + (info >> 8) * 16 * kRowPad + kRowPad * a, n);
+      float v0 = 0.f, v1 = 0.f;
+#pragma unroll
+      for (int r = 0; r < 5; r++) v0 = fmaf(n[r], __ldg(D + 45 * r + wd0), v0);
+      B.wT[9 * kRowPad * pc + wpos0] = v0;
+      if (has1) {
+#pragma unroll
+        for (int r = 0; r < 5; r++) v1 = fmaf(n[r], __ldg(D + 45 * r + wd1), v1);
+        B.wT[9 * kRowPad * pc + wpos1] = v1;
+      }
+    }
+    __syncwarp();
+    /* h = 0: blocks 0..31, compensated into acc (registers); h = 1: blocks
+       32..63, into acc1 (each lane's own shared-memory column) */
+    for (int h = 0; h < (hi ? 2 : 1); h++) {
 #pragma unroll
       for (int q = 0; q < 9; q++) tmp[q] = 0.f;
-      for (int pc = 0; pc < np; pc++) {
-        const int *rc = B.rec + kRowRec * pc;
-        const int a = rc[0] >> 27, info = rc[1], cs = rc[2];
-        const int nen = info & 0xff;
-        const float *tabT = tabsT + (info >> 8) * 16 * kRowPad;
-        const float *wT = B.wT + 9 * kRowPad * pc;
-        const unsigned *slot = reinterpret_cast<const unsigned *>(rc + 4);
-        const int b = B.inv[32 * pc + lane];
-        if (b != 255) {
-          float n[5];
-          load5(tabT + kRowPad * b, n);
-          row_reg_block(wT, n, tmp);
-          const int cslot0 = cs & 31, cslot1 = (cs >> 5) & 31, cslot2 = (cs >> 10) & 31;
-          if (pres_live && (a == cslot0 || a == cslot1 || a == cslot2)) {
-            const int kc = b == cslot0 ? 0 : (b == cslot1 ? 1 : (b == cslot2 ? 2 : -1));
-            if (kc >= 0) {
-              const float *vv = De + (size_t)kDeStride * (rc[0] & ((1 << 27) - 1)) + kDePres + 3 * kc;
+      row_reg_chunk(B, tabsT, De, psc, pres_live, np, lane, 32 * h + lane, 32 * h + lane, tmp);
+      if (h == 0) {
 #pragma unroll
-              for (int q = 0; q < 9; q++) tmp[q] += skew_entry(q / 3, q % 3, vv, psc);
-            }
-          }
+        for (int q = 0; q < 9; q++) {
+          const float y = tmp[q] - B.comp[32 * q + lane];
+          const float t = acc[q] + y;
+          B.comp[32 * q + lane] = (t - acc[q]) - y;
+          acc[q] = t;
         }
-        /* ghost slots, in slot order: the owners of the three parents add +, +, - */
-        const bool ghost_lane = lane < nen && (slot[lane] & kRowSlotGhost);
-        for (unsigned gm = __ballot_sync(0xffffffffu, ghost_lane); gm; gm &= gm - 1) {
-          const int gb = __ffs(gm) - 1;
-          const unsigned sl = slot[gb];
-          const int pos0 = (int)(sl & 1023u), pos1 = (int)((sl >> 10) & 1023u), pos2 = (int)((sl >> 20) & 1023u);
-          if (k == pos0 || k == pos1 || k == pos2) {
-            float n[5], v[9];
-            load5(tabT + kRowPad * gb, n);
+      } else {
 #pragma unroll
-            for (int q = 0; q < 9; q++) v[q] = 0.f;
-            row_reg_block(wT, n, v);
-            const float sg = k == pos2 ? -1.f : 1.f;
-#pragma unroll
-            for (int q = 0; q < 9; q++) tmp[q] = fmaf(sg, v[q], tmp[q]);
-          }
+        for (int q = 0; q < 9; q++) {
+          const float s = B.acc1[9 * lane + q];
+          const float y = tmp[q] - B.comp1[9 * lane + q];
+          const float t = s + y;
+          B.comp1[9 * lane + q] = (t - s) - y;
+          B.acc1[9 * lane + q] = t;
         }
       }
-      /* the chunk's partial sums into the row, compensated (each lane keeps its
-         own compensations; no other lane touches them) */
-#pragma unroll
-      for (int q = 0; q < 9; q++) {
-        const float y = tmp[q] - B.comp[32 * q + lane];
-        const float t = acc[q] + y;
-        B.comp[32 * q + lane] = (t - acc[q]) - y;
-        acc[q] = t;
-      }
-      __syncwarp();   /* records, inverse map and wT are rewritten by the next chunk */
     }
-    /* dynamic term diagonal, scale, write-out staged through shared memory */
-    if (k < nb) {
+    __syncwarp();   /* records, inverse map and wT are rewritten by the next chunk */
+  }
+  /* dynamic term diagonal, scale, block layout; blocks 32.. are written first
+     (from acc1, in place), then acc1 stages blocks 0..31 */
+  auto finish = [&](float v, int k, int q) {
+    if (p.dyn && k == pd && (q == 0 || q == 4 || q == 8)) v += (float)m.dyn_diag[i];
+    if (fmax > 1.0) v = (float)((double)v * (1.0 / fmax));
+    return v;
+  };
+  if (two) {
+    if (32 + lane < nb) {
+      float v[9];
 #pragma unroll
-      for (int q = 0; q < 9; q++) {
-        float v = acc[q];
-        if (p.dyn && k == pd && (q == 0 || q == 4 || q == 8)) v += (float)m.dyn_diag[i];
-        if (fmax > 1.0) v = (float)((double)v * (1.0 / fmax));
-        B.stage[9 * lane + (colmajor ? 3 * (q % 3) + q / 3 : q)] = v;
-      }
+      for (int q = 0; q < 9; q++) v[q] = finish(B.acc1[9 * lane + q], 32 + lane, q);
+#pragma unroll
+      for (int q = 0; q < 9; q++) B.acc1[9 * lane + (colmajor ? 3 * (q % 3) + q / 3 : q)] = v[q];
     }
     __syncwarp();
-    const int nw = 9 * min(32, nb - base);
-    for (int t = lane; t < nw; t += 32) Kr[9 * base + t] = B.stage[t];
+    for (int t = lane; t < 9 * (nb - 32); t += 32) Kr[9 * 32 + t] = B.acc1[t];
     __syncwarp();
   }
+  if (lane < nb) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) B.acc1[9 * lane + (colmajor ? 3 * (q % 3) + q / 3 : q)] = finish(acc[q], lane, q);
+  }
+  __syncwarp();
+  const int nw = 9 * min(32, nb);
+  for (int t = lane; t < nw; t += 32) Kr[t] = B.acc1[t];
 }
 
 /* Row-assembly records (see DevMesh::rrec), built on the device once per
