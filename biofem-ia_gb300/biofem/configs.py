@@ -157,7 +157,10 @@ class ConeWorkload:
 class SphereWorkload:
     """A closed surface (mesh.closed_sphere): no boundary ring, so no ghost
     nodes and no clamp; internal follower pressure, fibres along the local
-    east direction, a seeded displacement of 1e-2 of the mean edge."""
+    east direction, a seeded displacement of 1e-2 of the mean edge.  With
+    ``drop`` the listed triangles are removed: holes whose rims are not
+    declared as rings, so the patches there repeat a node (the reference's
+    stencil fill-in, bending.c:1637-1650)."""
     name: str
     freq: int
     index: int = 0
@@ -171,6 +174,7 @@ class SphereWorkload:
     tnormal: int = 0
     dead_load: int = 0
     iso_act: int = 0
+    drop: tuple = ()       # triangles removed: holes whose rims are no boundary ring
 
     @property
     def seed(self) -> int:
@@ -178,6 +182,11 @@ class SphereWorkload:
 
     def build_mesh(self) -> meshmod.Mesh:
         m = meshmod.closed_sphere(self.freq, self.seed, jitter=self.jitter, lambda_a=self.lambda_a)
+        if self.drop:
+            keep = np.ones(m.n_elmt, bool)
+            keep[list(self.drop)] = False
+            m.tri, m.fib, m.gamma_scale = m.tri[keep], m.fib[keep], m.gamma_scale[keep]
+            m.meta["drop"] = list(self.drop)
         m.meta["workload"] = self.name
         return m
 

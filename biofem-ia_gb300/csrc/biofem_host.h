@@ -27,6 +27,9 @@ constexpr int kDePres = 225;      /* then the three follower-pressure corner vec
 constexpr int kMaxRowBlocks = 1023;   /* tangent blocks per row the row assembly handles (10-bit slot targets) */
 constexpr int kRowRec = 20;           /* ints per row-assembly record (80 bytes, 16-byte aligned) */
 constexpr unsigned kRowSlotGhost = 1u << 31;   /* record slot target of a ghost slot: three packed parents */
+constexpr unsigned kRowSlotDup = 1u << 30;     /* with kRowSlotGhost: a slot repeating an earlier slot's real node
+                                                  (an open boundary that is no ring); its target in the first two
+                                                  10-bit fields, 1023 (no block) in the third */
 
 /* Topology in IBMNodes layout (see topology.cpp). */
 struct HostTopo {

@@ -628,12 +628,13 @@ __device__ __forceinline__ RowAsmBuf<R> row_buf(unsigned char *base, int maxblk)
   return b;
 }
 
-/* The records of the contributions [cb, cb + kRowChunk) of a row ending at
-   c1, one 16-byte piece per lane (lanes < 5 np); zero past the row. */
-static_assert(kRowRec % 4 == 0 && (kRowRec / 4) * kRowChunk <= 32, "a chunk's records must fit one piece per lane");
+/* The records of the contributions [cb, cb + CH) of a row ending at c1, one
+   16-byte piece per lane (lanes < 5 np); zero past the row. */
+template <int CH>
 __device__ __forceinline__ int4 row_rec_load(const int *rrec, int cb, int c1, int lane)
 {
-  const int np = min(kRowChunk, c1 - cb);
+  static_assert(kRowRec % 4 == 0 && (kRowRec / 4) * CH <= 32, "a chunk's records must fit one piece per lane");
+  const int np = min(CH, c1 - cb);
   if (np <= 0 || lane >= (kRowRec / 4) * np) return make_int4(0, 0, 0, 0);
   return __ldg(reinterpret_cast<const int4 *>(rrec) + (size_t)(kRowRec / 4) * cb + lane);
 }
@@ -660,7 +661,9 @@ __device__ __forceinline__ void row_add(R *acc, R *comp, int idx, R v)
    values are fused into the block accumulator (acc + sum_s N[s][b] wT[q][s]
    as one FMA chain), FP32 values are formed alone and added with Kahan
    compensation; a ghost slot's values go to its parents after the real
-   slots, in slot order. */
+   slots, in slot order, and so do a repeated real node's (a patch at an open
+   boundary that is no ring holds some node twice: kRowSlotDup, one target),
+   so that no two lanes add into one block at once. */
 template <class R>
 __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KParams p, const R *__restrict__ De,
                                                                  const R *__restrict__ ntab, R psc, R *__restrict__ K,
@@ -695,11 +698,11 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
   }
   const bool pres_live = p.pressure != 0.0 && !p.pres_dead;
   const int c1 = m.rptr[i + 1];
-  int4 nrec = row_rec_load(m.rrec, m.rptr[i], c1, lane);
+  int4 nrec = row_rec_load<kRowChunk>(m.rrec, m.rptr[i], c1, lane);
   for (int cb = m.rptr[i]; cb < c1; cb += kRowChunk) {
     const int np = min(kRowChunk, c1 - cb);
     if (lane < (kRowRec / 4) * np) reinterpret_cast<int4 *>(B.rec)[lane] = nrec;
-    nrec = row_rec_load(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
+    nrec = row_rec_load<kRowChunk>(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
     __syncwarp();   /* also orders the cols / acc set-up and the previous chunk's reads */
     /* w of the chunk: lane u -> contribution u / 45, entry u % 45 */
     for (int u = lane; u < 45 * np; u += 32) {
@@ -743,7 +746,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
         /* ghost slots, in slot order: lane 9k + q adds to entry q of parent k */
         for (unsigned gm = gmask; gm; gm &= gm - 1) {
           const int b = __ffs(gm) - 1;
-          if (lane < 27) {
+          if (lane < ((slot[b] & kRowSlotDup) ? 9 : 27)) {   /* a repeated real node has one target */
             const int k = lane / 9, q = lane - 9 * k;
             const int pos = (int)((slot[b] >> (10 * k)) & 1023u);
             const R v = B.gv[9 * b + q];
@@ -780,7 +783,8 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_row_assemble(DevMesh m, KPar
    entries), then each owned block's values formed by its owner lane (N[.][b]
    from the table, the 9 x 5 values of w read by every lane at once) and fused
    into a per-chunk partial sum; a ghost slot's values go to the lanes owning
-   its parents, after the real slots, in slot order.  The partial sums are
+   its parents, after the real slots, in slot order, and so do those of a
+   slot repeating an earlier slot's real node (kRowSlotDup, one owner).  The partial sums are
    added into the row with Kahan compensation once per chunk, in element
    order; the second 32 blocks' pass is skipped for a chunk that touches none
    of them. */
@@ -861,7 +865,7 @@ __device__ __forceinline__ void row_reg_chunk(const RowRegBuf &B, const float *t
       const int gb = __ffs(gm) - 1;
       const unsigned sl = slot[gb];
       const int pos0 = (int)(sl & 1023u), pos1 = (int)((sl >> 10) & 1023u), pos2 = (int)((sl >> 20) & 1023u);
-      if (k == pos0 || k == pos1 || k == pos2) {
+      if (k == pos0 || k == pos1 || k == pos2) {   /* a repeated real node: pos0 = pos1, pos2 none */
         float n[5], v[9];
         load5(tabT + kRowPad * gb, n);
 #pragma unroll
@@ -920,11 +924,11 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
   __syncwarp();
   const int pd = row_find(B.cols, nb, i);
   const int c1 = m.rptr[i + 1];
-  int4 nrec = row_rec_load(m.rrec, m.rptr[i], c1, lane);
+  int4 nrec = row_rec_load<kRowChunk>(m.rrec, m.rptr[i], c1, lane);
   for (int cb = m.rptr[i]; cb < c1; cb += kRowChunk) {
     const int np = min(kRowChunk, c1 - cb);
     if (lane < (kRowRec / 4) * np) reinterpret_cast<int4 *>(B.rec)[lane] = nrec;
-    nrec = row_rec_load(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
+    nrec = row_rec_load<kRowChunk>(m.rrec, cb + kRowChunk, c1, lane);   /* the next chunk's, in flight meanwhile */
     for (int u = lane; u < kRowChunk * 16; u += 32) reinterpret_cast<unsigned *>(B.inv)[u] = 0xffffffffu;
     __syncwarp();
     /* inverse map: owned block -> real slot (lane u -> contribution u / 16, slot u % 16);
@@ -939,7 +943,8 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
           B.inv[64 * pc + sl] = (unsigned char)b;
           hi |= sl >= 32u;
         } else {
-          hi |= (sl & 1023u) >= 32u || ((sl >> 10) & 1023u) >= 32u || ((sl >> 20) & 1023u) >= 32u;
+          hi |= (sl & 1023u) >= 32u ||
+                (!(sl & kRowSlotDup) && (((sl >> 10) & 1023u) >= 32u || ((sl >> 20) & 1023u) >= 32u));
         }
       }
     }
@@ -1020,7 +1025,9 @@ __global__ void __launch_bounds__(32 * kRowWarps, 8) k_row_assemble_f32(DevMesh 
    mesh: one warp per row, lanes over (contribution, patch slot); the slot's
    target is its node's position in the row's sorted columns (a lower-bound
    search), a ghost slot packs its parents nv2, nv1, nv3 at 10 bits each with
-   kRowSlotGhost.  Rows with an identity block get zero records. */
+   kRowSlotGhost, and a slot repeating an earlier slot's real node is marked
+   kRowSlotGhost | kRowSlotDup with its one target (it then takes the ghost
+   slots' serial path).  Rows with an identity block get zero records. */
 __device__ __forceinline__ unsigned col_lower_bound(const int *cols, int nb, int node)
 {
   int lo = 0, hi = nb;
@@ -1054,9 +1061,12 @@ __global__ void k_row_records(DevMesh m, KParams p, int *__restrict__ rrec)
     }
     unsigned sl = 0;
     if (live && b < nen) {
-      const int node = m.patch[16 * (size_t)e + b];
+      const int *pe = m.patch + 16 * (size_t)e;
+      const int node = pe[b];
       if (node < p.nv) {
         sl = col_lower_bound(cols, nb, node);
+        for (int b2 = 0; b2 < b; b2++)
+          if (pe[b2] == node) { sl |= kRowSlotGhost | kRowSlotDup | (sl << 10) | (1023u << 20); break; }
       } else {
         const int g = node - p.nv;
         sl = kRowSlotGhost | col_lower_bound(cols, nb, m.ghost3[3 * g + 1]) |

@@ -26,7 +26,9 @@ def pair(w):
 
 
 @pytest.mark.parametrize("w", [configs.C1, configs.small(12, 9, activation="random", index=70, pressure=1e-3),
-                               configs.cone(10), configs.capped(12, 6, True), configs.C2], ids=lambda w: w.name)
+                               configs.cone(10), configs.capped(12, 6, True),
+                               configs.SphereWorkload("sphere_f4_holed", 4, index=72, drop=(5, 200)), configs.C2],
+                         ids=lambda w: w.name)
 def test_fp32_bulk_tangent_error(w, oracle_lib):
     m, s64, s32 = pair(w)
     t = s64.topology()

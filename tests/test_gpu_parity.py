@@ -88,6 +88,7 @@ def test_residual_is_deterministic():
                                 configs.SphereWorkload("sphere_f6", 6, index=71),
                                 configs.capped(10, 5), configs.capped(12, 6, True, clamp=True, n_qp=4),
                                 configs.capped(16, 8, True, pressure=2e-3),
+                                configs.SphereWorkload("sphere_f4_holed", 4, index=72, drop=(5, 200)),
                                 configs.C1],
                          ids=lambda w: w.name + ("_exact" if w.basis else "") + ("_tnormal" if w.tnormal else "")
                          + ("_dead" if w.dead_load else "") + ("_iso" if w.iso_act else ""))

@@ -89,6 +89,24 @@ def test_oracle_matches_live_reference_capped(apex_vertex, oracle_lib):
     assert np.abs(R.reshape(-1, 3)[cap_nodes]).max() > 0.0
 
 
+def test_oracle_matches_live_reference_holed_sphere(oracle_lib):
+    """Holes not declared as rings (stencils that repeat a node), against the
+    live reference build."""
+    from oracle import build_ref
+    if not build_ref.available():
+        pytest.skip("reference sources not on this host")
+    from oracle.pyoracle import RefOracle
+    w = configs.SphereWorkload("sphere_f4_holed", 4, index=72, drop=(5, 200))
+    m = w.build_mesh()
+    ref = RefOracle().setup(m, w, configs.MU, configs.BULK, configs.H0)
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0)
+    tr, to = ref.topology(), o.topology()
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        assert np.array_equal(getattr(tr, k), getattr(to, k)), k
+    x = w.initial_x(m, tr.xyz0_full)
+    assert np.array_equal(ref.residual(x), o.residual(x))
+
+
 def test_oracle_jvp_matches_central_differences(oracle_lib):
     """The dual-number directional derivative is the tangent checker; it must
     agree with central differences of the (bitwise-pinned) residual."""

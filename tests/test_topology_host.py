@@ -119,6 +119,24 @@ def test_host_topology_equals_oracle_capped(n_phi, n_theta, apex_vertex, oracle_
     assert ((g3 >= n_phi) & (g3 < 2 * n_phi)).all()
 
 
+def test_host_topology_equals_oracle_holed_sphere(oracle_lib):
+    """Holes whose rims are no boundary ring: the reference's stencil fill-in
+    repeats a node in some patches (the row assembly then takes those slots
+    one at a time)."""
+    w = configs.SphereWorkload("sphere_f4_holed", 4, index=72, drop=(5, 200))
+    m = w.build_mesh()
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, host_only=True)
+    t = sh.topology()
+    sh.close()
+    o = oracle_lib.setup(m, w, configs.MU, configs.BULK, configs.H0).topology()
+    for k in ("patch", "ire", "val", "irv", "gtri", "xyz0_full", "dA0"):
+        np.testing.assert_array_equal(np.asarray(t[k]).reshape(np.asarray(getattr(o, k)).shape), getattr(o, k),
+                                      err_msg=k)
+    P = np.asarray(t["patch"]).reshape(-1, 16)
+    nen = np.where(np.asarray(t["ire"]) == 0, 12, np.asarray(t["val"]) + 6)
+    assert sum(len(set(P[e, :nen[e]])) < nen[e] for e in range(len(P))) > 0
+
+
 @pytest.mark.parametrize("name", ["C2_flat_256x192", "C4_lv_ellipsoid"])
 def test_host_topology_matches_reference_checksum(name):
     """C2 (98,304 triangles) and C4 (200,614 triangles, valence-5/7 vertices):
