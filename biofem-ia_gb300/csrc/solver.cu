@@ -11,9 +11,10 @@
  *             kept), preconditioned by smoothed-aggregation multigrid (FP32
  *             V-cycle, amg.cu) or by block-Jacobi(3x3); classical
  *             Gram-Schmidt applied twice, Givens rotations and the small
- *             triangular solve on the device; all Krylov vectors, the BSR
- *             matvec and the dot products in FP64 (the tangent values may be
- *             FP32 for an FP32-bulk handle).  One iteration: preconditioner,
+ *             triangular solve on the device; all Krylov vectors and the
+ *             dot products in FP64; the BSR matvec in FP64, or, with the FP32
+ *             tangent of an FP32-bulk handle, in float-float arithmetic on
+ *             the FP32 pipe (about 47 bits, against K's own 24).  One iteration: preconditioner,
  *             matvec, two projection passes (dot products with an in-kernel
  *             deterministic reduction, the second also doing the Givens
  *             step), and two updates.
@@ -30,6 +31,7 @@
 
 #include "amg.h"
 #include "biofem_host.h"
+#include "ff.cuh"
 
 namespace biofem {
 
@@ -70,6 +72,52 @@ __global__ void k_bsr_matvec(int nb, const int *__restrict__ rowptr, const int *
     s2 += __shfl_xor_sync(0xffffffffu, s2, o);
   }
   if (row < nb && q == 0) { y[3 * (size_t)row] = s0; y[3 * (size_t)row + 1] = s1; y[3 * (size_t)row + 2] = s2; }
+}
+
+/* y = K x for FP32 K and FP64 x on the FP32 pipe: x is split into float
+   pairs (hi + lo, bit operations), each product K hi is formed exactly
+   (two-product) and summed into a float-float accumulator with two-sum, K lo
+   goes to its low part; the half-warp's partial sums are combined as
+   float-float and widened to FP64 at the end.  About 47 significant bits
+   (K itself carries 24); GB300's FP64 pipe runs at 1/64 of the FP32 rate. */
+__device__ __forceinline__ void ff_axpy(FF &s, float a, FF x)
+{
+  const FF p = ff_two_prod(a, x.hi);
+  FF t = ff_two_sum(s.hi, p.hi);
+  t.lo += fmaf(a, x.lo, s.lo + p.lo);
+  s = ff_fast_two_sum(t.hi, t.lo);
+}
+
+__global__ void k_bsr_matvec_ff(int nb, const int *__restrict__ rowptr, const int *__restrict__ colind,
+                                const float *__restrict__ K, const double *__restrict__ x, double *__restrict__ y,
+                                const GmState *__restrict__ gs)
+{
+  if (gs && gm_done(gs)) return;
+  /* one half-warp per block row, lane q taking whole blocks q, q + 16, ... */
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = t >> 4, q = t & 15;
+  FF s0(0.f, 0.f), s1(0.f, 0.f), s2(0.f, 0.f);
+  if (row < nb) {
+    const int k1 = rowptr[row + 1];
+    for (int k = rowptr[row] + q; k < k1; k += 16) {
+      const int c = colind[k];
+      const float *b = K + 9 * (size_t)k;
+      const FF x0 = ff_split(x[3 * (size_t)c]), x1 = ff_split(x[3 * (size_t)c + 1]), x2 = ff_split(x[3 * (size_t)c + 2]);
+      ff_axpy(s0, b[0], x0); ff_axpy(s0, b[1], x1); ff_axpy(s0, b[2], x2);
+      ff_axpy(s1, b[3], x0); ff_axpy(s1, b[4], x1); ff_axpy(s1, b[5], x2);
+      ff_axpy(s2, b[6], x0); ff_axpy(s2, b[7], x1); ff_axpy(s2, b[8], x2);
+    }
+  }
+  for (int o = 1; o < 16; o <<= 1) {
+    s0 = s0 + FF(__shfl_xor_sync(0xffffffffu, s0.hi, o), __shfl_xor_sync(0xffffffffu, s0.lo, o));
+    s1 = s1 + FF(__shfl_xor_sync(0xffffffffu, s1.hi, o), __shfl_xor_sync(0xffffffffu, s1.lo, o));
+    s2 = s2 + FF(__shfl_xor_sync(0xffffffffu, s2.hi, o), __shfl_xor_sync(0xffffffffu, s2.lo, o));
+  }
+  if (row < nb && q == 0) {
+    y[3 * (size_t)row] = ff_to_double_bits(s0);
+    y[3 * (size_t)row + 1] = ff_to_double_bits(s1);
+    y[3 * (size_t)row + 2] = ff_to_double_bits(s2);
+  }
 }
 
 /* inverse of every diagonal block (block-Jacobi) */
@@ -447,7 +495,7 @@ class Gmres {
 
   void matvec(const double *x, double *y, const GmState *gs)
   {
-    if (f32_) k_bsr_matvec<float><<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, x, y, gs);
+    if (f32_) k_bsr_matvec_ff<<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, x, y, gs);
     else k_bsr_matvec<double><<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const double *)K_, x, y, gs);
   }
   /* z = M^-1 r: smoothed-aggregation V-cycle, or block-Jacobi */
