@@ -90,20 +90,23 @@ def test_eisenstat_walker_forcing_reaches_the_same_root():
     sh.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32_bulk"])
 @pytest.mark.parametrize("pc", [0, 1], ids=["multigrid", "bjacobi"])
-def test_device_gmres_step_matches_scipy_gmres(pc):
+def test_device_gmres_step_matches_scipy_gmres(pc, precision):
     """The device Krylov solve against scipy's gmres, the stand-in for PETSc
     KSP: one Newton step without line search, linear tolerance 1e-11, solves
     the system scipy's gmres (block-Jacobi(3x3) preconditioned, same
-    tolerance) solves on the same assembled tangent and residual."""
+    tolerance) solves on the same assembled tangent and residual.  With an
+    FP32-bulk handle the tangent is its FP32 K and the device solve runs its
+    matvec and projections in float-float arithmetic."""
     import scipy.sparse.linalg as spla
     from biofem.gpu import GpuShell
     w = configs.Workload("flat_40x30", 40, 30, z_sigma=1e-3, activation="smooth", index=83, pressure=3e-4)
     m = w.build_mesh()
-    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0)
+    sh = GpuShell(m, w, configs.MU, configs.BULK, configs.H0, precision=precision)
     x0 = w.initial_x(m, sh.topology()["xyz0_full"])
     R, K = sh.form_jacobian(x0)
-    A = sh.to_scipy(K).tocsr()
+    A = sh.to_scipy(K.astype(np.float64)).tocsr()
     nb = A.shape[0] // 3
     blocks = np.array([np.linalg.inv(A[3 * i:3 * i + 3, 3 * i:3 * i + 3].toarray()) for i in range(nb)])
     M = spla.LinearOperator(A.shape, matvec=lambda v: np.einsum("bij,bj->bi", blocks, v.reshape(-1, 3)).ravel())
