@@ -74,8 +74,19 @@ __global__ void k_bsr_matvec(int nb, const int *__restrict__ rowptr, const int *
   if (row < nb && q == 0) { y[3 * (size_t)row] = s0; y[3 * (size_t)row + 1] = s1; y[3 * (size_t)row + 2] = s2; }
 }
 
-/* y = K x for FP32 K and FP64 x on the FP32 pipe: x is split into float
-   pairs (hi + lo, bit operations), each product K hi is formed exactly
+/* x as float pairs hi + lo (bit operations), once per matvec: every column
+   is read by ~36 block rows */
+__global__ void k_split_ff(int n, const double *__restrict__ x, float2 *__restrict__ xs, const GmState *__restrict__ gs)
+{
+  if (gs && gm_done(gs)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const FF f = ff_split(x[i]);
+  xs[i] = make_float2(f.hi, f.lo);
+}
+
+/* y = K x for FP32 K and FP64 x on the FP32 pipe: x comes split into float
+   pairs (hi + lo, k_split_ff), each product K hi is formed exactly
    (two-product) and summed into a float-float accumulator with two-sum, K lo
    goes to its low part; the half-warp's partial sums are combined as
    float-float and widened to FP64 at the end.  About 47 significant bits
@@ -89,7 +100,7 @@ __device__ __forceinline__ void ff_axpy(FF &s, float a, FF x)
 }
 
 __global__ void k_bsr_matvec_ff(int nb, const int *__restrict__ rowptr, const int *__restrict__ colind,
-                                const float *__restrict__ K, const double *__restrict__ x, double *__restrict__ y,
+                                const float *__restrict__ K, const float2 *__restrict__ xs, double *__restrict__ y,
                                 const GmState *__restrict__ gs)
 {
   if (gs && gm_done(gs)) return;
@@ -102,7 +113,8 @@ __global__ void k_bsr_matvec_ff(int nb, const int *__restrict__ rowptr, const in
     for (int k = rowptr[row] + q; k < k1; k += 16) {
       const int c = colind[k];
       const float *b = K + 9 * (size_t)k;
-      const FF x0 = ff_split(x[3 * (size_t)c]), x1 = ff_split(x[3 * (size_t)c + 1]), x2 = ff_split(x[3 * (size_t)c + 2]);
+      const float2 p0 = xs[3 * (size_t)c], p1 = xs[3 * (size_t)c + 1], p2 = xs[3 * (size_t)c + 2];
+      const FF x0(p0.x, p0.y), x1(p1.x, p1.y), x2(p2.x, p2.y);
       ff_axpy(s0, b[0], x0); ff_axpy(s0, b[1], x1); ff_axpy(s0, b[2], x2);
       ff_axpy(s1, b[3], x0); ff_axpy(s1, b[4], x1); ff_axpy(s1, b[5], x2);
       ff_axpy(s2, b[6], x0); ff_axpy(s2, b[7], x1); ff_axpy(s2, b[8], x2);
@@ -495,7 +507,12 @@ class Gmres {
 
   void matvec(const double *x, double *y, const GmState *gs)
   {
-    if (f32_) k_bsr_matvec_ff<<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, x, y, gs);
+    if (f32_) {
+      /* the split x lives in the line search's trial vector, unused while GMRES runs */
+      float2 *xs = reinterpret_cast<float2 *>(w_.xt);
+      k_split_ff<<<nblk(w_.n, 256), 256, 0, st_>>>(w_.n, x, xs, gs);
+      k_bsr_matvec_ff<<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const float *)K_, xs, y, gs);
+    }
     else k_bsr_matvec<double><<<nblk(16LL * w_.nb, 256), 256, 0, st_>>>(w_.nb, dm_.rowptr, dm_.colind, (const double *)K_, x, y, gs);
   }
   /* z = M^-1 r: smoothed-aggregation V-cycle, or block-Jacobi */
