@@ -189,5 +189,16 @@ __host__ __device__ __forceinline__ double ff_widen(float f)
 /* hi + lo as a double: two exact widenings and one double addition. */
 __host__ __device__ __forceinline__ double ff_to_double_bits(FF a) { return ff_widen(a.hi) + ff_widen(a.lo); }
 
+/* s += a x for a float a and a float-float x: the head product a x.hi exact
+   (two-product), added to s.hi by two-sum; the tails and a x.lo go to the
+   low word (the accumulation of the float-float matvec). */
+__host__ __device__ __forceinline__ void ff_axpy(FF &s, float a, FF x)
+{
+  const FF p = ff_two_prod(a, x.hi);
+  FF t = ff_two_sum(s.hi, p.hi);
+  t.lo += fmaf(a, x.lo, s.lo + p.lo);
+  s = ff_fast_two_sum(t.hi, t.lo);
+}
+
 } /* namespace biofem */
 #endif

@@ -91,14 +91,6 @@ __global__ void k_split_ff(int n, const double *__restrict__ x, float2 *__restri
    goes to its low part; the half-warp's partial sums are combined as
    float-float and widened to FP64 at the end.  About 47 significant bits
    (K itself carries 24); GB300's FP64 pipe runs at 1/64 of the FP32 rate. */
-__device__ __forceinline__ void ff_axpy(FF &s, float a, FF x)
-{
-  const FF p = ff_two_prod(a, x.hi);
-  FF t = ff_two_sum(s.hi, p.hi);
-  t.lo += fmaf(a, x.lo, s.lo + p.lo);
-  s = ff_fast_two_sum(t.hi, t.lo);
-}
-
 __global__ void k_bsr_matvec_ff(int nb, const int *__restrict__ rowptr, const int *__restrict__ colind,
                                 const float *__restrict__ K, const float2 *__restrict__ xs, double *__restrict__ y,
                                 const GmState *__restrict__ gs)

@@ -64,7 +64,23 @@ int main()
   }
   const FF z = ff_split(0.0), nz = ff_split(-0.0);
   const bool zeros = z.hi == 0.f && z.lo == 0.f && nz.hi == 0.f && std::signbit(nz.hi) && ff_widen(0.f) == 0.0;
-  std::printf("%.3e %.3e %.3e %.3e %.3e %.3e %ld %ld %ld %d\n", e_add, e_cancel, e_mul, e_div, e_sqrt, e_split,
-              bad_norm, bad_widen, bad_todouble, zeros ? 1 : 0);
+  /* the float-float matvec's row sums: 324 terms (36 blocks x 9) of float K
+     values over four decades times split double x, accumulated by ff_axpy,
+     against long double, relative to sum |K x| */
+  double e_dot = 0.0;
+  for (int r = 0; r < 4000; r++) {
+    FF s(0.f, 0.f);
+    long double exact = 0.0L, mag = 0.0L;
+    for (int k = 0; k < 324; k++) {
+      const float a = (float)((urand() < 0.5 ? -1.0 : 1.0) * std::pow(10.0, -2.0 + 4.0 * urand()));
+      const double x = (urand() < 0.5 ? -1.0 : 1.0) * std::pow(10.0, -3.0 + 3.0 * urand());
+      ff_axpy(s, a, ff_split(x));
+      exact += (long double)a * (long double)x;
+      mag += std::fabs((long double)a * (long double)x);
+    }
+    e_dot = std::fmax(e_dot, (double)(std::fabs((long double)ff_to_double_bits(s) - exact) / mag));
+  }
+  std::printf("%.3e %.3e %.3e %.3e %.3e %.3e %ld %ld %ld %d %.3e\n", e_add, e_cancel, e_mul, e_div, e_sqrt, e_split,
+              bad_norm, bad_widen, bad_todouble, zeros ? 1 : 0, e_dot);
   return 0;
 }
